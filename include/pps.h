@@ -1,0 +1,174 @@
+/*
+ * pps.h -- C ABI of libpps_cuda.so, the GB300 (sm_103a) particle-swarm engine
+ * that sits below ParallelParticleSwarms.jl's solve/init/solve!/reinit! API.
+ *
+ * Conventions
+ *   - Every entry point returns a pps_status; on failure pps_last_error()
+ *     returns a message for the calling thread.  No exception or longjmp
+ *     crosses the ABI.
+ *   - Pointers are HOST pointers unless a name says otherwise; the library
+ *     owns every device allocation it makes.
+ *   - Arrays of particle data are structure-of-arrays, particle fastest:
+ *     element (particle i, dim d) of an n-particle array is at [d*n + i].
+ *     The reference keeps an array of SPSOParticle structs
+ *     (src/ParallelParticleSwarms.jl:34-40); the Julia glue converts at the
+ *     boundary.
+ *   - A pps_swarm handle owns one CUDA stream.  A handle is not thread-safe;
+ *     distinct handles may be used from distinct threads.
+ *   - All arithmetic is IEEE binary32 (the reference's Float32 problems).
+ */
+#ifndef PPS_H
+#define PPS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PPS_VERSION 100 /* 0.1.0 */
+
+#if defined(__GNUC__)
+#define PPS_API __attribute__((visibility("default")))
+#else
+#define PPS_API
+#endif
+
+typedef enum pps_status {
+  PPS_OK = 0,
+  PPS_EINVAL = 1,   /* bad argument (the reference raises ArgumentError / AssertionError) */
+  PPS_ENOMEM = 2,   /* device or host allocation failed */
+  PPS_ECUDA = 3,    /* a CUDA call failed */
+  PPS_ETIMEOUT = 4, /* a bounded device-side wait gave up */
+  PPS_EBUSY = 5,    /* result not ready yet */
+  PPS_ENOTSUP = 6,  /* valid request this build does not support */
+  PPS_ENODEV = 7    /* no usable CUDA device */
+} pps_status;
+
+/* Objective registry.  The reference compiles an arbitrary Julia closure
+ * into its kernels (src/kernels.jl:33); a C ABI cannot take a closure, so the
+ * engine evaluates a registered set selected by id with a float parameter
+ * vector (the reference's `p`). */
+typedef enum pps_objective {
+  PPS_OBJ_SPHERE = 0,     /* sum x_i^2 */
+  PPS_OBJ_ROSENBROCK = 1, /* sum_{i<D} p2 (x_{i+1}-x_i^2)^2 + (p1-x_i)^2; p=(p1,p2), default (1,100) */
+  PPS_OBJ_RASTRIGIN = 2,  /* A D + sum (x_i^2 - A cos 2 pi x_i); p=(A), default 10 */
+  PPS_OBJ_ACKLEY = 3,     /* -a exp(-b sqrt(mean x^2)) - exp(mean cos 2 pi k x) + a + e; p=(a,b,k) default (20,0.2,1) */
+  PPS_OBJ_LV_FIT = 4,     /* SSE of an RK4 Lotka-Volterra solve vs observations (data) */
+  PPS_OBJ_FHN_FIT = 5,    /* SSE of an RK4 FitzHugh-Nagumo solve vs observations (data) */
+  PPS_OBJ_MLP = 6,        /* MSE of a 2-layer tanh MLP on a sample set (data) */
+  /* the closed-form objectives of the reference's L-BFGS tests (test/lbfgs.jl:20-26) */
+  PPS_OBJ_BEALE = 16,
+  PPS_OBJ_BOOTH = 17,
+  PPS_OBJ_HIMMELBLAU = 18,
+  PPS_OBJ_QUADRATIC = 19,         /* p1 (x1-1)^2 + (x2+2)^2 */
+  PPS_OBJ_BOUNDARY_QUADRATIC = 20 /* (x1+1)^2 */
+} pps_objective;
+
+/* An OptimizationProblem(f, u0, p; lb, ub) (SciMLBase) restated. */
+typedef struct pps_problem {
+  int32_t objective;     /* pps_objective */
+  int32_t dim;           /* length(u0) */
+  const float* lb;       /* dim floats; NULL means -Inf (check_init_bounds, src/utils.jl:310-318) */
+  const float* ub;       /* dim floats; NULL means +Inf */
+  const float* u0;       /* dim floats; NULL means zeros (used by the unbounded sampler) */
+  const float* params;   /* objective parameters p */
+  int32_t nparams;
+  const float* data;     /* objective data (observations / samples), may be NULL */
+  int64_t ndata;         /* floats in data */
+} pps_problem;
+
+typedef struct pps_swarm pps_swarm;
+
+/* samplers (src/algorithms.jl:33-37 GPUUniformSampler / GPUUnboundedSampler) */
+enum {
+  PPS_SAMPLER_AUTO = 0,      /* unbounded if every bound is infinite, else uniform (src/init.jl:102-106) */
+  PPS_SAMPLER_UNIFORM = 1,   /* x = U (ub - lb) + lb           (src/utils.jl:57-84) */
+  PPS_SAMPLER_UNBOUNDED = 2  /* x = u0 + U |u0| or U if u0 = 0 (src/utils.jl:23-55) */
+};
+
+/* swarm flags */
+enum {
+  /* The CPU-backend sync loop takes the next global best's position from the
+   * winner's CURRENT position, not its personal best
+   * (src/lowerlevel_solve.jl:59-60).  Off: the GPU semantics
+   * (src/lowerlevel_solve.jl:31). */
+  PPS_FLAG_GBEST_FROM_POSITION = 1u
+};
+
+/* state fields for pps_get_state / pps_set_state */
+enum {
+  PPS_FIELD_POSITION = 0, /* dim*n */
+  PPS_FIELD_VELOCITY = 1, /* dim*n */
+  PPS_FIELD_PBEST = 2,    /* dim*n */
+  PPS_FIELD_PCOST = 3,    /* n */
+  PPS_FIELD_COST = 4      /* n */
+};
+
+typedef struct pps_swarm_info {
+  int64_t n;
+  int32_t dim;
+  int32_t objective;
+  uint32_t iteration;   /* iterations run since the last pps_swarm_init */
+  int32_t async_lanes;  /* threads per particle of pps_async_run */
+  int32_t async_slice;  /* dims per lane of pps_async_run (even) */
+  int32_t device;
+  uint64_t seed;
+  uint64_t device_bytes;
+} pps_swarm_info;
+
+/* ---- library ---- */
+PPS_API int32_t pps_version(void);
+PPS_API const char* pps_last_error(void);
+PPS_API int pps_device_count(int32_t* count);
+/* make `device` current for the calling thread (swarms are created on the
+ * current device; the reference selects it through its backend object) */
+PPS_API int pps_set_device(int32_t device);
+
+/* ---- swarm lifetime: init (src/init.jl:56-115) / reinit! (src/init.jl:117-141) ---- */
+/* Allocates the swarm on the current device.  n >= 1, 1 <= dim <= 4096. */
+PPS_API int pps_swarm_create(const pps_problem* prob, int64_t n, uint64_t seed, uint32_t flags,
+                     pps_swarm** out);
+PPS_API int pps_swarm_destroy(pps_swarm* s);
+/* Samples positions, zero velocities, evaluates costs and selects the initial
+ * global best (gpu_init_particles!, src/utils.jl:23-84; src/init.jl:38-54).
+ * Resets the iteration counter. */
+PPS_API int pps_swarm_init(pps_swarm* s, int32_t sampler);
+PPS_API int pps_swarm_info_get(pps_swarm* s, pps_swarm_info* info);
+
+/* ---- the PSO step ---- */
+/* ParallelSyncPSOKernel: maxiters synchronous iterations, global best
+ * recomputed after each (src/lowerlevel_solve.jl:1-65, src/kernels.jl:1-26,
+ * 127-194).  w is damped by wdamp after each iteration.  device_ms (may be
+ * NULL) receives the device time of the iteration loop. */
+PPS_API int pps_sync_run(pps_swarm* s, int32_t maxiters, float w, float wdamp, float c1, float c2,
+                 float* device_ms);
+/* ParallelPSOKernel(global_update=false): one launch runs all iterations,
+ * each particle against a private global best (src/kernels.jl:196-225). */
+PPS_API int pps_async_run(pps_swarm* s, int32_t maxiters, float w, float wdamp, float c1, float c2,
+                  float* device_ms);
+/* ParallelPSOKernel(global_update=true) (src/kernels.jl:38-125,
+ * src/lowerlevel_solve.jl:67-93).  The reference publishes block bests under
+ * a spin lock while other blocks read the global best mid-kernel, so its
+ * result depends on scheduling.  This engine publishes through a lock-free
+ * 64-bit atomicMin and lets every block read the previous iteration's best:
+ * the interleaving in which all reads precede all writes, i.e. the
+ * synchronous iteration. */
+PPS_API int pps_queue_run(pps_swarm* s, int32_t maxiters, float w, float wdamp, float c1, float c2,
+                  float* device_ms);
+
+/* ---- results ---- */
+/* global best position (dim floats), cost and particle index; any may be NULL */
+PPS_API int pps_get_gbest(pps_swarm* s, float* u, float* cost, int64_t* idx);
+/* copy a state field to / from host memory (SoA, particle fastest) */
+PPS_API int pps_get_state(pps_swarm* s, int32_t field, float* out);
+PPS_API int pps_set_state(pps_swarm* s, int32_t field, const float* in);
+/* evaluate the problem's objective at npoints points (SoA dim x npoints) on
+ * the device; used for sol.objective = f(u, p) (src/solve.jl:54-57) */
+PPS_API int pps_eval_objective(const pps_problem* prob, int64_t npoints, const float* x, float* f);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PPS_H */

@@ -1,0 +1,178 @@
+/*
+ * pps_oracle.h -- CPU restatement of ParallelParticleSwarms.jl's hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the checker: it may be loaded by
+ * tests/, by __graft_entry__.smoke() and by bench.py's CPU-baseline /
+ * reference leg, never by the product path (libpps_cuda.so and the Python
+ * package do not link, import or execute anything here).
+ *
+ * What it restates (file:line of the reference project):
+ *   - particle update        src/kernels.jl:1-26   (update_particle_state)
+ *   - sync CPU-backend loop  src/lowerlevel_solve.jl:38-65, src/kernels.jl:182-194
+ *   - sync GPU loop (gbest from the winner's personal best)
+ *                            src/lowerlevel_solve.jl:1-36, src/kernels.jl:127-177
+ *   - async in-kernel loop   src/kernels.jl:196-225, src/lowerlevel_solve.jl:95-121
+ *   - uniform / unbounded init  src/utils.jl:23-84, src/init.jl:38-54
+ *   - argmin ordering        src/ParallelParticleSwarms.jl:59-71 (isless on cost)
+ *   - defaults w=0.7298, wdamp=1, c1=c2=1.4962
+ *                            src/lowerlevel_solve.jl:6-7, src/kernels.jl:130-131
+ *   - Rosenbrock objective   test/regression.jl:12-18, test/gpu.jl:14-20
+ *   - HybridPSO local stage  src/hybrid.jl:100-158, src/lbfgs.jl:9-21
+ *   - ode_pso loop and SSE   src/ode_pso.jl:1-52,113-170
+ *
+ * Random numbers: the reference draws r1, r2 with rand() (src/kernels.jl:3,8);
+ * this restatement and the CUDA kernels draw them from the same counter-based
+ * Philox4x32-10 stream (Salmon, Moraes, Dror, Shaw, "Parallel Random Numbers:
+ * As Easy as 1, 2, 3", SC'11), so the two can be compared iteration by
+ * iteration.  Counter layout:
+ *   update draws: ctr = {particle, dim/2, iteration, PPS_TAG_STEP}, key = seed
+ *                 out = {r1[2j], r2[2j], r1[2j+1], r2[2j+1]}
+ *   init draws:   ctr = {particle, dim/4, 0, PPS_TAG_INIT}, out[k] -> dim 4j+k
+ *   u01(o) = (o >> 8) * 2^-24
+ *
+ * Arithmetic: every operation is a single IEEE-754 binary32 operation in the
+ * reference's evaluation order; fused multiply-add appears only where written
+ * as fmaf() (the CUDA kernels use __fmaf_rn at the same places), so results are
+ * bit-identical to the kernels.  Build with -ffp-contract=off.
+ *
+ * Parity pins: the reference's own tests are thresholds under fixed seeds
+ * (test/regression.jl, test/gpu.jl), an exact loss-reduction check
+ * (test/regression.jl:345-389) and L-BFGS known answers (test/lbfgs.jl:3-73);
+ * tests/test_oracle_pins.py re-runs each of them against this library.
+ */
+#ifndef PPS_ORACLE_H
+#define PPS_ORACLE_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ORC_TAG_INIT 0x494E4954u  /* "INIT" */
+#define ORC_TAG_STEP 0x50534F31u  /* "PSO1" */
+
+enum {
+  ORC_OBJ_SPHERE = 0,
+  ORC_OBJ_ROSENBROCK = 1,
+  ORC_OBJ_RASTRIGIN = 2,
+  ORC_OBJ_ACKLEY = 3,
+  ORC_OBJ_LV_FIT = 4,   /* SSE of an RK4 Lotka-Volterra solve vs data */
+  ORC_OBJ_FHN_FIT = 5,  /* SSE of an RK4 FitzHugh-Nagumo solve vs data */
+  /* closed-form objectives of the reference's L-BFGS tests (test/lbfgs.jl:20-26) */
+  ORC_OBJ_BEALE = 16,
+  ORC_OBJ_BOOTH = 17,
+  ORC_OBJ_HIMMELBLAU = 18,
+  ORC_OBJ_QUADRATIC = 19,          /* p1 (x1-1)^2 + (x2+2)^2 */
+  ORC_OBJ_BOUNDARY_QUADRATIC = 20, /* (x1+1)^2 */
+};
+
+struct orc_ode_fit;
+
+/* problem description, mirrors pps_problem in include/pps.h */
+typedef struct orc_problem {
+  int32_t objective;
+  int32_t dim;
+  const float* lb;      /* dim floats, may hold +-inf */
+  const float* ub;      /* dim floats */
+  const float* u0;      /* dim floats (unbounded sampler only) */
+  float params[8];      /* objective parameters */
+  int32_t nparams;
+  const struct orc_ode_fit* ode;  /* ORC_OBJ_LV_FIT / ORC_OBJ_FHN_FIT only */
+} orc_problem;
+
+/* structure-of-arrays swarm state: x[d*n + i] */
+typedef struct orc_swarm {
+  int64_t n;
+  int32_t dim;
+  float* x;
+  float* v;
+  float* pbest;
+  float* pcost;
+  float* cost;
+  float* g;       /* dim floats: global best position */
+  float gcost;
+  int64_t gidx;
+} orc_swarm;
+
+/* ---- primitives ---- */
+void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
+void orc_philox4x64_10(const uint64_t ctr[4], const uint64_t key[2], uint64_t out[4]);
+float orc_u01(uint32_t bits);
+float orc_cos2pi(float x);
+float orc_sin2pi(float x);
+float orc_exp(float x);
+uint64_t orc_argmin_key(float cost, uint32_t idx);
+
+/* objective value with the dims split into `lanes` contiguous slices of
+ * even length, each summed in order, the slice sums combined by a balanced
+ * pairwise tree (lanes a power of two, 1 = plain sequential sum). */
+float orc_objective(const orc_problem* prob, const float* x, int64_t stride, int32_t lanes);
+/* analytic gradient (Rosenbrock, Rastrigin, Ackley, sphere), sequential sums */
+float orc_objective_grad(const orc_problem* prob, const float* x, float* grad);
+
+/* ---- swarm ---- */
+enum { ORC_SAMPLER_UNIFORM = 0, ORC_SAMPLER_UNBOUNDED = 1 };
+enum { ORC_GBEST_FROM_PBEST = 0, ORC_GBEST_FROM_POSITION = 1 };
+
+void orc_init(const orc_problem* prob, orc_swarm* s, uint64_t seed, int32_t sampler);
+/* argmin of pcost (lowest index on ties), gather g from pbest or position */
+void orc_select_gbest(const orc_problem* prob, orc_swarm* s, int32_t gbest_source);
+/* `iters` synchronous iterations starting at iteration counter t0.
+ * Returns the inertia weight after the last damping step. */
+float orc_sync_run(const orc_problem* prob, orc_swarm* s, uint64_t seed, uint32_t t0,
+                   int32_t iters, float w, float wdamp, float c1, float c2,
+                   int32_t gbest_source, int32_t nthreads);
+/* async: every particle runs `iters` iterations against a private global best
+ * seeded from s->g; the objective is summed with `lanes` slices. */
+float orc_async_run(const orc_problem* prob, orc_swarm* s, uint64_t seed, uint32_t t0,
+                    int32_t iters, float w, float wdamp, float c1, float c2,
+                    int32_t lanes, int32_t nthreads);
+/* how the CUDA async kernel splits D dims over lanes: returns lanes, writes
+ * the even slice length */
+int32_t orc_async_lanes(int32_t dim, int32_t* slice);
+
+/* ---- HybridPSO local stage ---- */
+typedef struct orc_lbfgs_opts {
+  int32_t history;     /* m */
+  int32_t maxiters;
+  float armijo_c1;
+  float gtol;
+  int32_t max_backtracks;
+} orc_lbfgs_opts;
+/* projected L-BFGS from each start point (x0[d*n+i]); writes xout, fout */
+void orc_lbfgs(const orc_problem* prob, int64_t n, const float* x0, const orc_lbfgs_opts* o,
+               float* xout, float* fout, int32_t* iters_out, int32_t nthreads);
+/* Broyden quasi-Newton on grad f = 0 (inverse-Jacobian update) */
+void orc_broyden(const orc_problem* prob, int64_t n, const float* x0, const orc_lbfgs_opts* o,
+                 float* xout, float* fout, int32_t* iters_out, int32_t nthreads);
+
+/* ---- ode_pso ---- */
+enum { ORC_ODE_LV = 0, ORC_ODE_FHN = 1 };
+typedef struct orc_ode_fit {
+  int32_t model;       /* ORC_ODE_LV / ORC_ODE_FHN */
+  int32_t nparams;     /* particle dimension */
+  float u0[2];
+  float dt;
+  int32_t nsteps;      /* RK4 steps */
+  int32_t save_every;  /* save a point every save_every steps (t=0 included) */
+  int32_t nsaves;
+  const float* data;   /* nsaves x 2, row major */
+  float fixed[4];      /* fixed model constants (FHN: l) */
+} orc_ode_fit;
+/* RK4 integration + SSE against data (src/ode_pso.jl:47-52) */
+float orc_ode_loss(const orc_ode_fit* fit, const float* p);
+/* trajectory at the save points: out[nsaves*2] */
+void orc_ode_solve(const orc_ode_fit* fit, const float* p, float* out);
+/* sum of squared differences per particle: data[m][k] vs us[i][m][k]
+ * (the reference's _reduce_losses!, test/regression.jl:345-357) */
+void orc_reduce_losses(int32_t m, int32_t ncomp, int64_t n, const float* data,
+                       const float* us, float* losses);
+/* An ODE fit is a swarm whose objective is ORC_OBJ_LV_FIT / ORC_OBJ_FHN_FIT
+ * (orc_problem.ode points at the fit): orc_init + orc_sync_run give the
+ * parameter_estim_ode! loop of src/ode_pso.jl:113-170 with an elementwise
+ * clamp and RK4 in place of GPUTsit5. */
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,258 @@
+"""ctypes wrapper of the CPU restatement (oracle/_build/libpps_oracle.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and
+bench.py's CPU-baseline / reference leg as the checker; the product package
+never imports it.  See pps_oracle.h for what is restated and the reference
+file:line each part follows.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB_PATH = HERE / "_build" / "libpps_oracle.so"
+
+TAG_INIT = 0x494E4954
+TAG_STEP = 0x50534F31
+SAMPLER_UNIFORM, SAMPLER_UNBOUNDED = 0, 1
+GBEST_FROM_PBEST, GBEST_FROM_POSITION = 0, 1
+ODE_LV, ODE_FHN = 0, 1
+
+_fp = ctypes.POINTER(ctypes.c_float)
+
+
+class OdeFit(ctypes.Structure):
+    _fields_ = [("model", ctypes.c_int32), ("nparams", ctypes.c_int32), ("u0", ctypes.c_float * 2),
+                ("dt", ctypes.c_float), ("nsteps", ctypes.c_int32), ("save_every", ctypes.c_int32),
+                ("nsaves", ctypes.c_int32), ("data", _fp), ("fixed", ctypes.c_float * 4)]
+
+
+class Problem(ctypes.Structure):
+    _fields_ = [("objective", ctypes.c_int32), ("dim", ctypes.c_int32), ("lb", _fp), ("ub", _fp),
+                ("u0", _fp), ("params", ctypes.c_float * 8), ("nparams", ctypes.c_int32),
+                ("ode", ctypes.POINTER(OdeFit))]
+
+
+class SwarmC(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int64), ("dim", ctypes.c_int32), ("x", _fp), ("v", _fp), ("pbest", _fp),
+                ("pcost", _fp), ("cost", _fp), ("g", _fp), ("gcost", ctypes.c_float), ("gidx", ctypes.c_int64)]
+
+
+class LbfgsOpts(ctypes.Structure):
+    _fields_ = [("history", ctypes.c_int32), ("maxiters", ctypes.c_int32), ("armijo_c1", ctypes.c_float),
+                ("gtol", ctypes.c_float), ("max_backtracks", ctypes.c_int32)]
+
+
+_lib = None
+
+
+def build() -> Path:
+    """Compile the restatement with its Makefile (gcc, -ffp-contract=off)."""
+    subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
+    return LIB_PATH
+
+
+def load() -> ctypes.CDLL:
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            build()
+        L = ctypes.CDLL(str(LIB_PATH))
+        L.orc_u01.restype = ctypes.c_float
+        L.orc_u01.argtypes = [ctypes.c_uint32]
+        for name in ("orc_cos2pi", "orc_sin2pi", "orc_exp"):
+            getattr(L, name).restype = ctypes.c_float
+            getattr(L, name).argtypes = [ctypes.c_float]
+        L.orc_objective.restype = ctypes.c_float
+        L.orc_objective.argtypes = [ctypes.POINTER(Problem), _fp, ctypes.c_int64, ctypes.c_int32]
+        L.orc_objective_grad.restype = ctypes.c_float
+        L.orc_objective_grad.argtypes = [ctypes.POINTER(Problem), _fp, _fp]
+        L.orc_init.argtypes = [ctypes.POINTER(Problem), ctypes.POINTER(SwarmC), ctypes.c_uint64, ctypes.c_int32]
+        L.orc_select_gbest.argtypes = [ctypes.POINTER(Problem), ctypes.POINTER(SwarmC), ctypes.c_int32]
+        L.orc_sync_run.restype = ctypes.c_float
+        L.orc_sync_run.argtypes = [ctypes.POINTER(Problem), ctypes.POINTER(SwarmC), ctypes.c_uint64,
+                                   ctypes.c_uint32, ctypes.c_int32, ctypes.c_float, ctypes.c_float,
+                                   ctypes.c_float, ctypes.c_float, ctypes.c_int32, ctypes.c_int32]
+        L.orc_async_run.restype = ctypes.c_float
+        L.orc_async_run.argtypes = [ctypes.POINTER(Problem), ctypes.POINTER(SwarmC), ctypes.c_uint64,
+                                    ctypes.c_uint32, ctypes.c_int32, ctypes.c_float, ctypes.c_float,
+                                    ctypes.c_float, ctypes.c_float, ctypes.c_int32, ctypes.c_int32]
+        L.orc_async_lanes.restype = ctypes.c_int32
+        L.orc_async_lanes.argtypes = [ctypes.c_int32, ctypes.POINTER(ctypes.c_int32)]
+        L.orc_argmin_key.restype = ctypes.c_uint64
+        L.orc_argmin_key.argtypes = [ctypes.c_float, ctypes.c_uint32]
+        for name in ("orc_lbfgs", "orc_broyden"):
+            getattr(L, name).argtypes = [ctypes.POINTER(Problem), ctypes.c_int64, _fp, ctypes.POINTER(LbfgsOpts),
+                                         _fp, _fp, ctypes.POINTER(ctypes.c_int32), ctypes.c_int32]
+        L.orc_ode_loss.restype = ctypes.c_float
+        L.orc_ode_loss.argtypes = [ctypes.POINTER(OdeFit), _fp]
+        L.orc_ode_solve.argtypes = [ctypes.POINTER(OdeFit), _fp, _fp]
+        L.orc_reduce_losses.argtypes = [ctypes.c_int32, ctypes.c_int32, ctypes.c_int64, _fp, _fp, _fp]
+        _lib = L
+    return _lib
+
+
+def fp(a: np.ndarray):
+    return a.ctypes.data_as(_fp)
+
+
+def philox4x32_10(ctr, key) -> list[int]:
+    L = load()
+    c = (ctypes.c_uint32 * 4)(*ctr)
+    k = (ctypes.c_uint32 * 2)(*key)
+    o = (ctypes.c_uint32 * 4)()
+    L.orc_philox4x32_10(c, k, o)
+    return list(o)
+
+
+def philox4x64_10(ctr, key) -> list[int]:
+    L = load()
+    c = (ctypes.c_uint64 * 4)(*ctr)
+    k = (ctypes.c_uint64 * 2)(*key)
+    o = (ctypes.c_uint64 * 4)()
+    L.orc_philox4x64_10(c, k, o)
+    return list(o)
+
+
+def default_threads() -> int:
+    return max(1, os.cpu_count() or 1)
+
+
+class OracleProblem:
+    """orc_problem over numpy buffers (objective ids are include/pps.h's)."""
+
+    def __init__(self, objective: int, dim: int, lb=None, ub=None, u0=None, params=(), ode=None):
+        self.dim = int(dim)
+        self.lb = np.ascontiguousarray(np.full(dim, -np.inf, np.float32) if lb is None else np.asarray(lb, np.float32))
+        self.ub = np.ascontiguousarray(np.full(dim, np.inf, np.float32) if ub is None else np.asarray(ub, np.float32))
+        self.u0 = np.ascontiguousarray(np.zeros(dim, np.float32) if u0 is None else np.asarray(u0, np.float32))
+        self.c = Problem()
+        self.c.objective = int(objective)
+        self.c.dim = self.dim
+        self.c.lb, self.c.ub, self.c.u0 = fp(self.lb), fp(self.ub), fp(self.u0)
+        params = [] if params is None else list(np.asarray(params, np.float32).reshape(-1))
+        for k, v in enumerate(params):
+            self.c.params[k] = float(v)
+        self.c.nparams = len(params)
+        self.ode = ode
+        if ode is not None:
+            self.c.ode = ctypes.pointer(ode.c)
+
+    def objective(self, x, lanes: int = 1) -> float:
+        x = np.ascontiguousarray(np.asarray(x, np.float32))
+        return float(load().orc_objective(ctypes.byref(self.c), fp(x), 1, lanes))
+
+    def objective_grad(self, x):
+        x = np.ascontiguousarray(np.asarray(x, np.float32))
+        g = np.empty_like(x)
+        f = load().orc_objective_grad(ctypes.byref(self.c), fp(x), fp(g))
+        return float(f), g
+
+
+class OracleOdeFit:
+    def __init__(self, model: int, nparams: int, u0, dt: float, nsteps: int, save_every: int, data,
+                 fixed=(0.0, 0.0, 0.0, 0.0)):
+        self.data = np.ascontiguousarray(np.asarray(data, np.float32).reshape(-1, 2))
+        self.c = OdeFit()
+        self.c.model, self.c.nparams = int(model), int(nparams)
+        self.c.u0[0], self.c.u0[1] = float(u0[0]), float(u0[1])
+        self.c.dt, self.c.nsteps, self.c.save_every = float(dt), int(nsteps), int(save_every)
+        self.c.nsaves = int(self.data.shape[0])
+        self.c.data = fp(self.data)
+        for k, v in enumerate(fixed):
+            self.c.fixed[k] = float(v)
+
+    def loss(self, p) -> float:
+        p = np.ascontiguousarray(np.asarray(p, np.float32))
+        return float(load().orc_ode_loss(ctypes.byref(self.c), fp(p)))
+
+    def solve(self, p) -> np.ndarray:
+        p = np.ascontiguousarray(np.asarray(p, np.float32))
+        out = np.empty((self.c.nsaves, 2), np.float32)
+        load().orc_ode_solve(ctypes.byref(self.c), fp(p), fp(out))
+        return out
+
+
+class OracleSwarm:
+    """SoA swarm state on the host, stepped by the restatement."""
+
+    def __init__(self, prob: OracleProblem, n: int, seed: int):
+        self.prob, self.n, self.dim, self.seed = prob, int(n), prob.dim, int(seed)
+        D, n = self.dim, self.n
+        self.x = np.zeros((D, n), np.float32)
+        self.v = np.zeros((D, n), np.float32)
+        self.pbest = np.zeros((D, n), np.float32)
+        self.pcost = np.zeros(n, np.float32)
+        self.cost = np.zeros(n, np.float32)
+        self.g = np.zeros(D, np.float32)
+        self.c = SwarmC(n, D, fp(self.x), fp(self.v), fp(self.pbest), fp(self.pcost), fp(self.cost), fp(self.g),
+                        0.0, 0)
+        self.t = 0
+
+    @property
+    def gcost(self) -> float:
+        return float(self.c.gcost)
+
+    @property
+    def gidx(self) -> int:
+        return int(self.c.gidx)
+
+    def init(self, sampler: int = SAMPLER_UNIFORM) -> "OracleSwarm":
+        load().orc_init(ctypes.byref(self.prob.c), ctypes.byref(self.c), self.seed, sampler)
+        self.t = 0
+        return self
+
+    def sync_run(self, iters, w=0.7298, wdamp=1.0, c1=1.4962, c2=1.4962, gbest_source=GBEST_FROM_PBEST,
+                 nthreads=None) -> float:
+        wo = load().orc_sync_run(ctypes.byref(self.prob.c), ctypes.byref(self.c), self.seed, self.t, int(iters),
+                                 w, wdamp, c1, c2, gbest_source, nthreads or default_threads())
+        self.t += int(iters)
+        return wo
+
+    def async_run(self, iters, w=0.7298, wdamp=1.0, c1=1.4962, c2=1.4962, lanes=None, nthreads=None) -> float:
+        if lanes is None:
+            lanes = async_lanes(self.dim)[0]
+        wo = load().orc_async_run(ctypes.byref(self.prob.c), ctypes.byref(self.c), self.seed, self.t, int(iters),
+                                  w, wdamp, c1, c2, lanes, nthreads or default_threads())
+        self.t += int(iters)
+        return wo
+
+    def state(self) -> dict:
+        return {"x": self.x.copy(), "v": self.v.copy(), "pbest": self.pbest.copy(), "pcost": self.pcost.copy(),
+                "cost": self.cost.copy()}
+
+
+def async_lanes(dim: int):
+    s = ctypes.c_int32()
+    lanes = load().orc_async_lanes(int(dim), ctypes.byref(s))
+    return int(lanes), int(s.value)
+
+
+def lbfgs(prob: OracleProblem, x0, history=10, maxiters=100, armijo_c1=1e-4, gtol=1e-5, max_backtracks=30,
+          nthreads=None, broyden=False):
+    """Local stage from start points x0 (dim, n). Returns (x, f, iters)."""
+    x0 = np.ascontiguousarray(np.asarray(x0, np.float32))
+    D, n = x0.shape
+    xo = np.empty_like(x0)
+    fo = np.empty(n, np.float32)
+    it = np.empty(n, np.int32)
+    o = LbfgsOpts(history, maxiters, armijo_c1, gtol, max_backtracks)
+    fn = load().orc_broyden if broyden else load().orc_lbfgs
+    fn(ctypes.byref(prob.c), n, fp(x0), ctypes.byref(o), fp(xo), fp(fo), it.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+       nthreads or default_threads())
+    return xo, fo, it
+
+
+def reduce_losses(data, us) -> np.ndarray:
+    """data (m, k), us (n, m, k) -> losses (n,)."""
+    data = np.ascontiguousarray(np.asarray(data, np.float32))
+    us = np.ascontiguousarray(np.asarray(us, np.float32))
+    n, m, k = us.shape
+    out = np.empty(n, np.float32)
+    load().orc_reduce_losses(m, k, n, fp(data), fp(us), fp(out))
+    return out

@@ -1,0 +1,470 @@
+// pps_api.cu -- the C ABI of include/pps.h: swarm lifetime, runs, results.
+//
+// Reference entry points this layer replaces (all on the host side of the
+// reference, which calls KernelAbstractions kernels from Julia):
+//   init(prob, ParallelPSOKernel | ParallelSyncPSOKernel)   src/init.jl:56-115
+//   reinit!(cache)                                          src/init.jl:117-141
+//   solve!(cache) -> vectorized_solve!                      src/solve.jl:11-59,
+//                                                           src/lowerlevel_solve.jl:1-121
+//   sol.objective = prob.f(gbest.position, prob.p)          src/solve.jl:54-57
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <limits>
+#include <new>
+
+#include "pps_internal.h"
+
+namespace pps {
+
+static thread_local char g_err[512] = "";
+
+int set_error(int code, const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+  return code;
+}
+
+int cuda_error(cudaError_t e, const char* what) {
+  return set_error(e == cudaErrorMemoryAllocation ? PPS_ENOMEM : PPS_ECUDA, "%s: %s (%s)", what,
+                   cudaGetErrorString(e), cudaGetErrorName(e));
+}
+
+static inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+static bool supported_objective(int obj) {
+  switch (obj) {
+    case kSphere:
+    case kRosenbrock:
+    case kRastrigin:
+    case kAckley:
+    case kBeale:
+    case kBooth:
+    case kHimmelblau:
+    case kQuadratic:
+    case kBoundaryQuadratic:
+      return true;
+    default:
+      return false;
+  }
+}
+
+static int check_problem(const pps_problem* prob) {
+  if (!prob) return set_error(PPS_EINVAL, "problem is NULL");
+  if (prob->dim < 1 || prob->dim > 4096)
+    return set_error(PPS_EINVAL, "dim must be in [1, 4096] (got %d)", prob->dim);
+  if (prob->nparams < 0 || prob->nparams > 8)
+    return set_error(PPS_EINVAL, "nparams must be in [0, 8] (got %d)", prob->nparams);
+  if (prob->nparams > 0 && !prob->params) return set_error(PPS_EINVAL, "params is NULL");
+  if (!supported_objective(prob->objective))
+    return set_error(PPS_ENOTSUP, "objective %d is not supported by this entry point", prob->objective);
+  if ((prob->objective >= kBeale) && prob->dim > 2)
+    return set_error(PPS_EINVAL, "objective %d is defined for dim <= 2", prob->objective);
+  for (int d = 0; d < prob->dim; ++d) {
+    const float lo = prob->lb ? prob->lb[d] : -INFINITY;
+    const float hi = prob->ub ? prob->ub[d] : INFINITY;
+    if (std::isnan(lo) || std::isnan(hi) || lo > hi)
+      return set_error(PPS_EINVAL, "bounds of dim %d are invalid (lb=%g ub=%g)", d, lo, hi);
+  }
+  return PPS_OK;
+}
+
+static ObjParams make_params(const pps_problem* prob) {
+  ObjParams op{};
+  for (int k = 0; k < prob->nparams; ++k) op.p[k] = prob->params[k];
+  op.np = prob->nparams;
+  op.dim = prob->dim;
+  return op;
+}
+
+}  // namespace pps
+
+using namespace pps;
+
+extern "C" {
+
+int32_t pps_version(void) { return PPS_VERSION; }
+
+const char* pps_last_error(void) { return g_err; }
+
+int pps_device_count(int32_t* count) {
+  int c = 0;
+  cudaError_t e = cudaGetDeviceCount(&c);
+  if (count) *count = (e == cudaSuccess) ? c : 0;
+  if (e != cudaSuccess) return set_error(PPS_ENODEV, "no CUDA device: %s", cudaGetErrorString(e));
+  return PPS_OK;
+}
+
+int pps_set_device(int32_t device) {
+  int c = 0;
+  if (cudaGetDeviceCount(&c) != cudaSuccess || c < 1) return set_error(PPS_ENODEV, "no CUDA device");
+  if (device < 0 || device >= c) return set_error(PPS_EINVAL, "device %d out of range [0, %d)", device, c);
+  PPS_CUDA(cudaSetDevice(device));
+  return PPS_OK;
+}
+
+int pps_swarm_create(const pps_problem* prob, int64_t n, uint64_t seed, uint32_t flags,
+                     pps_swarm** out) {
+  if (!out) return set_error(PPS_EINVAL, "out is NULL");
+  *out = nullptr;
+  int rc = check_problem(prob);
+  if (rc) return rc;
+  if (n < 1 || n > (int64_t)0xFFFFFF00LL) return set_error(PPS_EINVAL, "n must be in [1, 2^32-256] (got %lld)", (long long)n);
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return set_error(PPS_ENODEV, "no CUDA device");
+
+  pps_swarm* s = new (std::nothrow) pps_swarm();
+  if (!s) return set_error(PPS_ENOMEM, "host allocation failed");
+  cudaGetDevice(&s->device);
+  cudaDeviceGetAttribute(&s->sm_count, cudaDevAttrMultiProcessorCount, s->device);
+  const int D = prob->dim;
+  const int64_t npad = (int64_t)align_up((size_t)n, 64);
+  // carve one allocation
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    const size_t at = off;
+    off = align_up(off + bytes, 256);
+    return at;
+  };
+  const size_t oX = take(sizeof(float) * D * npad);
+  const size_t oV = take(sizeof(float) * D * npad);
+  const size_t oP = take(sizeof(float) * D * npad);
+  const size_t oPc = take(sizeof(float) * npad);
+  const size_t oC = take(sizeof(float) * npad);
+  const size_t oF = take(npad);
+  const size_t oG = take(sizeof(float) * D);
+  const size_t oLb = take(sizeof(float) * D);
+  const size_t oUb = take(sizeof(float) * D);
+  const size_t oU0 = take(sizeof(float) * D);
+  const size_t oSt = take(sizeof(IterState));
+  s->bytes = off;
+  cudaError_t e = cudaMalloc(&s->block, s->bytes);
+  if (e != cudaSuccess) {
+    delete s;
+    return cuda_error(e, "cudaMalloc(swarm state)");
+  }
+  char* b = static_cast<char*>(s->block);
+  s->dv.X = reinterpret_cast<float*>(b + oX);
+  s->dv.V = reinterpret_cast<float*>(b + oV);
+  s->dv.P = reinterpret_cast<float*>(b + oP);
+  s->dv.pcost = reinterpret_cast<float*>(b + oPc);
+  s->dv.cost = reinterpret_cast<float*>(b + oC);
+  s->dv.flag = reinterpret_cast<uint8_t*>(b + oF);
+  s->dv.g = reinterpret_cast<float*>(b + oG);
+  s->dv.lb = reinterpret_cast<float*>(b + oLb);
+  s->dv.ub = reinterpret_cast<float*>(b + oUb);
+  s->dv.st = reinterpret_cast<IterState*>(b + oSt);
+  s->u0_dev = reinterpret_cast<float*>(b + oU0);
+  s->dv.n = n;
+  s->dv.npad = npad;
+  s->dv.dim = D;
+  s->op = make_params(prob);
+  s->objective = prob->objective;
+  s->seed = seed;
+  s->flags = flags;
+  s->host_lb = static_cast<float*>(malloc(sizeof(float) * 3 * D));
+  if (!s->host_lb) {
+    cudaFree(s->block);
+    delete s;
+    return set_error(PPS_ENOMEM, "host allocation failed");
+  }
+  s->host_ub = s->host_lb + D;
+  s->host_u0 = s->host_lb + 2 * D;
+  for (int d = 0; d < D; ++d) {
+    s->host_lb[d] = prob->lb ? prob->lb[d] : -INFINITY;
+    s->host_ub[d] = prob->ub ? prob->ub[d] : INFINITY;
+    s->host_u0[d] = prob->u0 ? prob->u0[d] : 0.0f;
+  }
+  rc = PPS_OK;
+  do {
+    e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) { rc = cuda_error(e, "cudaStreamCreate"); break; }
+    if ((e = cudaEventCreate(&s->ev0)) != cudaSuccess || (e = cudaEventCreate(&s->ev1)) != cudaSuccess) {
+      rc = cuda_error(e, "cudaEventCreate");
+      break;
+    }
+    if ((e = cudaMemsetAsync(s->block, 0, s->bytes, s->stream)) != cudaSuccess) { rc = cuda_error(e, "cudaMemset"); break; }
+    if ((e = cudaMemcpyAsync(s->dv.lb, s->host_lb, sizeof(float) * D, cudaMemcpyHostToDevice, s->stream)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(s->dv.ub, s->host_ub, sizeof(float) * D, cudaMemcpyHostToDevice, s->stream)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(b + oU0, s->host_u0, sizeof(float) * D, cudaMemcpyHostToDevice, s->stream)) != cudaSuccess) {
+      rc = cuda_error(e, "cudaMemcpy(bounds)");
+      break;
+    }
+    if ((e = cudaStreamSynchronize(s->stream)) != cudaSuccess) { rc = cuda_error(e, "cudaStreamSynchronize"); break; }
+  } while (0);
+  if (rc) {
+    pps_swarm_destroy(s);
+    return rc;
+  }
+  *out = s;
+  return PPS_OK;
+}
+
+int pps_swarm_destroy(pps_swarm* s) {
+  if (!s) return PPS_OK;
+  int dev = -1;
+  cudaGetDevice(&dev);
+  if (dev != s->device) cudaSetDevice(s->device);
+  if (s->stream) cudaStreamSynchronize(s->stream);
+  if (s->graph) cudaGraphExecDestroy(s->graph);
+  if (s->ev0) cudaEventDestroy(s->ev0);
+  if (s->ev1) cudaEventDestroy(s->ev1);
+  if (s->stream) cudaStreamDestroy(s->stream);
+  if (s->block) cudaFree(s->block);
+  free(s->host_lb);
+  if (dev >= 0 && dev != s->device) cudaSetDevice(dev);
+  delete s;
+  return PPS_OK;
+}
+
+static int use_device(pps_swarm* s) {
+  int dev = -1;
+  cudaGetDevice(&dev);
+  if (dev != s->device) PPS_CUDA(cudaSetDevice(s->device));
+  return PPS_OK;
+}
+
+int pps_swarm_init(pps_swarm* s, int32_t sampler) {
+  if (!s) return set_error(PPS_EINVAL, "swarm is NULL");
+  int rc = use_device(s);
+  if (rc) return rc;
+  const int D = s->dv.dim;
+  if (sampler == PPS_SAMPLER_AUTO) {
+    bool all_inf = true;
+    for (int d = 0; d < D; ++d)
+      if (!(std::isinf(s->host_lb[d]) && std::isinf(s->host_ub[d]))) all_inf = false;
+    sampler = all_inf ? PPS_SAMPLER_UNBOUNDED : PPS_SAMPLER_UNIFORM;
+  }
+  if (sampler != PPS_SAMPLER_UNIFORM && sampler != PPS_SAMPLER_UNBOUNDED)
+    return set_error(PPS_EINVAL, "unknown sampler %d", sampler);
+  if (sampler == PPS_SAMPLER_UNIFORM) {
+    for (int d = 0; d < D; ++d)
+      if (!std::isfinite(s->host_lb[d]) || !std::isfinite(s->host_ub[d]))
+        return set_error(PPS_EINVAL, "uniform sampler needs finite bounds (dim %d)", d);
+  }
+  if ((rc = launch_set_iter(s, 0u, 0.7298f, 1.0f))) return rc;
+  if ((rc = launch_init(s, sampler, s->u0_dev))) return rc;
+  PPS_CUDA(cudaStreamSynchronize(s->stream));
+  s->t = 0;
+  s->initialized = 1;
+  return PPS_OK;
+}
+
+int pps_swarm_info_get(pps_swarm* s, pps_swarm_info* info) {
+  if (!s || !info) return set_error(PPS_EINVAL, "NULL argument");
+  info->n = s->dv.n;
+  info->dim = s->dv.dim;
+  info->objective = s->objective;
+  info->iteration = s->t;
+  int slice = 0;
+  info->async_lanes = async_lanes(s->dv.dim, &slice);
+  info->async_slice = slice;
+  info->device = s->device;
+  info->seed = s->seed;
+  info->device_bytes = s->bytes;
+  return PPS_OK;
+}
+
+static int check_run(pps_swarm* s, int32_t maxiters, float w, float wdamp, float c1, float c2) {
+  if (!s) return set_error(PPS_EINVAL, "swarm is NULL");
+  if (!s->initialized) return set_error(PPS_EINVAL, "swarm is not initialised (call pps_swarm_init)");
+  if (maxiters < 0) return set_error(PPS_EINVAL, "maxiters must be >= 0");
+  if (!std::isfinite(w) || !std::isfinite(wdamp) || !std::isfinite(c1) || !std::isfinite(c2))
+    return set_error(PPS_EINVAL, "coefficients must be finite");
+  if ((uint64_t)s->t + (uint64_t)maxiters > 0xFFFFFFFFull)
+    return set_error(PPS_EINVAL, "iteration counter would overflow");
+  return use_device(s);
+}
+
+static int finish_timing(pps_swarm* s, float* device_ms) {
+  PPS_CUDA(cudaEventSynchronize(s->ev1));
+  if (device_ms) {
+    float ms = 0.0f;
+    PPS_CUDA(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
+    *device_ms = ms;
+  }
+  return PPS_OK;
+}
+
+static constexpr int kGraphChunk = 32;
+
+static int run_steps(pps_swarm* s, int32_t maxiters, float c1, float c2, uint32_t run_flags) {
+  int rc;
+  const uint32_t saved = s->flags;
+  s->flags = run_flags;
+  sync_grid(s);  // resolve occupancy outside any capture
+  if (maxiters >= kGraphChunk) {
+    const bool stale = !s->graph || s->graph_len != kGraphChunk || s->graph_async_lanes != (int)run_flags ||
+                       s->graph_c1 != c1 || s->graph_c2 != c2;
+    if (stale) {
+      if (s->graph) cudaGraphExecDestroy(s->graph);
+      s->graph = nullptr;
+      cudaGraph_t g = nullptr;
+      PPS_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+      for (int k = 0; k < kGraphChunk; ++k) {
+        if ((rc = launch_sync_step(s, c1, c2))) {
+          cudaStreamEndCapture(s->stream, &g);
+          if (g) cudaGraphDestroy(g);
+          s->flags = saved;
+          return rc;
+        }
+      }
+      PPS_CUDA(cudaStreamEndCapture(s->stream, &g));
+      cudaError_t e = cudaGraphInstantiate(&s->graph, g, 0);
+      cudaGraphDestroy(g);
+      if (e != cudaSuccess) {
+        s->flags = saved;
+        return cuda_error(e, "cudaGraphInstantiate");
+      }
+      s->graph_len = kGraphChunk;
+      s->graph_async_lanes = (int)run_flags;
+      s->graph_c1 = c1;
+      s->graph_c2 = c2;
+    }
+  }
+  int32_t left = maxiters;
+  while (left >= kGraphChunk) {
+    cudaError_t e = cudaGraphLaunch(s->graph, s->stream);
+    if (e != cudaSuccess) {
+      s->flags = saved;
+      return cuda_error(e, "cudaGraphLaunch");
+    }
+    left -= kGraphChunk;
+  }
+  for (; left > 0; --left) {
+    if ((rc = launch_sync_step(s, c1, c2))) {
+      s->flags = saved;
+      return rc;
+    }
+  }
+  s->flags = saved;
+  return PPS_OK;
+}
+
+static int sync_like_run(pps_swarm* s, int32_t maxiters, float w, float wdamp, float c1, float c2,
+                         float* device_ms, uint32_t run_flags) {
+  int rc = check_run(s, maxiters, w, wdamp, c1, c2);
+  if (rc) return rc;
+  if ((rc = launch_set_iter(s, s->t, w, wdamp))) return rc;
+  PPS_CUDA(cudaEventRecord(s->ev0, s->stream));
+  if ((rc = run_steps(s, maxiters, c1, c2, run_flags))) return rc;
+  PPS_CUDA(cudaEventRecord(s->ev1, s->stream));
+  if ((rc = launch_materialize(s))) return rc;
+  if ((rc = finish_timing(s, device_ms))) return rc;
+  PPS_CUDA(cudaStreamSynchronize(s->stream));
+  s->t += (uint32_t)maxiters;
+  return PPS_OK;
+}
+
+int pps_sync_run(pps_swarm* s, int32_t maxiters, float w, float wdamp, float c1, float c2,
+                 float* device_ms) {
+  return sync_like_run(s, maxiters, w, wdamp, c1, c2, device_ms,
+                       s ? (s->flags & PPS_FLAG_GBEST_FROM_POSITION) : 0u);
+}
+
+int pps_queue_run(pps_swarm* s, int32_t maxiters, float w, float wdamp, float c1, float c2,
+                  float* device_ms) {
+  // block bests are (pbest, pbest cost) pairs (src/kernels.jl:85-91)
+  return sync_like_run(s, maxiters, w, wdamp, c1, c2, device_ms, 0u);
+}
+
+int pps_async_run(pps_swarm* s, int32_t maxiters, float w, float wdamp, float c1, float c2,
+                  float* device_ms) {
+  int rc = check_run(s, maxiters, w, wdamp, c1, c2);
+  if (rc) return rc;
+  if ((rc = launch_set_iter(s, s->t, w, wdamp))) return rc;
+  PPS_CUDA(cudaEventRecord(s->ev0, s->stream));
+  int lanes = 0;
+  if ((rc = launch_async(s, maxiters, c1, c2, &lanes))) return rc;
+  PPS_CUDA(cudaEventRecord(s->ev1, s->stream));
+  if ((rc = finish_timing(s, device_ms))) return rc;
+  PPS_CUDA(cudaStreamSynchronize(s->stream));
+  s->t += (uint32_t)maxiters;
+  return PPS_OK;
+}
+
+int pps_get_gbest(pps_swarm* s, float* u, float* cost, int64_t* idx) {
+  if (!s) return set_error(PPS_EINVAL, "swarm is NULL");
+  if (!s->initialized) return set_error(PPS_EINVAL, "swarm is not initialised");
+  int rc = use_device(s);
+  if (rc) return rc;
+  IterState st;
+  PPS_CUDA(cudaMemcpyAsync(&st, s->dv.st, sizeof(st), cudaMemcpyDeviceToHost, s->stream));
+  if (u) PPS_CUDA(cudaMemcpyAsync(u, s->dv.g, sizeof(float) * s->dv.dim, cudaMemcpyDeviceToHost, s->stream));
+  PPS_CUDA(cudaStreamSynchronize(s->stream));
+  if (cost) *cost = st.gcost;
+  if (idx) *idx = (int64_t)st.gidx;
+  return PPS_OK;
+}
+
+static int field_ptr(pps_swarm* s, int32_t field, float** dev, int* rows) {
+  switch (field) {
+    case PPS_FIELD_POSITION: *dev = s->dv.X; *rows = s->dv.dim; return PPS_OK;
+    case PPS_FIELD_VELOCITY: *dev = s->dv.V; *rows = s->dv.dim; return PPS_OK;
+    case PPS_FIELD_PBEST: *dev = s->dv.P; *rows = s->dv.dim; return PPS_OK;
+    case PPS_FIELD_PCOST: *dev = s->dv.pcost; *rows = 1; return PPS_OK;
+    case PPS_FIELD_COST: *dev = s->dv.cost; *rows = 1; return PPS_OK;
+    default: return set_error(PPS_EINVAL, "unknown field %d", field);
+  }
+}
+
+int pps_get_state(pps_swarm* s, int32_t field, float* out) {
+  if (!s || !out) return set_error(PPS_EINVAL, "NULL argument");
+  int rc = use_device(s);
+  if (rc) return rc;
+  float* dev;
+  int rows;
+  if ((rc = field_ptr(s, field, &dev, &rows))) return rc;
+  const size_t w = sizeof(float) * (size_t)s->dv.n;
+  PPS_CUDA(cudaMemcpy2DAsync(out, w, dev, sizeof(float) * (size_t)s->dv.npad, w, rows,
+                             cudaMemcpyDeviceToHost, s->stream));
+  PPS_CUDA(cudaStreamSynchronize(s->stream));
+  return PPS_OK;
+}
+
+int pps_set_state(pps_swarm* s, int32_t field, const float* in) {
+  if (!s || !in) return set_error(PPS_EINVAL, "NULL argument");
+  int rc = use_device(s);
+  if (rc) return rc;
+  float* dev;
+  int rows;
+  if ((rc = field_ptr(s, field, &dev, &rows))) return rc;
+  const size_t w = sizeof(float) * (size_t)s->dv.n;
+  PPS_CUDA(cudaMemcpy2DAsync(dev, sizeof(float) * (size_t)s->dv.npad, in, w, w, rows,
+                             cudaMemcpyHostToDevice, s->stream));
+  PPS_CUDA(cudaStreamSynchronize(s->stream));
+  return PPS_OK;
+}
+
+int pps_eval_objective(const pps_problem* prob, int64_t npoints, const float* x, float* f) {
+  int rc = check_problem(prob);
+  if (rc) return rc;
+  if (npoints < 0 || (npoints > 0 && (!x || !f))) return set_error(PPS_EINVAL, "bad points");
+  if (npoints == 0) return PPS_OK;
+  const int D = prob->dim;
+  float* dx = nullptr;
+  cudaStream_t st = nullptr;
+  PPS_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  const size_t bx = sizeof(float) * (size_t)D * (size_t)npoints;
+  cudaError_t e = cudaMallocAsync(&dx, bx + sizeof(float) * (size_t)npoints, st);
+  if (e != cudaSuccess) {
+    cudaStreamDestroy(st);
+    return cuda_error(e, "cudaMallocAsync");
+  }
+  float* df = dx + (size_t)D * (size_t)npoints;
+  ObjParams op = make_params(prob);
+  ObjData od{};
+  rc = PPS_OK;
+  if ((e = cudaMemcpyAsync(dx, x, bx, cudaMemcpyHostToDevice, st)) != cudaSuccess) rc = cuda_error(e, "cudaMemcpy");
+  if (!rc) rc = launch_eval(op, od, prob->objective, dx, npoints, npoints, df, st);
+  if (!rc && (e = cudaMemcpyAsync(f, df, sizeof(float) * npoints, cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+    rc = cuda_error(e, "cudaMemcpy");
+  cudaFreeAsync(dx, st);
+  if ((e = cudaStreamSynchronize(st)) != cudaSuccess && !rc) rc = cuda_error(e, "cudaStreamSynchronize");
+  cudaStreamDestroy(st);
+  return rc;
+}
+
+}  // extern "C"

@@ -1,0 +1,244 @@
+// pps_device.cuh -- device-side primitives shared by every PSO kernel.
+//
+// Random stream: Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11) with the
+// counter layout
+//   update draws: ctr = {particle, dim/2, iteration, PPS_TAG_STEP}, key = seed
+//                 out = {r1[2j], r2[2j], r1[2j+1], r2[2j+1]}
+//   init draws:   ctr = {particle, dim/4, 0, PPS_TAG_INIT},   out[k] -> dim 4j+k
+// so a draw depends only on (seed, particle, dim, iteration) -- never on the
+// block, slot or launch that computes it.  The reference draws r1, r2 with
+// rand() (src/kernels.jl:3,8) and positions with rand() (src/utils.jl:1-5).
+//
+// Arithmetic: the library is compiled with -fmad=false, so every + and * is a
+// single IEEE binary32 operation in the order written; fused multiply-adds are
+// spelled __fmaf_rn where the algorithm uses them.  cos(2 pi x), sin(2 pi x)
+// and exp(x) are this project's own: exact reduction y = 2x = n + r (|r|<=1/2)
+// followed by the Taylor series of cos(pi r) / sin(pi r) with coefficients
+// pi^k/k! rounded to binary32, and Cody-Waite reduction by ln 2 followed by
+// the Taylor series of exp.  Accuracy: <= 1.7 ulp (cos/sin), <= 0.9 ulp (exp).
+#pragma once
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+namespace pps {
+
+constexpr uint32_t kTagInit = 0x494E4954u;  // "INIT"
+constexpr uint32_t kTagStep = 0x50534F31u;  // "PSO1"
+
+enum Objective : int {
+  kSphere = 0,
+  kRosenbrock = 1,
+  kRastrigin = 2,
+  kAckley = 3,
+  kLvFit = 4,
+  kFhnFit = 5,
+  kMlp = 6,
+  kBeale = 16,
+  kBooth = 17,
+  kHimmelblau = 18,
+  kQuadratic = 19,
+  kBoundaryQuadratic = 20,
+};
+
+// ---------------------------------------------------------------- Philox
+struct Rand4 {
+  uint32_t a, b, c, d;
+};
+
+__device__ __forceinline__ Rand4 philox4x32_10(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3,
+                                               uint32_t k0, uint32_t k1) {
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    const uint64_t p0 = (uint64_t)0xD2511F53u * (uint64_t)c0;
+    const uint64_t p1 = (uint64_t)0xCD9E8D57u * (uint64_t)c2;
+    const uint32_t n0 = (uint32_t)(p1 >> 32) ^ c1 ^ k0;
+    const uint32_t n1 = (uint32_t)p1;
+    const uint32_t n2 = (uint32_t)(p0 >> 32) ^ c3 ^ k1;
+    const uint32_t n3 = (uint32_t)p0;
+    c0 = n0;
+    c1 = n1;
+    c2 = n2;
+    c3 = n3;
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+  return Rand4{c0, c1, c2, c3};
+}
+
+__device__ __forceinline__ float u01(uint32_t bits) {
+  return __fmul_rn(__uint2float_rn(bits >> 8), 0x1p-24f);
+}
+
+// ---------------------------------------------------------------- math
+__device__ __forceinline__ float cospi_poly(float a) {  // cos(pi a), 0 <= a <= 1/4
+  const float z = __fmul_rn(a, a);
+  float p = 0x1.f9d38ap-10f;             //  pi^12/12!
+  p = __fmaf_rn(p, z, -0x1.a6d1f2p-6f);  // -pi^10/10!
+  p = __fmaf_rn(p, z, 0x1.e1f506p-3f);   //  pi^8/8!
+  p = __fmaf_rn(p, z, -0x1.55d3c8p+0f);  // -pi^6/6!
+  p = __fmaf_rn(p, z, 0x1.03c1f0p+2f);   //  pi^4/4!
+  p = __fmaf_rn(p, z, -0x1.3bd3ccp+2f);  // -pi^2/2!
+  return __fmaf_rn(p, z, 1.0f);
+}
+__device__ __forceinline__ float sinpi_poly(float b) {  // sin(pi b), 0 <= b <= 1/4
+  const float z = __fmul_rn(b, b);
+  float p = -0x1.e30750p-8f;             // -pi^11/11!
+  p = __fmaf_rn(p, z, 0x1.507834p-4f);   //  pi^9/9!
+  p = __fmaf_rn(p, z, -0x1.32d2ccp-1f);  // -pi^7/7!
+  p = __fmaf_rn(p, z, 0x1.466bc6p+1f);   //  pi^5/5!
+  p = __fmaf_rn(p, z, -0x1.4abbcep+2f);  // -pi^3/3!
+  p = __fmaf_rn(p, z, 0x1.921fb6p+1f);   //  pi
+  return __fmul_rn(p, b);
+}
+__device__ __forceinline__ bool is_odd_integer(float n) {
+  return __fmul_rn(rintf(__fmul_rn(n, 0.5f)), 2.0f) != n;
+}
+__device__ __forceinline__ float cos2pi(float x) {
+  const float y = __fadd_rn(x, x);
+  const float n = rintf(y);
+  const float r = __fsub_rn(y, n);
+  const float a = fabsf(r);
+  const float c = (a <= 0.25f) ? cospi_poly(a) : sinpi_poly(__fsub_rn(0.5f, a));
+  return is_odd_integer(n) ? -c : c;
+}
+__device__ __forceinline__ float sin2pi(float x) {
+  const float y = __fadd_rn(x, x);
+  const float n = rintf(y);
+  const float r = __fsub_rn(y, n);
+  const float a = fabsf(r);
+  float s = (a <= 0.25f) ? sinpi_poly(a) : cospi_poly(__fsub_rn(0.5f, a));
+  if (r < 0.0f) s = -s;
+  return is_odd_integer(n) ? -s : s;
+}
+__device__ __forceinline__ float exp_f(float x) {
+  if (x != x) return x;
+  if (x > 88.72283f) return __int_as_float(0x7f800000);
+  if (x < -87.33654f) return 0.0f;
+  const float k = rintf(__fmul_rn(x, 0x1.715476p+0f));
+  float r = __fmaf_rn(-k, 0x1.62e430p-1f, x);
+  r = __fmaf_rn(-k, -0x1.05c610p-29f, r);
+  float p = 0x1.a01a02p-13f;
+  p = __fmaf_rn(p, r, 0x1.6c16c2p-10f);
+  p = __fmaf_rn(p, r, 0x1.111112p-7f);
+  p = __fmaf_rn(p, r, 0x1.555556p-5f);
+  p = __fmaf_rn(p, r, 0x1.555556p-3f);
+  p = __fmaf_rn(p, r, 0.5f);
+  p = __fmaf_rn(p, r, 1.0f);
+  p = __fmaf_rn(p, r, 1.0f);
+  const int ki = (int)k;
+  if (ki > 127) return __fmul_rn(__fmul_rn(p, __int_as_float(0x7f000000)), 2.0f);
+  return __fmul_rn(p, __int_as_float((ki + 127) << 23));
+}
+
+// orderable image of a cost (NaN above +inf) packed with the particle index:
+// the minimum key is the lowest cost, lowest index on ties.
+__device__ __forceinline__ unsigned long long argmin_key(float c, uint32_t idx) {
+  uint32_t o;
+  if (c != c) {
+    o = 0xFFFFFFFFu;
+  } else {
+    const uint32_t b = __float_as_uint(c);
+    o = (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+  }
+  return ((unsigned long long)o << 32) | (unsigned long long)idx;
+}
+
+// max.(x, lb) then min.(x, ub) (src/kernels.jl:15-16)
+__device__ __forceinline__ float clamp_lb_ub(float x, float lo, float hi) {
+  x = (x < lo) ? lo : x;
+  x = (x > hi) ? hi : x;
+  return x;
+}
+
+// the velocity update of src/kernels.jl:2-9 in Julia's broadcast order:
+// ((w*v) + ((c1*r1)*(p-x))) + ((c2*r2)*(g-x))
+__device__ __forceinline__ float velocity(float x, float v, float p, float g, float w, float c1,
+                                          float c2, float r1, float r2) {
+  const float a = __fmul_rn(w, v);
+  const float b = __fmul_rn(__fmul_rn(c1, r1), __fsub_rn(p, x));
+  const float c = __fmul_rn(__fmul_rn(c2, r2), __fsub_rn(g, x));
+  return __fadd_rn(__fadd_rn(a, b), c);
+}
+
+// ---------------------------------------------------------------- objectives
+// Objective parameters, passed by value to every kernel.
+struct ObjParams {
+  float p[8];
+  int np;
+  int dim;
+};
+__device__ __forceinline__ float prm(const ObjParams& o, int k, float dflt) {
+  return (k < o.np) ? o.p[k] : dflt;
+}
+
+// Streaming accumulator over dims d = 0..D-1 (separable and chained
+// objectives).  add(d, x) must be called in increasing d.
+template <int OBJ>
+struct Acc {
+  float s1 = 0.0f, s2 = 0.0f, prev = 0.0f;
+  __device__ __forceinline__ void add(const ObjParams& o, int d, float x) {
+    if constexpr (OBJ == kSphere) {
+      s1 = __fadd_rn(s1, __fmul_rn(x, x));
+    } else if constexpr (OBJ == kRosenbrock) {
+      // res += p2*(x[i+1]-x[i]^2)^2 + (p1-x[i])^2  (test/regression.jl:12-18)
+      if (d > 0) {
+        const float t = __fsub_rn(x, __fmul_rn(prev, prev));
+        const float u = __fsub_rn(prm(o, 0, 1.0f), prev);
+        s1 = __fadd_rn(s1, __fadd_rn(__fmul_rn(prm(o, 1, 100.0f), __fmul_rn(t, t)), __fmul_rn(u, u)));
+      }
+      prev = x;
+    } else if constexpr (OBJ == kRastrigin) {
+      s1 = __fadd_rn(s1, __fsub_rn(__fmul_rn(x, x), __fmul_rn(prm(o, 0, 10.0f), cos2pi(x))));
+    } else if constexpr (OBJ == kAckley) {
+      s1 = __fadd_rn(s1, __fmul_rn(x, x));
+      s2 = __fadd_rn(s2, cos2pi(__fmul_rn(prm(o, 2, 1.0f), x)));
+    } else {
+      // closed-form low-dimensional objectives keep x1, x2
+      if (d == 0) s1 = x;
+      if (d == 1) s2 = x;
+    }
+  }
+};
+
+__device__ __forceinline__ float sq(float a) { return __fmul_rn(a, a); }
+
+// combine slice sums s1, s2 into the objective value
+template <int OBJ>
+__device__ __forceinline__ float finalize(const ObjParams& o, float s1, float s2) {
+  const float Df = (float)o.dim;
+  if constexpr (OBJ == kRastrigin) {
+    return __fadd_rn(__fmul_rn(prm(o, 0, 10.0f), Df), s1);
+  } else if constexpr (OBJ == kAckley) {
+    const float a = prm(o, 0, 20.0f), b = prm(o, 1, 0.2f);
+    const float t1 = __fmul_rn(-a, exp_f(__fmul_rn(-b, __fsqrt_rn(__fdiv_rn(s1, Df)))));
+    const float t2 = exp_f(__fdiv_rn(s2, Df));
+    return __fadd_rn(__fadd_rn(__fsub_rn(t1, t2), a), 0x1.5bf0a8p+1f);
+  } else if constexpr (OBJ == kBeale) {
+    // (1.5 - x1 + x1 x2)^2 + (2.25 - x1 + x1 x2^2)^2 + (2.625 - x1 + x1 x2^3)^2
+    const float x1 = s1, x2 = s2, x22 = sq(x2), x23 = __fmul_rn(x22, x2);
+    const float a = __fadd_rn(__fsub_rn(1.5f, x1), __fmul_rn(x1, x2));
+    const float b = __fadd_rn(__fsub_rn(2.25f, x1), __fmul_rn(x1, x22));
+    const float c = __fadd_rn(__fsub_rn(2.625f, x1), __fmul_rn(x1, x23));
+    return __fadd_rn(__fadd_rn(sq(a), sq(b)), sq(c));
+  } else if constexpr (OBJ == kBooth) {
+    // (x1 + 2 x2 - 7)^2 + (2 x1 + x2 - 5)^2
+    const float a = __fsub_rn(__fadd_rn(s1, __fmul_rn(2.0f, s2)), 7.0f);
+    const float b = __fsub_rn(__fadd_rn(__fmul_rn(2.0f, s1), s2), 5.0f);
+    return __fadd_rn(sq(a), sq(b));
+  } else if constexpr (OBJ == kHimmelblau) {
+    // (x1^2 + x2 - 11)^2 + (x1 + x2^2 - 7)^2
+    const float a = __fsub_rn(__fadd_rn(sq(s1), s2), 11.0f);
+    const float b = __fsub_rn(__fadd_rn(s1, sq(s2)), 7.0f);
+    return __fadd_rn(sq(a), sq(b));
+  } else if constexpr (OBJ == kQuadratic) {
+    // p1 (x1 - 1)^2 + (x2 + 2)^2
+    return __fadd_rn(__fmul_rn(prm(o, 0, 1.0f), sq(__fsub_rn(s1, 1.0f))), sq(__fadd_rn(s2, 2.0f)));
+  } else if constexpr (OBJ == kBoundaryQuadratic) {
+    return sq(__fadd_rn(s1, 1.0f));  // (x1 + 1)^2
+  } else {
+    return s1;
+  }
+}
+
+}  // namespace pps

@@ -1,0 +1,111 @@
+// pps_internal.h -- host-side structures shared by the translation units of
+// libpps_cuda.so.  Not part of the public C ABI (include/pps.h is).
+#pragma once
+#include <cstdarg>
+#include <cstdint>
+#include <cstdio>
+#include <string>
+
+#include <cuda_runtime.h>
+
+#include "../../include/pps.h"
+#include "pps_device.cuh"
+
+namespace pps {
+
+// Device-resident iteration state of one swarm.  The last block of every
+// step launch publishes the new global best here and advances t and w, so
+// consecutive launches need no host round trip and capture into a CUDA graph
+// with identical parameters.
+struct IterState {
+  unsigned long long key;  // running argmin key of the current launch
+  unsigned int count;      // blocks finished in the current launch
+  unsigned int t;          // iteration counter of the next launch
+  float w;                 // inertia weight of the next launch
+  float wdamp;
+  float gcost;             // global best cost
+  unsigned int gidx;       // global best particle
+  unsigned int status;     // nonzero: a kernel detected a bad launch
+  unsigned int pad[7];
+};
+
+// Swarm state in HBM (structure of arrays, particle index fastest):
+//   X, V, P   [dim][npad] float   position, velocity, personal best
+//   pcost     [npad] float        personal best cost
+//   cost      [npad] float        current cost
+//   flag      [npad] uint8        1: personal best improved in the last step
+//                                  and not yet copied (P lags X by one step)
+//   g         [dim] float         global best position
+//   lb, ub    [dim] float
+struct SwarmDev {
+  float* X;
+  float* V;
+  float* P;
+  float* pcost;
+  float* cost;
+  uint8_t* flag;
+  float* g;
+  float* lb;
+  float* ub;
+  IterState* st;
+  int64_t n;
+  int64_t npad;
+  int dim;
+};
+
+struct ObjData {
+  const float* data;  // device copy of the objective's data (ODE obs, MLP set)
+  int64_t ndata;
+};
+
+}  // namespace pps
+
+struct pps_swarm {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  void* block = nullptr;  // the single device allocation
+  size_t bytes = 0;
+  pps::SwarmDev dv{};
+  pps::ObjParams op{};
+  pps::ObjData od{};
+  float* data_dev = nullptr;
+  int objective = 0;
+  uint64_t seed = 0;
+  uint32_t flags = 0;
+  uint32_t t = 0;  // host mirror of the iteration counter
+  int initialized = 0;
+  float* host_lb = nullptr;
+  float* host_ub = nullptr;
+  float* host_u0 = nullptr;
+  float* u0_dev = nullptr;
+  cudaGraphExec_t graph = nullptr;  // captured chunk of step launches
+  int graph_len = 0;
+  int graph_async_lanes = 0;  // run flags the graph was captured with
+  float graph_c1 = 0.0f, graph_c2 = 0.0f;
+  int sm_count = 0;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+
+namespace pps {
+
+int set_error(int code, const char* fmt, ...);
+int cuda_error(cudaError_t e, const char* what);
+
+#define PPS_CUDA(call)                                  \
+  do {                                                  \
+    cudaError_t e_ = (call);                            \
+    if (e_ != cudaSuccess) return pps::cuda_error(e_, #call); \
+  } while (0)
+
+// kernel launchers (pps_sync.cu, pps_async.cu)
+int launch_init(pps_swarm* s, int sampler, const float* u0_dev);
+int launch_set_iter(pps_swarm* s, uint32_t t, float w, float wdamp);
+int launch_sync_step(pps_swarm* s, float c1, float c2);
+int launch_materialize(pps_swarm* s);
+int launch_async(pps_swarm* s, int iters, float c1, float c2, int* lanes_out);
+int launch_eval(const ObjParams& op, const ObjData& od, int objective, const float* x, int64_t npts,
+                int64_t stride, float* f, cudaStream_t stream);
+int async_lanes(int dim, int* slice);
+int sync_grid(pps_swarm* s);
+
+}  // namespace pps

@@ -1,0 +1,23 @@
+"""ParallelParticleSwarms on GB300: the reference's solve/init/solve!/reinit!
+API over libpps_cuda.so (hand-written sm_103a kernels, C ABI in include/pps.h).
+
+Exports mirror src/ParallelParticleSwarms.jl:102-104.
+"""
+from ._lib import ArgumentError, PPSError
+from .algorithms import (BFGS, CUDA, GPUUniformSampler, GPUUnboundedSampler, HybridPSO, ParallelPSOKernel,
+                         ParallelSyncPSOKernel, PSOAlgorithm, SimpleLBFGS)
+from .problem import (REGISTRY, Objective, OptimizationProblem, ackley, beale, booth, boundary_quadratic,
+                      evaluate, fitzhugh_nagumo_fit, himmelblau, lotka_volterra_fit, mlp_regression,
+                      quadratic, rastrigin, rosenbrock, sphere)
+from .solve import (HybridPSOCache, OptimizationSolution, OptimizationStats, PSOCache, init, reinit_, solve,
+                    solve_)
+from .swarm import Swarm
+
+__all__ = [
+    "ParallelPSOKernel", "ParallelSyncPSOKernel", "PSOAlgorithm", "HybridPSO", "SimpleLBFGS", "BFGS",
+    "OptimizationProblem", "solve", "solve_", "init", "reinit_", "GPUUniformSampler", "GPUUnboundedSampler",
+    "PSOCache", "HybridPSOCache", "OptimizationSolution", "OptimizationStats", "Swarm", "PPSError",
+    "ArgumentError", "evaluate", "Objective", "REGISTRY", "sphere", "rosenbrock", "rastrigin", "ackley",
+    "lotka_volterra_fit", "fitzhugh_nagumo_fit", "mlp_regression", "beale", "booth", "himmelblau",
+    "quadratic", "boundary_quadratic", "CUDA",
+]

@@ -1,0 +1,119 @@
+"""OptimizationProblem and the registry of device objectives.
+
+The reference builds ``OptimizationProblem(f, u0, p; lb, ub)`` (SciMLBase) with
+an arbitrary Julia function ``f(x, p)`` that its kernels compile in
+(src/kernels.jl:33).  Through a C ABI the objective is chosen from the
+engine's registry; the objects below name the registry entries and carry
+their default parameters.  They are markers, not Python callables: objective
+values are always computed on the GPU (``evaluate`` below).
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib
+
+
+@dataclass(frozen=True)
+class Objective:
+    name: str
+    id: int
+    default_params: tuple = ()
+    max_dim: int | None = None
+
+    def __repr__(self) -> str:
+        return f"<objective {self.name}>"
+
+
+sphere = Objective("sphere", 0)
+rosenbrock = Objective("rosenbrock", 1, (1.0, 100.0))
+rastrigin = Objective("rastrigin", 2, (10.0,))
+ackley = Objective("ackley", 3, (20.0, 0.2, 1.0))
+lotka_volterra_fit = Objective("lotka_volterra_fit", 4)
+fitzhugh_nagumo_fit = Objective("fitzhugh_nagumo_fit", 5)
+mlp_regression = Objective("mlp_regression", 6)
+# closed-form objectives of test/lbfgs.jl:20-26
+beale = Objective("beale", 16, (), 2)
+booth = Objective("booth", 17, (), 2)
+himmelblau = Objective("himmelblau", 18, (), 2)
+quadratic = Objective("quadratic", 19, (1.0,), 2)
+boundary_quadratic = Objective("boundary_quadratic", 20, (), 1)
+
+REGISTRY = {o.name: o for o in (sphere, rosenbrock, rastrigin, ackley, lotka_volterra_fit,
+                               fitzhugh_nagumo_fit, mlp_regression, beale, booth, himmelblau,
+                               quadratic, boundary_quadratic)}
+
+
+def _f32(a, n=None):
+    if a is None:
+        return None
+    arr = np.ascontiguousarray(np.asarray(a, dtype=np.float32).reshape(-1))
+    if n is not None and arr.size != n:
+        raise _lib.ArgumentError(_lib.EINVAL, f"expected {n} values, got {arr.size}")
+    return arr
+
+
+@dataclass
+class OptimizationProblem:
+    """``OptimizationProblem(f, u0, p; lb, ub)``.
+
+    ``lb``/``ub`` of ``None`` mean unbounded (src/utils.jl:310-318).  ``data``
+    carries an objective's observations (ODE fits) or sample set (MLP).
+    """
+
+    f: Objective
+    u0: np.ndarray
+    p: np.ndarray | None = None
+    lb: np.ndarray | None = None
+    ub: np.ndarray | None = None
+    data: np.ndarray | None = None
+    _keep: list = field(default_factory=list, repr=False)
+
+    def __post_init__(self):
+        if isinstance(self.f, str):
+            self.f = REGISTRY[self.f]
+        if not isinstance(self.f, Objective):
+            raise _lib.ArgumentError(_lib.EINVAL, "f must be a registered objective (see problem.REGISTRY); "
+                                                  "the engine has no path for arbitrary Python callables")
+        self.u0 = _f32(self.u0)
+        self.dim = int(self.u0.size)
+        if self.p is None:
+            self.p = np.asarray(self.f.default_params, dtype=np.float32) if self.f.default_params else None
+        self.p = _f32(self.p)
+        self.lb = _f32(self.lb, self.dim) if self.lb is not None else None
+        self.ub = _f32(self.ub, self.dim) if self.ub is not None else None
+        self.data = _f32(self.data)
+
+    def remake(self, **kw) -> "OptimizationProblem":
+        args = dict(f=self.f, u0=self.u0, p=self.p, lb=self.lb, ub=self.ub, data=self.data)
+        args.update(kw)
+        return OptimizationProblem(**args)
+
+    def to_c(self) -> _lib.Problem:
+        """C struct view; the numpy buffers stay referenced by this problem."""
+        pr = _lib.Problem()
+        pr.objective = self.f.id
+        pr.dim = self.dim
+        pr.lb = _lib.fptr(self.lb)
+        pr.ub = _lib.fptr(self.ub)
+        pr.u0 = _lib.fptr(self.u0)
+        pr.params = _lib.fptr(self.p)
+        pr.nparams = 0 if self.p is None else int(self.p.size)
+        pr.data = _lib.fptr(self.data)
+        pr.ndata = 0 if self.data is None else int(self.data.size)
+        return pr
+
+
+def evaluate(prob: OptimizationProblem, x) -> np.ndarray:
+    """Objective values at points ``x`` (shape (npoints, dim) or (dim,)) on the GPU."""
+    x = np.asarray(x, dtype=np.float32)
+    single = x.ndim == 1
+    pts = x.reshape(-1, prob.dim)
+    soa = np.ascontiguousarray(pts.T)
+    out = np.empty(pts.shape[0], dtype=np.float32)
+    pr = prob.to_c()
+    _lib.check(_lib.load().pps_eval_objective(ctypes.byref(pr), pts.shape[0], _lib.fptr(soa), _lib.fptr(out)))
+    return out[0] if single else out

@@ -1,0 +1,106 @@
+"""Thin owner of one ``pps_swarm`` handle (device-resident swarm state)."""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from .problem import OptimizationProblem
+
+# defaults of src/lowerlevel_solve.jl:6-7 and src/kernels.jl:130-131
+W_DEFAULT = 0.7298
+WDAMP_DEFAULT = 1.0
+C1_DEFAULT = 1.4962
+C2_DEFAULT = 1.4962
+
+
+class Swarm:
+    """Device swarm of ``n`` particles for ``prob`` (SoA state in HBM)."""
+
+    def __init__(self, prob: OptimizationProblem, n: int, seed: int = 0, gbest_from_position: bool = False):
+        self.prob = prob
+        self.n = int(n)
+        self.dim = prob.dim
+        self.seed = int(seed) & 0xFFFFFFFFFFFFFFFF
+        self._lib = _lib.load()
+        self._h = ctypes.c_void_p()
+        flags = _lib.FLAG_GBEST_FROM_POSITION if gbest_from_position else 0
+        pr = prob.to_c()
+        _lib.check(self._lib.pps_swarm_create(ctypes.byref(pr), self.n, self.seed, flags, ctypes.byref(self._h)))
+        self.last_device_ms = 0.0
+
+    # -- lifetime ---------------------------------------------------------
+    def close(self) -> None:
+        if getattr(self, "_h", None) and self._h.value:
+            self._lib.pps_swarm_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- operations -------------------------------------------------------
+    def init(self, sampler: int = _lib.SAMPLER_AUTO) -> "Swarm":
+        _lib.check(self._lib.pps_swarm_init(self._h, int(sampler)))
+        return self
+
+    def _run(self, fn, maxiters, w, wdamp, c1, c2) -> float:
+        ms = ctypes.c_float(0.0)
+        _lib.check(fn(self._h, int(maxiters), float(w), float(wdamp), float(c1), float(c2), ctypes.byref(ms)))
+        self.last_device_ms = float(ms.value)
+        return self.last_device_ms
+
+    def sync_run(self, maxiters, w=W_DEFAULT, wdamp=WDAMP_DEFAULT, c1=C1_DEFAULT, c2=C2_DEFAULT) -> float:
+        return self._run(self._lib.pps_sync_run, maxiters, w, wdamp, c1, c2)
+
+    def async_run(self, maxiters, w=W_DEFAULT, wdamp=WDAMP_DEFAULT, c1=C1_DEFAULT, c2=C2_DEFAULT) -> float:
+        return self._run(self._lib.pps_async_run, maxiters, w, wdamp, c1, c2)
+
+    def queue_run(self, maxiters, w=W_DEFAULT, wdamp=WDAMP_DEFAULT, c1=C1_DEFAULT, c2=C2_DEFAULT) -> float:
+        return self._run(self._lib.pps_queue_run, maxiters, w, wdamp, c1, c2)
+
+    # -- state ------------------------------------------------------------
+    def gbest(self):
+        u = np.empty(self.dim, dtype=np.float32)
+        c = ctypes.c_float()
+        i = ctypes.c_int64()
+        _lib.check(self._lib.pps_get_gbest(self._h, _lib.fptr(u), ctypes.byref(c), ctypes.byref(i)))
+        return u, float(c.value), int(i.value)
+
+    def get(self, field: int) -> np.ndarray:
+        rows = self.dim if field in (_lib.FIELD_POSITION, _lib.FIELD_VELOCITY, _lib.FIELD_PBEST) else 1
+        out = np.empty((rows, self.n), dtype=np.float32)
+        _lib.check(self._lib.pps_get_state(self._h, int(field), _lib.fptr(out)))
+        return out if rows > 1 else out[0]
+
+    def set(self, field: int, values) -> None:
+        rows = self.dim if field in (_lib.FIELD_POSITION, _lib.FIELD_VELOCITY, _lib.FIELD_PBEST) else 1
+        arr = np.ascontiguousarray(np.asarray(values, dtype=np.float32).reshape(rows, self.n))
+        _lib.check(self._lib.pps_set_state(self._h, int(field), _lib.fptr(arr)))
+
+    def positions(self) -> np.ndarray:
+        """(dim, n) SoA positions."""
+        return self.get(_lib.FIELD_POSITION)
+
+    def state(self) -> dict:
+        return {
+            "x": self.get(_lib.FIELD_POSITION),
+            "v": self.get(_lib.FIELD_VELOCITY),
+            "pbest": self.get(_lib.FIELD_PBEST),
+            "pcost": self.get(_lib.FIELD_PCOST),
+            "cost": self.get(_lib.FIELD_COST),
+        }
+
+    def info(self) -> _lib.SwarmInfo:
+        inf = _lib.SwarmInfo()
+        _lib.check(self._lib.pps_swarm_info_get(self._h, ctypes.byref(inf)))
+        return inf
