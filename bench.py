@@ -189,6 +189,8 @@ def main():
     ap.add_argument("--iters", type=int, default=ITERS)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-async", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU-baseline sample")
     args = ap.parse_args()
     rank, world, local = dist_env()
 
@@ -247,7 +249,7 @@ def main():
 
     # ---- async at the same size -----------------------------------------
     async_rate = None
-    if rank == 0:
+    if rank == 0 and not args.no_async:
         sa = pps.Swarm(prob, N_PARTICLES, seed=seed0 + 1)
         sa.init()
         sa.async_run(50)
@@ -280,7 +282,9 @@ def main():
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        n_s, it_s = 1 << 18, 6
+        n_s = 1 << 18
+        rate0, _ = cpu_oracle_rate(n_s, 1, threads)  # size the sample to about --cpu-seconds
+        it_s = max(1, min(200, int(args.cpu_seconds * rate0 / n_s)))
         rate, secs = cpu_oracle_rate(n_s, it_s, threads)
         cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"{n_s} particles x {DIM}-D Rastrigin, {it_s} sync iterations ({secs:.1f} s), "
@@ -304,7 +308,7 @@ def main():
                          "avg_launch_ms": launch_ms},
             "cpu_baseline": cpu,
             "clocks": clk.summary(),
-            "async": {"metric": METRIC, "value": async_rate, "unit": UNIT,
+            "async": None if async_rate is None else {"metric": METRIC, "value": async_rate, "unit": UNIT,
                       "workload": "ParallelPSOKernel(global_update=false), same size, one launch"},
             "final_gbest_cost": gcost,
         }

@@ -77,10 +77,11 @@ class Swarm:
         return u, float(c.value), int(i.value)
 
     def get(self, field: int) -> np.ndarray:
-        rows = self.dim if field in (_lib.FIELD_POSITION, _lib.FIELD_VELOCITY, _lib.FIELD_PBEST) else 1
-        out = np.empty((rows, self.n), dtype=np.float32)
+        """(dim, n) for position / velocity / pbest, (n,) for the costs."""
+        vec = field in (_lib.FIELD_POSITION, _lib.FIELD_VELOCITY, _lib.FIELD_PBEST)
+        out = np.empty((self.dim if vec else 1, self.n), dtype=np.float32)
         _lib.check(self._lib.pps_get_state(self._h, int(field), _lib.fptr(out)))
-        return out if rows > 1 else out[0]
+        return out if vec else out[0]
 
     def set(self, field: int, values) -> None:
         rows = self.dim if field in (_lib.FIELD_POSITION, _lib.FIELD_VELOCITY, _lib.FIELD_PBEST) else 1
