@@ -168,6 +168,55 @@ PPS_API int pps_set_state(pps_swarm* s, int32_t field, const float* in);
  * the device; used for sol.objective = f(u, p) (src/solve.jl:54-57) */
 PPS_API int pps_eval_objective(const pps_problem* prob, int64_t npoints, const float* x, float* f);
 
+/* ---- caller-owned device buffers, no allocation ---- */
+/* A swarm whose device arrays belong to the caller.  All pointers are DEVICE
+ * pointers, 16-byte aligned.  Element (particle i, dim d) is at [d*ld + i];
+ * ld is a multiple of 32 with n <= ld; columns n..ld-1 are padding that the
+ * kernels overwrite.  pcost and cost hold ld floats, lb, ub and g dim floats. */
+typedef struct pps_device_swarm {
+  int64_t n;
+  int64_t ld;
+  int32_t dim;
+  float* x;         /* positions, in/out */
+  float* v;         /* velocities, in/out */
+  float* pbest;     /* personal bests, in/out */
+  float* pcost;     /* personal best costs, in/out */
+  float* cost;      /* current costs, out */
+  const float* lb;  /* lower bounds (may hold -inf) */
+  const float* ub;  /* upper bounds (may hold +inf) */
+  float* g;         /* global best position, out */
+} pps_device_swarm;
+
+/* The synchronous run of pps_sync_run on buffers the caller owns, with no
+ * allocation: no cudaMalloc, cudaFree, stream or event creation.  It has no
+ * counterpart in the reference (whose Julia host allocates through
+ * KernelAbstractions).  It is for callers that cannot let a library
+ * allocate: memory held by a pooled allocator such as CUDA.jl's, where a
+ * hidden cudaMalloc can fail while the pool holds the memory and
+ * synchronises the device, or a host framework that hands every buffer to
+ * its plugins from its own arena.
+ *   objective, params, nparams  the registered objective (pps_objective)
+ *   seed, iteration             Philox key and the iteration counter of the
+ *                               first step (0 after an init; add maxiters per call)
+ *   flags                       PPS_FLAG_GBEST_FROM_POSITION or 0
+ *   stream                      cudaStream_t to launch on (NULL: the legacy default stream)
+ *   gcost_out, gidx_out         host pointers, may be NULL; when given, the call
+ *                               waits for the stream and returns the global best
+ * The run starts from the argmin of pcost (its pbest, or its position with
+ * PPS_FLAG_GBEST_FROM_POSITION) and leaves the global best in g.
+ * Scratch: the per-iteration argmin state and one byte per particle live in a
+ * static device array of 1 MiB + 256 B in the library, so n and ld are limited
+ * to 1,048,576 particles (larger requests fail with PPS_EINVAL before any
+ * device work).  Every GPU that loads the library holds that array until the
+ * process exits.  The first call on a device looks up the array's address
+ * with that device current; make it before any stream capture begins.  Each
+ * call clears the part it uses, but all calls share the array: calls that
+ * overlap on the GPU (other streams, unordered host threads) race. */
+PPS_API int pps_sync_run_noalloc(int32_t objective, const float* params, int32_t nparams,
+                                 const pps_device_swarm* swarm, uint64_t seed, uint32_t iteration,
+                                 int32_t maxiters, float w, float wdamp, float c1, float c2,
+                                 uint32_t flags, void* stream, float* gcost_out, int64_t* gidx_out);
+
 #ifdef __cplusplus
 }
 #endif

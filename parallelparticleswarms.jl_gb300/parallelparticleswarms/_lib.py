@@ -66,6 +66,24 @@ class SwarmInfo(ctypes.Structure):
     ]
 
 
+class DeviceSwarm(ctypes.Structure):
+    """pps_device_swarm: a swarm in device buffers owned by the caller."""
+
+    _fields_ = [
+        ("n", ctypes.c_int64),
+        ("ld", ctypes.c_int64),
+        ("dim", ctypes.c_int32),
+        ("x", ctypes.c_void_p),
+        ("v", ctypes.c_void_p),
+        ("pbest", ctypes.c_void_p),
+        ("pcost", ctypes.c_void_p),
+        ("cost", ctypes.c_void_p),
+        ("lb", ctypes.c_void_p),
+        ("ub", ctypes.c_void_p),
+        ("g", ctypes.c_void_p),
+    ]
+
+
 _P = ctypes.c_void_p
 _SIGNATURES = {
     "pps_version": (ctypes.c_int32, []),
@@ -87,6 +105,10 @@ _SIGNATURES = {
     "pps_get_state": (ctypes.c_int, [_P, ctypes.c_int32, c_float_p]),
     "pps_set_state": (ctypes.c_int, [_P, ctypes.c_int32, c_float_p]),
     "pps_eval_objective": (ctypes.c_int, [ctypes.POINTER(Problem), ctypes.c_int64, c_float_p, c_float_p]),
+    "pps_sync_run_noalloc": (ctypes.c_int, [ctypes.c_int32, c_float_p, ctypes.c_int32, ctypes.POINTER(DeviceSwarm),
+                                            ctypes.c_uint64, ctypes.c_uint32, ctypes.c_int32, ctypes.c_float,
+                                            ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_uint32,
+                                            ctypes.c_void_p, c_float_p, ctypes.POINTER(ctypes.c_int64)]),
 }
 
 _lock = threading.Lock()
