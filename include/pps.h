@@ -103,7 +103,11 @@ enum {
   PPS_FIELD_VELOCITY = 1, /* dim*n */
   PPS_FIELD_PBEST = 2,    /* dim*n */
   PPS_FIELD_PCOST = 3,    /* n */
-  PPS_FIELD_COST = 4      /* n */
+  PPS_FIELD_COST = 4,     /* n */
+  /* results of the last HybridPSO local stage (read-only) */
+  PPS_FIELD_LOCAL_X = 5,     /* dim*n: each particle's local optimum */
+  PPS_FIELD_LOCAL_F = 6,     /* n: its objective, non-finite -> +Inf */
+  PPS_FIELD_LOCAL_ITERS = 7  /* n: iterations used (as float) */
 };
 
 typedef struct pps_swarm_info {
@@ -157,6 +161,27 @@ PPS_API int pps_async_run(pps_swarm* s, int32_t maxiters, float w, float wdamp, 
  * synchronous iteration. */
 PPS_API int pps_queue_run(pps_swarm* s, int32_t maxiters, float w, float wdamp, float c1, float c2,
                   float* device_ms);
+
+/* ---- HybridPSO local stage (src/hybrid.jl:47-158) ---- */
+typedef struct pps_local_opts {
+  int32_t history;        /* L-BFGS pairs m (1..16); ignored by the Broyden stage */
+  int32_t maxiters;       /* local_maxiters (the reference's default is 50) */
+  float armijo_c1;        /* sufficient-decrease constant of the backtracking search */
+  float gtol;             /* stop when ||projected gradient|| (L-BFGS) or ||grad|| (Broyden) <= gtol */
+  int32_t max_backtracks; /* halvings of the step before a search fails */
+} pps_local_opts;
+/* HybridPSO{SimpleLBFGS}: one projected L-BFGS per particle from its personal
+ * best within [lb, ub] (lbfgs_run!, src/lbfgs.jl:9-21), then the argmin over
+ * the results (src/hybrid.jl:145-146).  u (dim floats), f and idx receive the
+ * best local result; every particle's result is in PPS_FIELD_LOCAL_*.
+ * dim <= 64. */
+PPS_API int pps_hybrid_lbfgs(pps_swarm* s, const pps_local_opts* opts, float* u, float* f, int64_t* idx,
+                             float* device_ms);
+/* HybridPSO{BFGS}: Broyden's method on grad f = 0 from every particle's current
+ * position, gradient 1e15 outside the box grown by twice its width
+ * (simplebfgs_run!, src/hybrid.jl:15-45), then the argmin.  dim <= 16. */
+PPS_API int pps_hybrid_bfgs(pps_swarm* s, const pps_local_opts* opts, float* u, float* f, int64_t* idx,
+                            float* device_ms);
 
 /* ---- results ---- */
 /* global best position (dim floats), cost and particle index; any may be NULL */

@@ -213,6 +213,7 @@ int pps_swarm_destroy(pps_swarm* s) {
   if (s->ev1) cudaEventDestroy(s->ev1);
   if (s->stream) cudaStreamDestroy(s->stream);
   if (s->block) cudaFree(s->block);
+  if (s->local_block) cudaFree(s->local_block);
   free(s->host_lb);
   if (dev >= 0 && dev != s->device) cudaSetDevice(dev);
   delete s;
@@ -249,6 +250,7 @@ int pps_swarm_init(pps_swarm* s, int32_t sampler) {
   PPS_CUDA(cudaStreamSynchronize(s->stream));
   s->t = 0;
   s->initialized = 1;
+  s->local_valid = 0;
   return PPS_OK;
 }
 
@@ -406,6 +408,10 @@ static int field_ptr(pps_swarm* s, int32_t field, float** dev, int* rows) {
     case PPS_FIELD_PBEST: *dev = s->dv.P; *rows = s->dv.dim; return PPS_OK;
     case PPS_FIELD_PCOST: *dev = s->dv.pcost; *rows = 1; return PPS_OK;
     case PPS_FIELD_COST: *dev = s->dv.cost; *rows = 1; return PPS_OK;
+    case PPS_FIELD_LOCAL_X:
+    case PPS_FIELD_LOCAL_F:
+    case PPS_FIELD_LOCAL_ITERS:
+      return local_field(s, field, dev, rows);
     default: return set_error(PPS_EINVAL, "unknown field %d", field);
   }
 }
@@ -426,6 +432,7 @@ int pps_get_state(pps_swarm* s, int32_t field, float* out) {
 
 int pps_set_state(pps_swarm* s, int32_t field, const float* in) {
   if (!s || !in) return set_error(PPS_EINVAL, "NULL argument");
+  if (field > PPS_FIELD_COST) return set_error(PPS_EINVAL, "field %d is read-only", field);
   int rc = use_device(s);
   if (rc) return rc;
   float* dev;

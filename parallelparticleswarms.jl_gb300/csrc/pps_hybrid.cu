@@ -1,0 +1,444 @@
+// pps_hybrid.cu -- HybridPSO's local stage: one local optimiser per particle.
+//
+// Reference: src/hybrid.jl:100-158 launches lbfgs_run! (src/lbfgs.jl:9-21),
+// one SimpleOptimization._lbfgs per particle started from its personal best,
+// then copies result_fx to the host and keeps its findmin if it beats the
+// swarm best (:145-150).  The BFGS variant (src/hybrid.jl:33-98) runs
+// SimpleNonlinearSolve.SimpleBroyden on grad f = 0 from every particle's
+// current position, with the gradient replaced by 1e15 outside the box grown
+// by twice its width (BoundedGrad, :15-31).
+//
+// Algorithms (the published ones the workload names; the third-party code is
+// not part of the reference tree):
+//   L-BFGS  projected two-loop recursion (Nocedal & Wright, Alg. 7.4), history
+//           m, H0 = (s'y / y'y) I, backtracking Armijo (c1) along the projected
+//           path, steepest-descent restart when the direction does not descend,
+//           stop on ||projected gradient|| <= gtol, maxiters, or a failed search.
+//   Broyden inverse-Jacobian ("good") update by Sherman-Morrison, J0 = I, a
+//           halving backtrack on ||F||^2, stop on ||F|| <= gtol.
+// Every dot product is a sequential binary32 sum (no fusion), the operation
+// sequence of the CPU restatement, so results are bit-identical to it.
+//
+// GB300 design: one thread per particle; vectors of the particle's dimension
+// live in registers (compile-time bound MAXD), the L-BFGS history (2 m D
+// floats) and the Broyden matrix (D^2) in thread-local memory, which stays
+// L1/L2 resident.  The argmin over the per-particle results (the reference's
+// host findmin) runs on the device with the 64-bit (cost, index) key.
+#include <cmath>
+
+#include "pps_internal.h"
+#include "pps_objgrad.cuh"
+
+namespace pps {
+
+constexpr int kMaxHistory = 16;
+
+struct LocalOpts {
+  int history;
+  int maxiters;
+  float c1;
+  float gtol;
+  int max_backtracks;
+};
+
+template <int MAXD>
+__device__ __forceinline__ float dotv(const float (&a)[MAXD], const float (&b)[MAXD], int D) {
+  float s = 0.0f;
+  PPS_FOR_D(d) s = __fadd_rn(s, __fmul_rn(a[d], b[d]));
+  return s;
+}
+
+template <int OBJ, int MAXD>
+__global__ void __launch_bounds__(128) k_lbfgs(const float* __restrict__ X0, int64_t ld, int64_t n, ObjParams op,
+                                               const float* __restrict__ lbp, const float* __restrict__ ubp,
+                                               LocalOpts o, float* __restrict__ xout, float* __restrict__ fout,
+                                               float* __restrict__ itout) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int D = op.dim;
+  const int m = o.history;
+  float lb[MAXD], ub[MAXD], x[MAXD], g[MAXD], pg[MAXD], q[MAXD], dir[MAXD], xn[MAXD], gn[MAXD];
+  float S[kMaxHistory][MAXD], Y[kMaxHistory][MAXD], rho[kMaxHistory], alpha[kMaxHistory];
+  PPS_FOR_D(d) {
+    lb[d] = lbp[d];
+    ub[d] = ubp[d];
+    x[d] = clamp_lb_ub(X0[(int64_t)d * ld + i], lb[d], ub[d]);
+  }
+  int hist = 0, head = 0;
+  float f = obj_grad<OBJ, MAXD>(op, x, g, D);
+  int it = 0;
+  for (; it < o.maxiters; ++it) {
+    if (!isfinite(f)) break;
+    PPS_FOR_D(d) {
+      const bool hold = (x[d] <= lb[d] && g[d] > 0.0f) || (x[d] >= ub[d] && g[d] < 0.0f);
+      pg[d] = hold ? 0.0f : g[d];
+    }
+    const float gn2 = dotv<MAXD>(pg, pg, D);
+    if (__fsqrt_rn(gn2) <= o.gtol) break;
+    PPS_FOR_D(d) q[d] = pg[d];
+    for (int j = 0; j < hist; ++j) {  // newest pair first
+      const int slot = (head - 1 - j + m) % m;
+      float sq_ = 0.0f;
+      PPS_FOR_D(d) sq_ = __fadd_rn(sq_, __fmul_rn(S[slot][d], q[d]));
+      const float a = __fmul_rn(rho[slot], sq_);
+      alpha[slot] = a;
+      PPS_FOR_D(d) q[d] = __fsub_rn(q[d], __fmul_rn(a, Y[slot][d]));
+    }
+    float gamma = 1.0f;
+    if (hist > 0) {
+      const int nw = (head - 1 + m) % m;
+      float sy = 0.0f, yy = 0.0f;
+      PPS_FOR_D(d) sy = __fadd_rn(sy, __fmul_rn(S[nw][d], Y[nw][d]));
+      PPS_FOR_D(d) yy = __fadd_rn(yy, __fmul_rn(Y[nw][d], Y[nw][d]));
+      gamma = __fdiv_rn(sy, yy);
+    }
+    PPS_FOR_D(d) q[d] = __fmul_rn(gamma, q[d]);
+    for (int j = hist - 1; j >= 0; --j) {  // oldest pair first
+      const int slot = (head - 1 - j + m) % m;
+      float yq = 0.0f;
+      PPS_FOR_D(d) yq = __fadd_rn(yq, __fmul_rn(Y[slot][d], q[d]));
+      const float b = __fmul_rn(rho[slot], yq);
+      PPS_FOR_D(d) q[d] = __fadd_rn(q[d], __fmul_rn(S[slot][d], __fsub_rn(alpha[slot], b)));
+    }
+    PPS_FOR_D(d) {
+      const float dd = -q[d];
+      const bool hold = (x[d] <= lb[d] && dd < 0.0f) || (x[d] >= ub[d] && dd > 0.0f);
+      dir[d] = hold ? 0.0f : dd;
+    }
+    float gd = dotv<MAXD>(g, dir, D);
+    if (!(gd < 0.0f)) {  // not a descent direction: restart from steepest descent
+      hist = 0;
+      head = 0;
+      PPS_FOR_D(d) dir[d] = -pg[d];
+      gd = dotv<MAXD>(g, dir, D);
+      if (!(gd < 0.0f)) break;
+    }
+    float step = 1.0f;
+    bool ok = false;
+    float fn = f;
+    for (int bt = 0; bt < o.max_backtracks; ++bt) {
+      PPS_FOR_D(d) xn[d] = clamp_lb_ub(__fadd_rn(x[d], __fmul_rn(step, dir[d])), lb[d], ub[d]);
+      fn = obj_value<OBJ, MAXD>(op, xn, D);
+      float dec = 0.0f;
+      PPS_FOR_D(d) dec = __fadd_rn(dec, __fmul_rn(g[d], __fsub_rn(xn[d], x[d])));
+      if (fn <= __fadd_rn(f, __fmul_rn(o.c1, dec))) {
+        ok = true;
+        break;
+      }
+      step = __fmul_rn(step, 0.5f);
+    }
+    if (!ok) break;
+    fn = obj_grad<OBJ, MAXD>(op, xn, gn, D);
+    float sy = 0.0f;
+    float sv[MAXD], yv[MAXD];
+    PPS_FOR_D(d) {
+      sv[d] = __fsub_rn(xn[d], x[d]);
+      yv[d] = __fsub_rn(gn[d], g[d]);
+      sy = __fadd_rn(sy, __fmul_rn(sv[d], yv[d]));
+    }
+    if (sy > 1e-12f) {
+      PPS_FOR_D(d) {
+        S[head][d] = sv[d];
+        Y[head][d] = yv[d];
+      }
+      rho[head] = __fdiv_rn(1.0f, sy);
+      head = (head + 1) % m;
+      if (hist < m) ++hist;
+    }
+    PPS_FOR_D(d) {
+      x[d] = xn[d];
+      g[d] = gn[d];
+    }
+    f = fn;
+  }
+  PPS_FOR_D(d) xout[(int64_t)d * ld + i] = x[d];
+  fout[i] = isfinite(f) ? f : __int_as_float(0x7f800000);  // non-finite -> Inf (src/lbfgs.jl:20)
+  itout[i] = (float)it;
+}
+
+// BoundedGrad (src/hybrid.jl:23-31): the gradient inside the box grown by
+// twice its width, 1e15 in every component outside it
+template <int OBJ, int MAXD>
+__device__ __forceinline__ void bounded_grad(const ObjParams& op, const float (&x)[MAXD], const float (&lb)[MAXD],
+                                             const float (&ub)[MAXD], float (&F)[MAXD], int D) {
+  bool in_box = true;
+  PPS_FOR_D(d) {
+    const float w = __fsub_rn(ub[d], lb[d]);
+    if (!isfinite(x[d]) || x[d] < __fsub_rn(lb[d], __fmul_rn(2.0f, w)) || x[d] > __fadd_rn(ub[d], __fmul_rn(2.0f, w)))
+      in_box = false;
+  }
+  if (in_box) {
+    obj_grad<OBJ, MAXD>(op, x, F, D);
+  } else {
+    PPS_FOR_D(d) F[d] = 1.0e15f;
+  }
+}
+
+template <int OBJ, int MAXD>
+__global__ void __launch_bounds__(128) k_broyden(const float* __restrict__ X0, int64_t ld, int64_t n, ObjParams op,
+                                                 const float* __restrict__ lbp, const float* __restrict__ ubp,
+                                                 LocalOpts o, float* __restrict__ xout, float* __restrict__ fout,
+                                                 float* __restrict__ itout) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int D = op.dim;
+  float lb[MAXD], ub[MAXD], x[MAXD], F[MAXD], xn[MAXD], Fn[MAXD], dx[MAXD], dF[MAXD], JdF[MAXD], dxJ[MAXD], step[MAXD];
+  float J[MAXD][MAXD];
+  PPS_FOR_D(d) {
+    lb[d] = lbp[d];
+    ub[d] = ubp[d];
+    x[d] = X0[(int64_t)d * ld + i];
+  }
+  PPS_FOR_D(a) {
+    PPS_FOR_D(b) J[a][b] = (a == b) ? 1.0f : 0.0f;
+  }
+  bounded_grad<OBJ, MAXD>(op, x, lb, ub, F, D);
+  float phi = dotv<MAXD>(F, F, D);
+  int it = 0;
+  for (; it < o.maxiters; ++it) {
+    if (!(__fsqrt_rn(phi) > o.gtol)) break;
+    PPS_FOR_D(a) {
+      float s = 0.0f;
+      PPS_FOR_D(b) s = __fadd_rn(s, __fmul_rn(J[a][b], F[b]));
+      step[a] = -s;
+    }
+    float sc = 1.0f, phin = phi;
+    bool ok = false;
+    for (int bt = 0; bt < o.max_backtracks; ++bt) {
+      PPS_FOR_D(d) xn[d] = __fadd_rn(x[d], __fmul_rn(sc, step[d]));
+      bounded_grad<OBJ, MAXD>(op, xn, lb, ub, Fn, D);
+      phin = dotv<MAXD>(Fn, Fn, D);
+      if (phin < phi) {
+        ok = true;
+        break;
+      }
+      sc = __fmul_rn(sc, 0.5f);
+    }
+    if (!ok) break;
+    PPS_FOR_D(d) {
+      dx[d] = __fsub_rn(xn[d], x[d]);
+      dF[d] = __fsub_rn(Fn[d], F[d]);
+    }
+    PPS_FOR_D(a) {
+      float s = 0.0f;
+      PPS_FOR_D(b) s = __fadd_rn(s, __fmul_rn(J[a][b], dF[b]));
+      JdF[a] = s;
+    }
+    PPS_FOR_D(b) {
+      float s = 0.0f;
+      PPS_FOR_D(a) s = __fadd_rn(s, __fmul_rn(dx[a], J[a][b]));
+      dxJ[b] = s;
+    }
+    const float den = dotv<MAXD>(dx, JdF, D);
+    if (den != 0.0f && isfinite(den)) {
+      PPS_FOR_D(a) {
+        const float c = __fdiv_rn(__fsub_rn(dx[a], JdF[a]), den);
+        PPS_FOR_D(b) J[a][b] = __fadd_rn(J[a][b], __fmul_rn(c, dxJ[b]));
+      }
+    }
+    PPS_FOR_D(d) {
+      x[d] = xn[d];
+      F[d] = Fn[d];
+    }
+    phi = phin;
+  }
+  PPS_FOR_D(d) xout[(int64_t)d * ld + i] = x[d];
+  const float v = obj_value<OBJ, MAXD>(op, x, D);
+  fout[i] = isfinite(v) ? v : __int_as_float(0x7f800000);  // NaN / Inf -> Inf (src/hybrid.jl:44)
+  itout[i] = (float)it;
+}
+
+// argmin over the local results (findmin, src/hybrid.jl:145-146) and gather
+// of the winner's point; key/count live in the result block
+struct ArgminSlot {
+  unsigned long long key;
+  unsigned int count;
+  unsigned int idx;
+  float cost;
+  unsigned int pad[59];
+};
+
+__global__ void k_reset_slot(ArgminSlot* sl) {
+  sl->key = ~0ull;
+  sl->count = 0u;
+}
+
+__global__ void k_argmin_gather(const float* __restrict__ f, const float* __restrict__ X, int64_t n, int64_t ld, int D,
+                                ArgminSlot* sl, float* __restrict__ u) {
+  __shared__ unsigned long long wmin[32];
+  __shared__ int last;
+  unsigned long long key = ~0ull;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const unsigned long long k = argmin_key(f[i], (uint32_t)i);
+    key = k < key ? k : key;
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    const unsigned long long o = __shfl_xor_sync(0xffffffffu, key, off);
+    key = o < key ? o : key;
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) wmin[warp] = key;
+  __syncthreads();
+  if (warp == 0) {
+    unsigned long long k = (lane < (int)(blockDim.x >> 5)) ? wmin[lane] : ~0ull;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      const unsigned long long o = __shfl_xor_sync(0xffffffffu, k, off);
+      k = o < k ? o : k;
+    }
+    if (lane == 0) {
+      atomicMin(&sl->key, k);
+      __threadfence();
+      last = (atomicAdd(&sl->count, 1u) == gridDim.x - 1) ? 1 : 0;
+    }
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  const unsigned long long best = atomicAdd(&sl->key, 0ull);
+  const uint32_t gi = (uint32_t)best;
+  for (int d = threadIdx.x; d < D; d += blockDim.x) u[d] = __ldcg(X + (int64_t)d * ld + gi);
+  if (threadIdx.x == 0) {
+    sl->idx = gi;
+    sl->cost = __ldcg(f + gi);
+  }
+}
+
+static int ensure_local_block(pps_swarm* s) {
+  if (s->local_block) return PPS_OK;
+  const size_t npad = (size_t)s->dv.npad, D = (size_t)s->dv.dim;
+  const size_t bytes = sizeof(float) * (D * npad + 2 * npad + 256) + sizeof(ArgminSlot) + 256;
+  PPS_CUDA(cudaMalloc(&s->local_block, bytes));
+  return PPS_OK;
+}
+
+struct LocalBufs {
+  float* x;
+  float* f;
+  float* it;
+  float* u;
+  ArgminSlot* slot;
+};
+
+static LocalBufs local_bufs(pps_swarm* s) {
+  const size_t npad = (size_t)s->dv.npad, D = (size_t)s->dv.dim;
+  float* b = static_cast<float*>(s->local_block);
+  LocalBufs lb;
+  lb.x = b;
+  lb.f = b + D * npad;
+  lb.it = lb.f + npad;
+  lb.u = lb.it + npad;  // 256 floats (dim <= 64)
+  lb.slot = reinterpret_cast<ArgminSlot*>(lb.u + 256);
+  return lb;
+}
+
+template <int OBJ, int MAXD>
+static void launch_local_lbfgs(pps_swarm* s, const float* x0, const LocalOpts& o, const LocalBufs& b) {
+  const int64_t n = s->dv.n;
+  const unsigned blocks = (unsigned)((n + 127) / 128);
+  k_lbfgs<OBJ, MAXD><<<blocks, 128, 0, s->stream>>>(x0, s->dv.npad, n, s->op, s->dv.lb, s->dv.ub, o, b.x, b.f, b.it);
+}
+
+template <int OBJ, int MAXD>
+static void launch_local_t(pps_swarm* s, int kind, const float* x0, const LocalOpts& o, const LocalBufs& b) {
+  const int64_t n = s->dv.n;
+  const unsigned blocks = (unsigned)((n + 127) / 128);
+  if (kind == 0)
+    k_lbfgs<OBJ, MAXD><<<blocks, 128, 0, s->stream>>>(x0, s->dv.npad, n, s->op, s->dv.lb, s->dv.ub, o, b.x, b.f, b.it);
+  else
+    k_broyden<OBJ, MAXD><<<blocks, 128, 0, s->stream>>>(x0, s->dv.npad, n, s->op, s->dv.lb, s->dv.ub, o, b.x, b.f, b.it);
+}
+
+template <int OBJ>
+static int launch_local_obj(pps_swarm* s, int kind, const float* x0, const LocalOpts& o, const LocalBufs& b) {
+  const int D = s->dv.dim;
+  if (kind == 1 && D > 16) return set_error(PPS_ENOTSUP, "the Broyden local stage supports dim <= 16 (got %d)", D);
+  if constexpr (OBJ >= kBeale) {  // closed forms are defined for dim <= 2
+    launch_local_t<OBJ, 2>(s, kind, x0, o, b);
+  } else {
+    if (D <= 2) launch_local_t<OBJ, 2>(s, kind, x0, o, b);
+    else if (D <= 4) launch_local_t<OBJ, 4>(s, kind, x0, o, b);
+    else if (D <= 8) launch_local_t<OBJ, 8>(s, kind, x0, o, b);
+    else if (D <= 16) launch_local_t<OBJ, 16>(s, kind, x0, o, b);
+    else if (D <= 32) launch_local_lbfgs<OBJ, 32>(s, x0, o, b);
+    else launch_local_lbfgs<OBJ, 64>(s, x0, o, b);
+  }
+  PPS_CUDA(cudaGetLastError());
+  return PPS_OK;
+}
+
+// kind 0: L-BFGS from personal bests; kind 1: Broyden from positions
+int run_local(pps_swarm* s, int kind, const pps_local_opts* opts, float* u_out, float* f_out, int64_t* idx_out,
+              float* device_ms) {
+  if (!s) return set_error(PPS_EINVAL, "swarm is NULL");
+  if (!s->initialized) return set_error(PPS_EINVAL, "swarm is not initialised");
+  if (!opts) return set_error(PPS_EINVAL, "options are NULL");
+  if (kind == 0 && (opts->history < 1 || opts->history > kMaxHistory))
+    return set_error(PPS_EINVAL, "history must be in [1, %d] (got %d)", kMaxHistory, opts->history);
+  if (opts->maxiters < 0 || opts->max_backtracks < 1)
+    return set_error(PPS_EINVAL, "maxiters must be >= 0 and max_backtracks >= 1");
+  if (!(opts->gtol >= 0.0f) || !std::isfinite(opts->armijo_c1))
+    return set_error(PPS_EINVAL, "gtol must be >= 0 and armijo_c1 finite");
+  if (s->dv.dim > 64) return set_error(PPS_ENOTSUP, "the local stage supports dim <= 64 (got %d)", s->dv.dim);
+  int dev = -1;
+  cudaGetDevice(&dev);
+  if (dev != s->device) PPS_CUDA(cudaSetDevice(s->device));
+  int rc = ensure_local_block(s);
+  if (rc) return rc;
+  const LocalBufs b = local_bufs(s);
+  LocalOpts o{opts->history, opts->maxiters, opts->armijo_c1, opts->gtol, opts->max_backtracks};
+  const float* x0 = (kind == 0) ? s->dv.P : s->dv.X;
+  PPS_CUDA(cudaEventRecord(s->ev0, s->stream));
+  switch (s->objective) {
+    case kSphere: rc = launch_local_obj<kSphere>(s, kind, x0, o, b); break;
+    case kRosenbrock: rc = launch_local_obj<kRosenbrock>(s, kind, x0, o, b); break;
+    case kRastrigin: rc = launch_local_obj<kRastrigin>(s, kind, x0, o, b); break;
+    case kAckley: rc = launch_local_obj<kAckley>(s, kind, x0, o, b); break;
+    case kBeale: rc = launch_local_obj<kBeale>(s, kind, x0, o, b); break;
+    case kBooth: rc = launch_local_obj<kBooth>(s, kind, x0, o, b); break;
+    case kHimmelblau: rc = launch_local_obj<kHimmelblau>(s, kind, x0, o, b); break;
+    case kQuadratic: rc = launch_local_obj<kQuadratic>(s, kind, x0, o, b); break;
+    case kBoundaryQuadratic: rc = launch_local_obj<kBoundaryQuadratic>(s, kind, x0, o, b); break;
+    default: return set_error(PPS_ENOTSUP, "objective %d has no gradient", s->objective);
+  }
+  if (rc) return rc;
+  k_reset_slot<<<1, 1, 0, s->stream>>>(b.slot);
+  k_argmin_gather<<<s->sm_count, 256, 0, s->stream>>>(b.f, b.x, s->dv.n, s->dv.npad, s->dv.dim, b.slot, b.u);
+  PPS_CUDA(cudaGetLastError());
+  PPS_CUDA(cudaEventRecord(s->ev1, s->stream));
+  ArgminSlot slot;
+  PPS_CUDA(cudaMemcpyAsync(&slot, b.slot, sizeof(slot), cudaMemcpyDeviceToHost, s->stream));
+  if (u_out) PPS_CUDA(cudaMemcpyAsync(u_out, b.u, sizeof(float) * s->dv.dim, cudaMemcpyDeviceToHost, s->stream));
+  PPS_CUDA(cudaStreamSynchronize(s->stream));
+  if (device_ms) PPS_CUDA(cudaEventElapsedTime(device_ms, s->ev0, s->ev1));
+  if (f_out) *f_out = slot.cost;
+  if (idx_out) *idx_out = (int64_t)slot.idx;
+  s->local_valid = 1;
+  return PPS_OK;
+}
+
+int local_field(pps_swarm* s, int32_t field, float** dev, int* rows) {
+  if (!s->local_block || !s->local_valid) return set_error(PPS_EINVAL, "no local-stage results yet");
+  const LocalBufs b = local_bufs(s);
+  switch (field) {
+    case PPS_FIELD_LOCAL_X: *dev = b.x; *rows = s->dv.dim; return PPS_OK;
+    case PPS_FIELD_LOCAL_F: *dev = b.f; *rows = 1; return PPS_OK;
+    case PPS_FIELD_LOCAL_ITERS: *dev = b.it; *rows = 1; return PPS_OK;
+    default: return set_error(PPS_EINVAL, "unknown field %d", field);
+  }
+}
+
+}  // namespace pps
+
+using namespace pps;
+
+extern "C" int pps_hybrid_lbfgs(pps_swarm* s, const pps_local_opts* o, float* u, float* f, int64_t* idx,
+                                float* device_ms) {
+  return run_local(s, 0, o, u, f, idx, device_ms);
+}
+
+extern "C" int pps_hybrid_bfgs(pps_swarm* s, const pps_local_opts* o, float* u, float* f, int64_t* idx,
+                               float* device_ms) {
+  return run_local(s, 1, o, u, f, idx, device_ms);
+}

@@ -84,6 +84,8 @@ struct pps_swarm {
   float graph_c1 = 0.0f, graph_c2 = 0.0f;
   int sm_count = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  void* local_block = nullptr;  // HybridPSO local-stage results (allocated on first use)
+  int local_valid = 0;
 };
 
 namespace pps {
@@ -107,5 +109,6 @@ int launch_eval(const ObjParams& op, const ObjData& od, int objective, const flo
                 int64_t stride, float* f, cudaStream_t stream);
 int async_lanes(int dim, int* slice);
 int sync_grid(pps_swarm* s);
+int local_field(pps_swarm* s, int32_t field, float** dev, int* rows);
 
 }  // namespace pps

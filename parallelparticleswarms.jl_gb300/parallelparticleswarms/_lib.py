@@ -22,6 +22,7 @@ STATUS_NAMES = {0: "PPS_OK", 1: "PPS_EINVAL", 2: "PPS_ENOMEM", 3: "PPS_ECUDA", 4
 SAMPLER_AUTO, SAMPLER_UNIFORM, SAMPLER_UNBOUNDED = 0, 1, 2
 FLAG_GBEST_FROM_POSITION = 1
 FIELD_POSITION, FIELD_VELOCITY, FIELD_PBEST, FIELD_PCOST, FIELD_COST = range(5)
+FIELD_LOCAL_X, FIELD_LOCAL_F, FIELD_LOCAL_ITERS = 5, 6, 7
 
 c_float_p = ctypes.POINTER(ctypes.c_float)
 
@@ -66,6 +67,16 @@ class SwarmInfo(ctypes.Structure):
     ]
 
 
+class LocalOpts(ctypes.Structure):
+    _fields_ = [
+        ("history", ctypes.c_int32),
+        ("maxiters", ctypes.c_int32),
+        ("armijo_c1", ctypes.c_float),
+        ("gtol", ctypes.c_float),
+        ("max_backtracks", ctypes.c_int32),
+    ]
+
+
 class DeviceSwarm(ctypes.Structure):
     """pps_device_swarm: a swarm in device buffers owned by the caller."""
 
@@ -105,6 +116,10 @@ _SIGNATURES = {
     "pps_get_state": (ctypes.c_int, [_P, ctypes.c_int32, c_float_p]),
     "pps_set_state": (ctypes.c_int, [_P, ctypes.c_int32, c_float_p]),
     "pps_eval_objective": (ctypes.c_int, [ctypes.POINTER(Problem), ctypes.c_int64, c_float_p, c_float_p]),
+    "pps_hybrid_lbfgs": (ctypes.c_int, [_P, ctypes.POINTER(LocalOpts), c_float_p, c_float_p,
+                                        ctypes.POINTER(ctypes.c_int64), c_float_p]),
+    "pps_hybrid_bfgs": (ctypes.c_int, [_P, ctypes.POINTER(LocalOpts), c_float_p, c_float_p,
+                                       ctypes.POINTER(ctypes.c_int64), c_float_p]),
     "pps_sync_run_noalloc": (ctypes.c_int, [ctypes.c_int32, c_float_p, ctypes.c_int32, ctypes.POINTER(DeviceSwarm),
                                             ctypes.c_uint64, ctypes.c_uint32, ctypes.c_int32, ctypes.c_float,
                                             ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_uint32,

@@ -1,0 +1,40 @@
+"""solve!(::HybridPSOCache) (src/hybrid.jl:47-158): the particle swarm, then a
+local optimiser on every particle, keeping the local best if it beats the
+swarm's."""
+from __future__ import annotations
+
+import time
+
+from . import _lib
+from .algorithms import BFGS, SimpleLBFGS
+
+
+def hybrid_solve(cache, *, maxiters=100, w=0.7298, wdamp=1.0, c1=1.4962, c2=1.4962, local_maxiters=50,
+                 abstol=None, reltol=None, **kwargs):
+    from .solve import OptimizationSolution, OptimizationStats, _pso_solve
+
+    if kwargs:
+        raise _lib.ArgumentError(_lib.EINVAL, f"unexpected keyword arguments {sorted(kwargs)}")
+    alg = cache.alg
+    sol_pso = _pso_solve(cache.pso_cache, maxiters, w, wdamp, c1, c2)
+    best_u, best_obj = sol_pso.u, sol_pso.objective
+    lo = alg.local_opt
+    sw = cache.pso_cache.swarm
+    t0 = time.perf_counter()
+    if isinstance(lo, SimpleLBFGS):
+        gtol = lo.gtol if abstol is None else float(abstol)
+        u, f, idx, ms = sw.local_stage("lbfgs", history=lo.history, maxiters=local_maxiters,
+                                       armijo_c1=lo.armijo_c1, gtol=gtol, max_backtracks=lo.max_backtracks)
+    elif isinstance(lo, BFGS):
+        gtol = lo.gtol if abstol is None else float(abstol)
+        u, f, idx, ms = sw.local_stage("bfgs", maxiters=local_maxiters, gtol=gtol, max_backtracks=lo.max_backtracks)
+    else:
+        raise _lib.ArgumentError(_lib.EINVAL, f"unsupported local optimiser {type(lo).__name__}")
+    t1 = time.perf_counter()
+    if f < best_obj:  # src/hybrid.jl:145-150
+        best_u, best_obj = u, f
+    return OptimizationSolution(u=best_u, objective=float(best_obj), original=None,
+                                stats=OptimizationStats(time=(t1 - t0) + sol_pso.stats.time,
+                                                        device_ms=ms + sol_pso.stats.device_ms,
+                                                        iterations=int(maxiters)),
+                                alg=alg)

@@ -76,9 +76,22 @@ class Swarm:
         _lib.check(self._lib.pps_get_gbest(self._h, _lib.fptr(u), ctypes.byref(c), ctypes.byref(i)))
         return u, float(c.value), int(i.value)
 
+    def local_stage(self, kind: str, history=10, maxiters=50, armijo_c1=1e-4, gtol=1e-5, max_backtracks=30):
+        """HybridPSO local stage on every particle: kind "lbfgs" (from personal
+        bests) or "bfgs" (Broyden, from positions).  Returns (u, f, idx, device_ms)
+        of the best local result."""
+        o = _lib.LocalOpts(int(history), int(maxiters), float(armijo_c1), float(gtol), int(max_backtracks))
+        u = np.empty(self.dim, dtype=np.float32)
+        f = ctypes.c_float()
+        i = ctypes.c_int64()
+        ms = ctypes.c_float()
+        fn = self._lib.pps_hybrid_lbfgs if kind == "lbfgs" else self._lib.pps_hybrid_bfgs
+        _lib.check(fn(self._h, ctypes.byref(o), _lib.fptr(u), ctypes.byref(f), ctypes.byref(i), ctypes.byref(ms)))
+        return u, float(f.value), int(i.value), float(ms.value)
+
     def get(self, field: int) -> np.ndarray:
-        """(dim, n) for position / velocity / pbest, (n,) for the costs."""
-        vec = field in (_lib.FIELD_POSITION, _lib.FIELD_VELOCITY, _lib.FIELD_PBEST)
+        """(dim, n) for position / velocity / pbest / local optima, (n,) otherwise."""
+        vec = field in (_lib.FIELD_POSITION, _lib.FIELD_VELOCITY, _lib.FIELD_PBEST, _lib.FIELD_LOCAL_X)
         out = np.empty((self.dim if vec else 1, self.n), dtype=np.float32)
         _lib.check(self._lib.pps_get_state(self._h, int(field), _lib.fptr(out)))
         return out if vec else out[0]
