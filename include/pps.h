@@ -183,6 +183,31 @@ PPS_API int pps_hybrid_lbfgs(pps_swarm* s, const pps_local_opts* opts, float* u,
 PPS_API int pps_hybrid_bfgs(pps_swarm* s, const pps_local_opts* opts, float* u, float* f, int64_t* idx,
                             float* device_ms);
 
+/* ---- batches: many independent swarms in one persistent launch ---- */
+/* No single reference call does this: the reference solves one problem per
+ * solve() (src/solve.jl:61-67) or one ODE fit per parameter_estim_ode!
+ * (src/ode_pso.jl:113-170).  Each added swarm is a full synchronous solve
+ * (sampling, maxiters iterations, global best from personal bests) with the
+ * same results as pps_swarm_create + pps_swarm_init + pps_sync_run on it.
+ * Objectives: sphere, Rosenbrock, Rastrigin, Ackley (dim <= 1024) and the
+ * ODE fits; n <= 65536 per swarm. */
+typedef struct pps_batch pps_batch;
+PPS_API int pps_batch_create(pps_batch** out);
+PPS_API int pps_batch_destroy(pps_batch* b);
+/* queue one swarm; *slot identifies it in the results */
+PPS_API int pps_batch_add(pps_batch* b, const pps_problem* prob, int64_t n, uint64_t seed, int32_t maxiters,
+                          float w, float wdamp, float c1, float c2, int32_t* slot);
+/* solve every queued swarm in one launch (longest work first); the block
+ * shape comes from the autotuner unless pps_batch_set_shape fixed it */
+PPS_API int pps_batch_run(pps_batch* b, float* device_ms);
+/* threads in {128, 256, 512}, ppt (particles per thread) in {1, 2};
+ * (0, 0) returns to autotuning */
+PPS_API int pps_batch_set_shape(pps_batch* b, int32_t threads, int32_t ppt);
+PPS_API int pps_batch_info(pps_batch* b, int32_t* nswarms, int32_t* threads, int32_t* ppt,
+                           uint64_t* device_bytes);
+PPS_API int pps_batch_result(pps_batch* b, int32_t slot, float* u, float* cost, int64_t* idx);
+PPS_API int pps_batch_get_state(pps_batch* b, int32_t slot, int32_t field, float* out);
+
 /* ---- results ---- */
 /* global best position (dim floats), cost and particle index; any may be NULL */
 PPS_API int pps_get_gbest(pps_swarm* s, float* u, float* cost, int64_t* idx);

@@ -45,6 +45,8 @@ static bool supported_objective(int obj) {
     case kHimmelblau:
     case kQuadratic:
     case kBoundaryQuadratic:
+    case kLvFit:
+    case kFhnFit:
       return true;
     default:
       return false;
@@ -62,6 +64,10 @@ static int check_problem(const pps_problem* prob) {
     return set_error(PPS_ENOTSUP, "objective %d is not supported by this entry point", prob->objective);
   if ((prob->objective >= kBeale) && prob->dim > 2)
     return set_error(PPS_EINVAL, "objective %d is defined for dim <= 2", prob->objective);
+  if (is_ode(prob->objective)) {
+    const int rc = ode_check(prob);
+    if (rc) return rc;
+  }
   for (int d = 0; d < prob->dim; ++d) {
     const float lo = prob->lb ? prob->lb[d] : -INFINITY;
     const float hi = prob->ub ? prob->ub[d] : INFINITY;
@@ -139,6 +145,7 @@ int pps_swarm_create(const pps_problem* prob, int64_t n, uint64_t seed, uint32_t
   const size_t oUb = take(sizeof(float) * D);
   const size_t oU0 = take(sizeof(float) * D);
   const size_t oSt = take(sizeof(IterState));
+  const size_t oData = take(sizeof(float) * (prob->data ? (size_t)prob->ndata : 0));
   s->bytes = off;
   cudaError_t e = cudaMalloc(&s->block, s->bytes);
   if (e != cudaSuccess) {
@@ -157,6 +164,9 @@ int pps_swarm_create(const pps_problem* prob, int64_t n, uint64_t seed, uint32_t
   s->dv.ub = reinterpret_cast<float*>(b + oUb);
   s->dv.st = reinterpret_cast<IterState*>(b + oSt);
   s->u0_dev = reinterpret_cast<float*>(b + oU0);
+  s->data_dev = reinterpret_cast<float*>(b + oData);
+  s->od.data = s->data_dev;
+  s->od.ndata = prob->data ? prob->ndata : 0;
   s->dv.n = n;
   s->dv.npad = npad;
   s->dv.dim = D;
@@ -190,6 +200,12 @@ int pps_swarm_create(const pps_problem* prob, int64_t n, uint64_t seed, uint32_t
         (e = cudaMemcpyAsync(s->dv.ub, s->host_ub, sizeof(float) * D, cudaMemcpyHostToDevice, s->stream)) != cudaSuccess ||
         (e = cudaMemcpyAsync(b + oU0, s->host_u0, sizeof(float) * D, cudaMemcpyHostToDevice, s->stream)) != cudaSuccess) {
       rc = cuda_error(e, "cudaMemcpy(bounds)");
+      break;
+    }
+    if (prob->data && prob->ndata > 0 &&
+        (e = cudaMemcpyAsync(s->data_dev, prob->data, sizeof(float) * (size_t)prob->ndata, cudaMemcpyHostToDevice,
+                             s->stream)) != cudaSuccess) {
+      rc = cuda_error(e, "cudaMemcpy(data)");
       break;
     }
     if ((e = cudaStreamSynchronize(s->stream)) != cudaSuccess) { rc = cuda_error(e, "cudaStreamSynchronize"); break; }
@@ -246,7 +262,8 @@ int pps_swarm_init(pps_swarm* s, int32_t sampler) {
         return set_error(PPS_EINVAL, "uniform sampler needs finite bounds (dim %d)", d);
   }
   if ((rc = launch_set_iter(s, 0u, 0.7298f, 1.0f))) return rc;
-  if ((rc = launch_init(s, sampler, s->u0_dev))) return rc;
+  if ((rc = is_ode(s->objective) ? launch_init_ode(s, sampler, s->u0_dev) : launch_init(s, sampler, s->u0_dev)))
+    return rc;
   PPS_CUDA(cudaStreamSynchronize(s->stream));
   s->t = 0;
   s->initialized = 1;
@@ -292,11 +309,15 @@ static int finish_timing(pps_swarm* s, float* device_ms) {
 
 static constexpr int kGraphChunk = 32;
 
+static int step_once(pps_swarm* s, float c1, float c2) {
+  return is_ode(s->objective) ? launch_sync_step_ode(s, c1, c2) : launch_sync_step(s, c1, c2);
+}
+
 static int run_steps(pps_swarm* s, int32_t maxiters, float c1, float c2, uint32_t run_flags) {
   int rc;
   const uint32_t saved = s->flags;
   s->flags = run_flags;
-  sync_grid(s);  // resolve occupancy outside any capture
+  if (!is_ode(s->objective)) sync_grid(s);  // resolve occupancy outside any capture
   if (maxiters >= kGraphChunk) {
     const bool stale = !s->graph || s->graph_len != kGraphChunk || s->graph_async_lanes != (int)run_flags ||
                        s->graph_c1 != c1 || s->graph_c2 != c2;
@@ -306,7 +327,7 @@ static int run_steps(pps_swarm* s, int32_t maxiters, float c1, float c2, uint32_
       cudaGraph_t g = nullptr;
       PPS_CUDA(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
       for (int k = 0; k < kGraphChunk; ++k) {
-        if ((rc = launch_sync_step(s, c1, c2))) {
+        if ((rc = step_once(s, c1, c2))) {
           cudaStreamEndCapture(s->stream, &g);
           if (g) cudaGraphDestroy(g);
           s->flags = saved;
@@ -336,7 +357,7 @@ static int run_steps(pps_swarm* s, int32_t maxiters, float c1, float c2, uint32_
     left -= kGraphChunk;
   }
   for (; left > 0; --left) {
-    if ((rc = launch_sync_step(s, c1, c2))) {
+    if ((rc = step_once(s, c1, c2))) {
       s->flags = saved;
       return rc;
     }
@@ -376,6 +397,8 @@ int pps_async_run(pps_swarm* s, int32_t maxiters, float w, float wdamp, float c1
                   float* device_ms) {
   int rc = check_run(s, maxiters, w, wdamp, c1, c2);
   if (rc) return rc;
+  if (is_ode(s->objective))
+    return set_error(PPS_ENOTSUP, "ODE fits run synchronously (parameter_estim_ode!); use pps_sync_run");
   if ((rc = launch_set_iter(s, s->t, w, wdamp))) return rc;
   PPS_CUDA(cudaEventRecord(s->ev0, s->stream));
   int lanes = 0;
@@ -463,12 +486,22 @@ int pps_eval_objective(const pps_problem* prob, int64_t npoints, const float* x,
   float* df = dx + (size_t)D * (size_t)npoints;
   ObjParams op = make_params(prob);
   ObjData od{};
+  float* ddata = nullptr;
   rc = PPS_OK;
-  if ((e = cudaMemcpyAsync(dx, x, bx, cudaMemcpyHostToDevice, st)) != cudaSuccess) rc = cuda_error(e, "cudaMemcpy");
-  if (!rc) rc = launch_eval(op, od, prob->objective, dx, npoints, npoints, df, st);
+  if (is_ode(prob->objective)) {
+    if ((e = cudaMallocAsync(&ddata, sizeof(float) * (size_t)prob->ndata, st)) != cudaSuccess) rc = cuda_error(e, "cudaMallocAsync");
+    if (!rc && (e = cudaMemcpyAsync(ddata, prob->data, sizeof(float) * (size_t)prob->ndata, cudaMemcpyHostToDevice, st)) != cudaSuccess)
+      rc = cuda_error(e, "cudaMemcpy");
+    od.data = ddata;
+    od.ndata = prob->ndata;
+  }
+  if (!rc && (e = cudaMemcpyAsync(dx, x, bx, cudaMemcpyHostToDevice, st)) != cudaSuccess) rc = cuda_error(e, "cudaMemcpy");
+  if (!rc) rc = is_ode(prob->objective) ? launch_eval_ode(op, od, prob->objective, dx, npoints, npoints, df, st)
+                                        : launch_eval(op, od, prob->objective, dx, npoints, npoints, df, st);
   if (!rc && (e = cudaMemcpyAsync(f, df, sizeof(float) * npoints, cudaMemcpyDeviceToHost, st)) != cudaSuccess)
     rc = cuda_error(e, "cudaMemcpy");
   cudaFreeAsync(dx, st);
+  if (ddata) cudaFreeAsync(ddata, st);
   if ((e = cudaStreamSynchronize(st)) != cudaSuccess && !rc) rc = cuda_error(e, "cudaStreamSynchronize");
   cudaStreamDestroy(st);
   return rc;

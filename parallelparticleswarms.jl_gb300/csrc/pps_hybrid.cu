@@ -381,6 +381,7 @@ int run_local(pps_swarm* s, int kind, const pps_local_opts* opts, float* u_out, 
   if (!(opts->gtol >= 0.0f) || !std::isfinite(opts->armijo_c1))
     return set_error(PPS_EINVAL, "gtol must be >= 0 and armijo_c1 finite");
   if (s->dv.dim > 64) return set_error(PPS_ENOTSUP, "the local stage supports dim <= 64 (got %d)", s->dv.dim);
+  if (is_ode(s->objective)) return set_error(PPS_ENOTSUP, "ODE-fit objectives have no analytic gradient here");
   int dev = -1;
   cudaGetDevice(&dev);
   if (dev != s->device) PPS_CUDA(cudaSetDevice(s->device));

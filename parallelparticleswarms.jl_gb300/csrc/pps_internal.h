@@ -110,5 +110,12 @@ int launch_eval(const ObjParams& op, const ObjData& od, int objective, const flo
 int async_lanes(int dim, int* slice);
 int sync_grid(pps_swarm* s);
 int local_field(pps_swarm* s, int32_t field, float** dev, int* rows);
+// ODE-fit objectives (pps_ode.cu)
+int ode_check(const pps_problem* prob);
+int launch_init_ode(pps_swarm* s, int sampler, const float* u0_dev);
+int launch_sync_step_ode(pps_swarm* s, float c1, float c2);
+int launch_eval_ode(const ObjParams& op, const ObjData& od, int objective, const float* x, int64_t npts,
+                    int64_t stride, float* f, cudaStream_t stream);
+inline bool is_ode(int objective) { return objective == kLvFit || objective == kFhnFit; }
 
 }  // namespace pps

@@ -1,0 +1,205 @@
+// pps_ode.cu -- one ODE-fit swarm at a time: init and the synchronous step
+// for the ode_pso objectives (parameter_estim_ode!, src/ode_pso.jl:113-170).
+//
+// The reference's loop per iteration: ode_update_particle_states! (:1-24),
+// a host broadcast that rebuilds every particle's ODE problem, the DiffEqGPU
+// solve, _reduce_losses!, ode_update_particle_costs! (:26-41) and a host
+// minimum -- about five launches and five synchronisations.  Here the whole
+// iteration is one launch: update, RK4 integration, SSE, personal best and
+// the argmin publication fused, one thread per particle, observations in
+// shared memory.
+//
+// The reference clamps with max(position, lb) on whole SVectors
+// (src/ode_pso.jl:18-19), which compares lexicographically; this build
+// clamps each parameter (max.(x, lb), min.(x, ub)) as the other kernels do.
+#include "pps_internal.h"
+#include "pps_ode.cuh"
+#include "pps_publish.cuh"
+
+namespace pps {
+
+constexpr int kOdeThreads = 128;
+constexpr int kOdeMaxDim = 4;
+
+template <int MODEL>
+__device__ __forceinline__ float ode_eval(const float (&x)[kOdeMaxDim], const OdeCfg& c, const float* data) {
+  return ode_loss<MODEL>(x, c, data);
+}
+
+template <int MODEL>
+__global__ void __launch_bounds__(kOdeThreads) k_init_ode(SwarmDev s, ObjParams op, OdeCfg cfg,
+                                                          const float* __restrict__ data_g, uint64_t seed,
+                                                          int sampler, const float* __restrict__ u0) {
+  __shared__ float data[2 * kOdeMaxSaves];
+  for (int k = threadIdx.x; k < 2 * cfg.nsaves; k += blockDim.x) data[k] = data_g[k];
+  __syncthreads();
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+  const int D = s.dim;
+  unsigned long long key = ~0ull;
+  if (i < s.npad) {
+    const bool valid = i < s.n;
+    float x[kOdeMaxDim] = {0.0f, 0.0f, 0.0f, 0.0f};
+    const Rand4 r = philox4x32_10((uint32_t)i, 0u, 0u, kTagInit, k0, k1);
+    const uint32_t rr[4] = {r.a, r.b, r.c, r.d};
+#pragma unroll
+    for (int d = 0; d < kOdeMaxDim; ++d) {
+      if (d < D) {
+        const float u = u01(rr[d]);
+        float xv;
+        if (sampler == PPS_SAMPLER_UNBOUNDED) {
+          const float z = u0 ? u0[d] : 0.0f;
+          const float a = fabsf(z);
+          xv = (a > 0.0f) ? __fadd_rn(z, __fmul_rn(u, a)) : u;
+        } else {
+          xv = __fadd_rn(__fmul_rn(u, __fsub_rn(s.ub[d], s.lb[d])), s.lb[d]);
+        }
+        x[d] = valid ? xv : 0.0f;
+        const int64_t o = (int64_t)d * s.npad + i;
+        s.X[o] = x[d];
+        s.V[o] = 0.0f;
+        s.P[o] = x[d];
+      }
+    }
+    const float c = valid ? ode_eval<MODEL>(x, cfg, data) : __int_as_float(0x7f800000);
+    s.cost[i] = c;
+    s.pcost[i] = c;
+    s.flag[i] = 0;
+    if (valid) key = argmin_key(c, (uint32_t)i);
+  }
+  if (publish_block_min(key, s.st)) finish_iteration(s, false, 0u, s.st->w);
+}
+
+template <int MODEL>
+__global__ void __launch_bounds__(kOdeThreads) k_sync_step_ode(SwarmDev s, ObjParams op, OdeCfg cfg,
+                                                               const float* __restrict__ data_g, uint64_t seed,
+                                                               float c1, float c2, int from_position) {
+  __shared__ float data[2 * kOdeMaxSaves];
+  __shared__ float sg[kOdeMaxDim], slb[kOdeMaxDim], sub[kOdeMaxDim];
+  IterState* st = s.st;
+  const uint32_t t = st->t;
+  const float w = st->w;
+  const int D = s.dim;
+  for (int k = threadIdx.x; k < 2 * cfg.nsaves; k += blockDim.x) data[k] = data_g[k];
+  if (threadIdx.x < D) {
+    sg[threadIdx.x] = s.g[threadIdx.x];
+    slb[threadIdx.x] = s.lb[threadIdx.x];
+    sub[threadIdx.x] = s.ub[threadIdx.x];
+  }
+  __syncthreads();
+  const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned long long key = ~0ull;
+  if (i < s.npad) {
+    const bool valid = i < s.n;
+    const bool pending = s.flag[i] != 0;
+    float x[kOdeMaxDim] = {0.0f, 0.0f, 0.0f, 0.0f};
+    const Rand4 r0 = philox4x32_10((uint32_t)i, 0u, t, kTagStep, k0, k1);
+    const Rand4 r1 = philox4x32_10((uint32_t)i, 1u, t, kTagStep, k0, k1);
+    const float ra[4] = {u01(r0.a), u01(r0.c), u01(r1.a), u01(r1.c)};  // r1 draws of dims 0..3
+    const float rb[4] = {u01(r0.b), u01(r0.d), u01(r1.b), u01(r1.d)};  // r2 draws
+#pragma unroll
+    for (int d = 0; d < kOdeMaxDim; ++d) {
+      if (d < D) {
+        const int64_t o = (int64_t)d * s.npad + i;
+        float xd = s.X[o];
+        float vd = s.V[o];
+        float pd = s.P[o];
+        if (pending) {
+          pd = xd;
+          s.P[o] = pd;
+        }
+        vd = velocity(xd, vd, pd, sg[d], w, c1, c2, ra[d], rb[d]);
+        xd = clamp_lb_ub(__fadd_rn(xd, vd), slb[d], sub[d]);
+        s.X[o] = xd;
+        s.V[o] = vd;
+        x[d] = xd;
+      }
+    }
+    const float c = ode_eval<MODEL>(x, cfg, data);
+    float pc = s.pcost[i];
+    const bool improved = valid && c < pc;
+    pc = improved ? c : pc;
+    s.pcost[i] = pc;
+    s.cost[i] = c;
+    s.flag[i] = improved ? 1 : 0;
+    if (valid) key = argmin_key(pc, (uint32_t)i);
+  }
+  if (publish_block_min(key, st)) finish_iteration(s, from_position != 0, t + 1u, __fmul_rn(w, st->wdamp));
+}
+
+int ode_check(const pps_problem* prob) {
+  if (prob->dim < 1 || prob->dim > kOdeMaxDim)
+    return set_error(PPS_EINVAL, "ODE fits have at most %d parameters (got %d)", kOdeMaxDim, prob->dim);
+  if (prob->objective == kLvFit && prob->dim != 4)
+    return set_error(PPS_EINVAL, "the Lotka-Volterra fit has 4 parameters (got %d)", prob->dim);
+  if (prob->objective == kFhnFit && prob->dim != 3)
+    return set_error(PPS_EINVAL, "the FitzHugh-Nagumo fit has 3 parameters (got %d)", prob->dim);
+  if (prob->nparams < 5 || !prob->params)
+    return set_error(PPS_EINVAL, "ODE fits take params = [u0_1, u0_2, dt, nsteps, save_every(, l)]");
+  if (prob->objective == kFhnFit && prob->nparams < 6)
+    return set_error(PPS_EINVAL, "the FitzHugh-Nagumo fit needs params[5] = l");
+  const float nsteps = prob->params[3], every = prob->params[4];
+  if (!(prob->params[2] > 0.0f) || !(nsteps >= 1.0f) || !(every >= 1.0f) || nsteps != (float)(int)nsteps ||
+      every != (float)(int)every)
+    return set_error(PPS_EINVAL, "ODE fit needs dt > 0 and integral nsteps, save_every >= 1");
+  if (!prob->data || prob->ndata < 2 || (prob->ndata & 1) || prob->ndata / 2 > kOdeMaxSaves)
+    return set_error(PPS_EINVAL, "ODE fit needs data of 2 * nsaves floats, 1 <= nsaves <= %d", kOdeMaxSaves);
+  if ((prob->ndata / 2 - 1) * (int64_t)every > (int64_t)nsteps)
+    return set_error(PPS_EINVAL, "ODE fit: (nsaves - 1) * save_every exceeds nsteps");
+  return PPS_OK;
+}
+
+static OdeCfg cfg_of(pps_swarm* s) { return ode_cfg(s->op, s->od.ndata); }
+
+int launch_init_ode(pps_swarm* s, int sampler, const float* u0_dev) {
+  const unsigned blocks = (unsigned)((s->dv.npad + kOdeThreads - 1) / kOdeThreads);
+  const OdeCfg c = cfg_of(s);
+  if (s->objective == kLvFit)
+    k_init_ode<kOdeLV><<<blocks, kOdeThreads, 0, s->stream>>>(s->dv, s->op, c, s->od.data, s->seed, sampler, u0_dev);
+  else
+    k_init_ode<kOdeFHN><<<blocks, kOdeThreads, 0, s->stream>>>(s->dv, s->op, c, s->od.data, s->seed, sampler, u0_dev);
+  PPS_CUDA(cudaGetLastError());
+  return PPS_OK;
+}
+
+int launch_sync_step_ode(pps_swarm* s, float c1, float c2) {
+  const unsigned blocks = (unsigned)((s->dv.npad + kOdeThreads - 1) / kOdeThreads);
+  const OdeCfg c = cfg_of(s);
+  const int from_pos = (s->flags & PPS_FLAG_GBEST_FROM_POSITION) ? 1 : 0;
+  if (s->objective == kLvFit)
+    k_sync_step_ode<kOdeLV><<<blocks, kOdeThreads, 0, s->stream>>>(s->dv, s->op, c, s->od.data, s->seed, c1, c2, from_pos);
+  else
+    k_sync_step_ode<kOdeFHN><<<blocks, kOdeThreads, 0, s->stream>>>(s->dv, s->op, c, s->od.data, s->seed, c1, c2, from_pos);
+  PPS_CUDA(cudaGetLastError());
+  return PPS_OK;
+}
+
+template <int MODEL>
+__global__ void k_eval_ode(ObjParams op, OdeCfg cfg, const float* __restrict__ data_g, const float* __restrict__ x,
+                           int64_t npts, int64_t stride, float* __restrict__ f) {
+  __shared__ float data[2 * kOdeMaxSaves];
+  for (int k = threadIdx.x; k < 2 * cfg.nsaves; k += blockDim.x) data[k] = data_g[k];
+  __syncthreads();
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= npts) return;
+  float p[kOdeMaxDim] = {0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll
+  for (int d = 0; d < kOdeMaxDim; ++d)
+    if (d < op.dim) p[d] = x[(int64_t)d * stride + i];
+  f[i] = ode_eval<MODEL>(p, cfg, data);
+}
+
+int launch_eval_ode(const ObjParams& op, const ObjData& od, int objective, const float* x, int64_t npts,
+                    int64_t stride, float* f, cudaStream_t stream) {
+  const unsigned blocks = (unsigned)((npts + 127) / 128);
+  const OdeCfg c = ode_cfg(op, od.ndata);
+  if (objective == kLvFit)
+    k_eval_ode<kOdeLV><<<blocks, 128, 0, stream>>>(op, c, od.data, x, npts, stride, f);
+  else
+    k_eval_ode<kOdeFHN><<<blocks, 128, 0, stream>>>(op, c, od.data, x, npts, stride, f);
+  PPS_CUDA(cudaGetLastError());
+  return PPS_OK;
+}
+
+}  // namespace pps

@@ -12,6 +12,8 @@ from .problem import (REGISTRY, Objective, OptimizationProblem, ackley, beale, b
 from .solve import (HybridPSOCache, OptimizationSolution, OptimizationStats, PSOCache, init, reinit_, solve,
                     solve_)
 from .swarm import Swarm
+from .batch import Batch
+from . import ode
 
 __all__ = [
     "ParallelPSOKernel", "ParallelSyncPSOKernel", "PSOAlgorithm", "HybridPSO", "SimpleLBFGS", "BFGS",
@@ -19,5 +21,5 @@ __all__ = [
     "PSOCache", "HybridPSOCache", "OptimizationSolution", "OptimizationStats", "Swarm", "PPSError",
     "ArgumentError", "evaluate", "Objective", "REGISTRY", "sphere", "rosenbrock", "rastrigin", "ackley",
     "lotka_volterra_fit", "fitzhugh_nagumo_fit", "mlp_regression", "beale", "booth", "himmelblau",
-    "quadratic", "boundary_quadratic", "CUDA",
+    "quadratic", "boundary_quadratic", "CUDA", "Batch", "ode",
 ]

@@ -116,6 +116,17 @@ _SIGNATURES = {
     "pps_get_state": (ctypes.c_int, [_P, ctypes.c_int32, c_float_p]),
     "pps_set_state": (ctypes.c_int, [_P, ctypes.c_int32, c_float_p]),
     "pps_eval_objective": (ctypes.c_int, [ctypes.POINTER(Problem), ctypes.c_int64, c_float_p, c_float_p]),
+    "pps_batch_create": (ctypes.c_int, [ctypes.POINTER(_P)]),
+    "pps_batch_destroy": (ctypes.c_int, [_P]),
+    "pps_batch_add": (ctypes.c_int, [_P, ctypes.POINTER(Problem), ctypes.c_int64, ctypes.c_uint64, ctypes.c_int32,
+                                     ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                                     ctypes.POINTER(ctypes.c_int32)]),
+    "pps_batch_run": (ctypes.c_int, [_P, c_float_p]),
+    "pps_batch_set_shape": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int32]),
+    "pps_batch_info": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_int32),
+                                      ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_uint64)]),
+    "pps_batch_result": (ctypes.c_int, [_P, ctypes.c_int32, c_float_p, c_float_p, ctypes.POINTER(ctypes.c_int64)]),
+    "pps_batch_get_state": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int32, c_float_p]),
     "pps_hybrid_lbfgs": (ctypes.c_int, [_P, ctypes.POINTER(LocalOpts), c_float_p, c_float_p,
                                         ctypes.POINTER(ctypes.c_int64), c_float_p]),
     "pps_hybrid_bfgs": (ctypes.c_int, [_P, ctypes.POINTER(LocalOpts), c_float_p, c_float_p,

@@ -1,0 +1,88 @@
+"""ode_pso: estimate ODE parameters by PSO (src/ode_pso.jl).
+
+An ODE fit is an OptimizationProblem whose objective integrates the model
+with the particle's position as its parameters (fixed-step RK4 on the device)
+and returns the SSE against observations (_reduce_losses!, src/ode_pso.jl:47-52).
+The fit configuration travels in ``p`` = [u0_1, u0_2, dt, nsteps, save_every, l]
+and the observations in ``data`` (nsaves x 2, t = 0 included).
+
+``trajectory64`` / ``synthetic_fit`` build synthetic observations on the host
+(float64 RK4 plus Gaussian noise) for the workloads; they are input
+generation, not part of the solve.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from .problem import OptimizationProblem, fitzhugh_nagumo_fit, lotka_volterra_fit
+
+LV_TRUTH = (1.5, 1.0, 3.0, 1.0)          # benchmarks/Lotka_Volterra/lotka_volterra.jl:16
+FHN_TRUTH = (0.7, 0.8, 0.08)             # (a, b, tinv) of benchmarks/Fitzhugh_Nagumo/ode_estimation.jl:14
+FHN_L = 0.5                              # l, held fixed
+
+
+def _rhs64(model: str, p, u, l):
+    if model == "lv":
+        return np.array([p[0] * u[0] - p[1] * u[0] * u[1], -p[2] * u[1] + p[3] * u[0] * u[1]])
+    v, w = u
+    return np.array([v - v ** 3 / 3 - w + l, p[2] * (v + p[0] - p[1] * w)])
+
+
+def trajectory64(model: str, p, u0, dt: float, nsteps: int, save_every: int, l: float = FHN_L) -> np.ndarray:
+    """float64 RK4 trajectory at every save_every-th step, t = 0 included."""
+    u = np.array(u0, dtype=np.float64)
+    p = np.asarray(p, dtype=np.float64)
+    out = [u.copy()]
+    for s in range(1, nsteps + 1):
+        k1 = _rhs64(model, p, u, l)
+        k2 = _rhs64(model, p, u + 0.5 * dt * k1, l)
+        k3 = _rhs64(model, p, u + 0.5 * dt * k2, l)
+        k4 = _rhs64(model, p, u + dt * k3, l)
+        u = u + dt / 6 * (k1 + 2 * k2 + 2 * k3 + k4)
+        if s % save_every == 0:
+            out.append(u.copy())
+    return np.array(out)
+
+
+def lv_problem(data, u0=(1.0, 1.0), dt=0.01, nsteps=1000, save_every=10, lb=0.0, ub=5.0) -> OptimizationProblem:
+    """Lotka-Volterra fit: du1 = a u1 - b u1 u2, du2 = -c u2 + d u1 u2 (4 parameters)."""
+    return OptimizationProblem(lotka_volterra_fit, np.zeros(4, np.float32),
+                               [u0[0], u0[1], dt, nsteps, save_every, 0.0],
+                               lb=np.full(4, lb, np.float32), ub=np.full(4, ub, np.float32), data=data)
+
+
+def fhn_problem(data, u0=(-1.0, 1.0), dt=0.01, nsteps=2000, save_every=10, l=FHN_L, lb=0.0,
+                ub=5.0) -> OptimizationProblem:
+    """FitzHugh-Nagumo fit of (a, b, tinv): dv = v - v^3/3 - w + l, dw = tinv (v + a - b w)."""
+    return OptimizationProblem(fitzhugh_nagumo_fit, np.zeros(3, np.float32),
+                               [u0[0], u0[1], dt, nsteps, save_every, l],
+                               lb=np.full(3, lb, np.float32), ub=np.full(3, ub, np.float32), data=data)
+
+
+def synthetic_fit(model: str, seed: int, noise: float = 0.01, perturb: float = 0.2):
+    """One fit of the batched ODE workload: truth = reference parameters times
+    U(1 - perturb, 1 + perturb) each, observations = RK4 trajectory + N(0, noise^2).
+    LV: u0 = [1, 1], t in [0, 10], 101 points; FHN: u0 = [-1, 1], t in [0, 20], 201 points."""
+    rng = np.random.default_rng(seed)
+    if model == "lv":
+        truth = np.array(LV_TRUTH) * rng.uniform(1 - perturb, 1 + perturb, 4)
+        traj = trajectory64("lv", truth, (1.0, 1.0), 0.01, 1000, 10)
+        data = (traj + rng.normal(0.0, noise, traj.shape)).astype(np.float32)
+        return lv_problem(data), truth
+    truth = np.array(FHN_TRUTH) * rng.uniform(1 - perturb, 1 + perturb, 3)
+    traj = trajectory64("fhn", truth, (-1.0, 1.0), 0.01, 2000, 10)
+    data = (traj + rng.normal(0.0, noise, traj.shape)).astype(np.float32)
+    return fhn_problem(data), truth
+
+
+def parameter_estim_ode(prob: OptimizationProblem, n: int, *, maxiters: int = 100, w: float = 0.7298,
+                        wdamp: float = 1.0, seed: int = 0):
+    """parameter_estim_ode!(prob, cache, lb, ub, Val(false); maxiters) (src/ode_pso.jl:113-170):
+    returns (gbest position, gbest cost)."""
+    from .swarm import Swarm
+
+    with Swarm(prob, n, seed=seed) as sw:
+        sw.init()
+        sw.sync_run(maxiters, w=w, wdamp=wdamp)
+        u, cost, _ = sw.gbest()
+    return u, cost
