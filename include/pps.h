@@ -208,6 +208,46 @@ PPS_API int pps_batch_info(pps_batch* b, int32_t* nswarms, int32_t* threads, int
 PPS_API int pps_batch_result(pps_batch* b, int32_t slot, float* u, float* cost, int64_t* idx);
 PPS_API int pps_batch_get_state(pps_batch* b, int32_t slot, int32_t field, float* out);
 
+/* ---- serving: continuous batching of arriving problems ---- */
+/* No counterpart in the reference (one solve() owns the device at a time).
+ * A worker thread admits submitted problems first-come first-served while
+ * their swarm state fits in a device arena of memory_budget bytes, packs them
+ * into batched launches (the kernel of pps_batch_run) and keeps up to
+ * max_launches launches in flight on separate streams, so requests that
+ * arrive while others run start on the SMs those leave free.  Each result
+ * equals the problem's solve alone (same seed) bit for bit. */
+typedef struct pps_serve_config {
+  uint64_t memory_budget; /* HBM arena for swarm state, bytes (0: 8 GiB) */
+  int32_t max_launches;   /* launches in flight (0: 8, at most 64) */
+  int32_t max_pack;       /* swarms per launch (0: 512, at most 4096) */
+  int32_t threads;        /* block size of the batched kernel (0: 256) */
+  int32_t ppt;            /* particles per thread (0: 1) */
+  double tick_us;         /* while launches are in flight, the oldest queued request
+                             waits at most this long for a fuller pack */
+} pps_serve_config;
+typedef struct pps_serve_stats {
+  uint64_t submitted, completed, launches;
+  double solves_per_s;    /* completed / (last completion - first submission) */
+  double p50_ms, p99_ms, mean_ms, max_ms; /* time to solution: submit -> result ready */
+  double mean_pack;       /* swarms per launch */
+  uint64_t arena_bytes, arena_peak_bytes;
+  int32_t queued, running;
+} pps_serve_stats;
+typedef struct pps_server pps_server;
+PPS_API int pps_serve_start(const pps_serve_config* cfg, pps_server** out);
+/* queue one problem (validated here; PPS_ENOMEM if it can never fit) */
+PPS_API int pps_serve_submit(pps_server* s, const pps_problem* prob, int64_t n, uint64_t seed, int32_t maxiters,
+                             float w, float wdamp, float c1, float c2, uint64_t* ticket);
+/* PPS_OK and the result (the ticket is then released), or PPS_EBUSY */
+PPS_API int pps_serve_poll(pps_server* s, uint64_t ticket, float* u, float* cost, int64_t* idx,
+                           double* latency_ms);
+/* block until done or timeout_s (PPS_ETIMEOUT) */
+PPS_API int pps_serve_wait(pps_server* s, uint64_t ticket, float* u, float* cost, int64_t* idx,
+                           double* latency_ms, double timeout_s);
+PPS_API int pps_serve_stats_get(pps_server* s, pps_serve_stats* stats);
+/* finish queued and running requests, then release everything */
+PPS_API int pps_serve_stop(pps_server* s);
+
 /* ---- results ---- */
 /* global best position (dim floats), cost and particle index; any may be NULL */
 PPS_API int pps_get_gbest(pps_swarm* s, float* u, float* cost, int64_t* idx);

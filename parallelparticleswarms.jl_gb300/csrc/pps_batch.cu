@@ -21,34 +21,25 @@
 // shape.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
 #include <new>
+#include <string>
+#include <tuple>
 #include <vector>
 
-#include "pps_internal.h"
+#include <cooperative_groups.h>
+
+#include "pps_batch.h"
 #include "pps_ode.cuh"
+#include "pps_vec.cuh"
 #include "pps_objgrad.cuh"
 
 namespace pps {
 
-constexpr int kBatchMaxDim = 1024;
-constexpr int64_t kBatchMaxParticles = 1 << 16;
-
-struct BatchSwarm {
-  int objective, dim, maxiters, sampler;
-  int64_t n, ld;
-  float w, wdamp, c1, c2;
-  uint64_t seed;
-  ObjParams op;
-  int64_t ndata;
-  const float* data;
-  float *X, *V, *P, *pcost, *cost;
-  const float *lb, *ub, *u0;
-  float* g;       // dim floats: global best position (out)
-  float* result;  // [gcost, gidx as bits, iterations]
-};
+namespace cg = cooperative_groups;
 
 __device__ __forceinline__ unsigned long long wmin64(unsigned long long k) {
 #pragma unroll
@@ -58,6 +49,13 @@ __device__ __forceinline__ unsigned long long wmin64(unsigned long long k) {
   }
   return k;
 }
+
+struct BatchSmem {
+  unsigned long long red[33];
+  unsigned long long win_key;  // this CTA's best key, read by the other CTAs of the cluster
+  int win_fromx;               // its deferred-pbest flag
+  float gcost;
+};
 
 // block-wide argmin; every thread returns the winning key
 __device__ __forceinline__ unsigned long long block_min(unsigned long long key, unsigned long long* red) {
@@ -75,16 +73,105 @@ __device__ __forceinline__ unsigned long long block_min(unsigned long long key, 
   return red[32];
 }
 
-struct BatchSmem {
-  unsigned long long red[33];
-  float gcost;
+// The swarm-wide argmin.  One CTA: the block reduction.  A cluster of C
+// CTAs: each CTA publishes its block minimum (and the winner's pending
+// personal-best flag) in shared memory, the hardware cluster barrier makes it
+// visible, and every CTA reads all C entries through distributed shared
+// memory, so all of them agree on the winner.  `from_x` says whether the
+// winner's personal best is its position (improved this iteration).
+__device__ __forceinline__ unsigned long long swarm_min(unsigned long long key, BatchSmem& S, const uint8_t* flag,
+                                                        int64_t pb, int C, int* from_x) {
+  const unsigned long long local = block_min(key, S.red);
+  if (C == 1) {
+    *from_x = (local != ~0ull) ? flag[(int64_t)(uint32_t)local - pb] : 0;
+    return local;
+  }
+  if (threadIdx.x == 0) {
+    S.win_key = local;
+    S.win_fromx = (local != ~0ull) ? flag[(int64_t)(uint32_t)local - pb] : 0;
+  }
+  cg::cluster_group cl = cg::this_cluster();
+  cl.sync();
+  unsigned long long best = ~0ull;
+  int fx = 0;
+  for (int r = 0; r < C; ++r) {
+    const BatchSmem* rs = cl.map_shared_rank(&S, r);
+    const unsigned long long k = rs->win_key;
+    if (k < best) {
+      best = k;
+      fx = rs->win_fromx;
+    }
+  }
+  *from_x = fx;
+  return best;
+}
+
+// after the global best has been gathered: no CTA of the swarm may start the
+// next iteration (which overwrites positions) or reuse its published key
+// before every CTA has read them
+__device__ __forceinline__ void swarm_barrier(int C) {
+  if (C == 1) {
+    __syncthreads();
+  } else {
+    cg::this_cluster().sync();
+  }
+}
+
+// particles of this CTA: [pb, pe).  The chunk is a multiple of the block's
+// particle width (threads x particles per thread), so every thread of every
+// CTA but the last owns the same number of particles.
+struct Range {
+  int64_t pb, pe;
 };
+__host__ __device__ __forceinline__ int64_t cta_chunk(int64_t n, int C, int width) {
+  return ((n + C - 1) / C + width - 1) / width * width;
+}
+__device__ __forceinline__ Range cta_range(int64_t n, int C, int rank, int width) {
+  const int64_t chunk = cta_chunk(n, C, width);
+  Range r;
+  r.pb = (int64_t)rank * chunk;
+  r.pe = r.pb + chunk < n ? r.pb + chunk : n;
+  if (r.pb > n) r.pb = n;
+  return r;
+}
+
+// rank 0 publishes the swarm's result: in device memory, and when the
+// descriptor carries a mailbox in mapped host memory, there too, followed by
+// the done flag -- only after every CTA of the swarm has stopped writing
+__device__ __forceinline__ void publish_result(const BatchSwarm& sw, const float* sg, float gcost,
+                                               unsigned long long win, int rank, int C) {
+  swarm_barrier(C);
+  if (rank != 0) return;
+  for (int d = threadIdx.x; d < sw.dim; d += blockDim.x) {
+    sw.g[d] = sg[d];
+    if (sw.mail) sw.mail[d] = sg[d];
+  }
+  if (threadIdx.x == 0) {
+    sw.result[0] = gcost;
+    sw.result[1] = __uint_as_float((uint32_t)win);
+    sw.result[2] = (float)sw.maxiters;
+    if (sw.mail) {
+      sw.mail[sw.dim] = gcost;
+      sw.mail[sw.dim + 1] = __uint_as_float((uint32_t)win);
+    }
+  }
+  if (sw.done) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      __threadfence_system();
+      *reinterpret_cast<volatile int*>(sw.done) = 1;
+    }
+  }
+}
 
 // ---------------------------------------------------------------- separable
 template <int OBJ, int PPT>
-__device__ void run_swarm(const BatchSwarm& sw, BatchSmem& S, float* sg, float* slb, float* sub, uint8_t* flag) {
+__device__ void run_swarm(const BatchSwarm& sw, BatchSmem& S, float* sg, float* slb, float* sub, uint8_t* flag,
+                          int rank, int C) {
   const int D = sw.dim;
   const int64_t n = sw.n, ld = sw.ld;
+  const Range R = cta_range(n, C, rank, (int)blockDim.x * PPT);
+  const int64_t pb = R.pb, pe = R.pe;
   const uint32_t k0 = (uint32_t)sw.seed, k1 = (uint32_t)(sw.seed >> 32);
   float* __restrict__ X = sw.X;
   float* __restrict__ V = sw.V;
@@ -93,11 +180,11 @@ __device__ void run_swarm(const BatchSwarm& sw, BatchSmem& S, float* sg, float* 
     slb[d] = sw.lb[d];
     sub[d] = sw.ub[d];
   }
-  for (int64_t i = threadIdx.x; i < ld; i += blockDim.x) flag[i] = 0;  // padding particles included
+  for (int64_t i = pb + threadIdx.x; i < pb + ((pe - pb + 31) / 32 * 32) + 1; i += blockDim.x) flag[i - pb] = 0;
   __syncthreads();
   // ---- init (gpu_init_particles!, src/utils.jl:23-84)
   unsigned long long best = ~0ull;
-  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+  for (int64_t i = pb + threadIdx.x; i < pe; i += blockDim.x) {
     Acc<OBJ> acc;
     for (int j = 0; j < D; j += 4) {
       const Rand4 r = philox4x32_10((uint32_t)i, (uint32_t)(j >> 2), 0u, kTagInit, k0, k1);
@@ -126,71 +213,105 @@ __device__ void run_swarm(const BatchSwarm& sw, BatchSmem& S, float* sg, float* 
     const float c = finalize<OBJ>(sw.op, acc.s1, acc.s2);
     sw.cost[i] = c;
     sw.pcost[i] = c;
-    flag[i] = 0;
     const unsigned long long k = argmin_key(c, (uint32_t)i);
     best = k < best ? k : best;
   }
-  unsigned long long win = block_min(best, S.red);
+  int fromx = 0;
+  unsigned long long win = swarm_min(best, S, flag, pb, C, &fromx);
   {
     const uint32_t gi = (uint32_t)win;
     for (int d = threadIdx.x; d < D; d += blockDim.x) sg[d] = P[(int64_t)d * ld + gi];
     if (threadIdx.x == 0) S.gcost = sw.pcost[gi];
   }
-  __syncthreads();
+  swarm_barrier(C);
   float w = sw.w;
   // ---- synchronous iterations (src/kernels.jl:1-26, src/lowerlevel_solve.jl:1-36)
+  // The body is the one of k_sync_step: PPT particles per thread as a vector
+  // along the particle axis, dims walked in pairs (one Philox call per
+  // particle and pair), the next pair's loads issued before the current pair
+  // is computed.
   for (int it = 0; it < sw.maxiters; ++it) {
     const uint32_t t = (uint32_t)it;
     best = ~0ull;
-    for (int64_t i0 = (int64_t)threadIdx.x * PPT; i0 < n; i0 += (int64_t)blockDim.x * PPT) {
+    for (int64_t i0 = pb + (int64_t)threadIdx.x * PPT; i0 < pe; i0 += (int64_t)blockDim.x * PPT) {
       uint8_t fl[PPT];
       bool anyfl = false;
 #pragma unroll
       for (int k = 0; k < PPT; ++k) {
-        fl[k] = flag[i0 + k];
+        fl[k] = flag[i0 + k - pb];
         anyfl |= fl[k] != 0;
       }
       Acc<OBJ> acc[PPT];
+      float xa[PPT], va[PPT], pa[PPT], xb[PPT], vb[PPT], pbv[PPT];
+      ldv<PPT>(xa, X + i0);
+      ldv<PPT>(va, V + i0);
+      ldv<PPT>(pa, P + i0);
+      if (D > 1) {
+        ldv<PPT>(xb, X + ld + i0);
+        ldv<PPT>(vb, V + ld + i0);
+        ldv<PPT>(pbv, P + ld + i0);
+      }
       for (int j = 0; j < D; j += 2) {
+        float nxa[PPT], nva[PPT], npa[PPT], nxb[PPT], nvb[PPT], npb[PPT];
+        if (j + 2 < D) {
+          const int64_t o = (int64_t)(j + 2) * ld + i0;
+          ldv<PPT>(nxa, X + o);
+          ldv<PPT>(nva, V + o);
+          ldv<PPT>(npa, P + o);
+        }
+        if (j + 3 < D) {
+          const int64_t o = (int64_t)(j + 3) * ld + i0;
+          ldv<PPT>(nxb, X + o);
+          ldv<PPT>(nvb, V + o);
+          ldv<PPT>(npb, P + o);
+        }
         Rand4 r[PPT];
 #pragma unroll
         for (int k = 0; k < PPT; ++k) r[k] = philox4x32_10((uint32_t)(i0 + k), (uint32_t)(j >> 1), t, kTagStep, k0, k1);
+        {
+          const int64_t o = (int64_t)j * ld + i0;
+          if (anyfl) {
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
-          const int d = j + h;
-          if (d < D) {
-            const int64_t o = (int64_t)d * ld + i0;
-            float x[PPT], v[PPT], p[PPT];
-#pragma unroll
-            for (int k = 0; k < PPT; ++k) {
-              x[k] = X[o + k];
-              v[k] = V[o + k];
-              p[k] = P[o + k];
-            }
-            if (anyfl) {
-#pragma unroll
-              for (int k = 0; k < PPT; ++k) {
-                p[k] = fl[k] ? x[k] : p[k];
-                if (fl[k]) P[o + k] = p[k];
-              }
-            }
-            const float gd = sg[d], lo = slb[d], hi = sub[d];
-#pragma unroll
-            for (int k = 0; k < PPT; ++k) {
-              const float r1 = u01(h ? r[k].c : r[k].a), r2 = u01(h ? r[k].d : r[k].b);
-              v[k] = velocity(x[k], v[k], p[k], gd, w, sw.c1, sw.c2, r1, r2);
-              x[k] = clamp_lb_ub(__fadd_rn(x[k], v[k]), lo, hi);
-              X[o + k] = x[k];
-              V[o + k] = v[k];
-              acc[k].add(sw.op, d, x[k]);
-            }
+            for (int k = 0; k < PPT; ++k) pa[k] = fl[k] ? xa[k] : pa[k];
+            stv<PPT>(P + o, pa);
           }
+          const float gd = sg[j], lo = slb[j], hi = sub[j];
+#pragma unroll
+          for (int k = 0; k < PPT; ++k) {
+            va[k] = velocity(xa[k], va[k], pa[k], gd, w, sw.c1, sw.c2, u01(r[k].a), u01(r[k].b));
+            xa[k] = clamp_lb_ub(__fadd_rn(xa[k], va[k]), lo, hi);
+            acc[k].add(sw.op, j, xa[k]);
+          }
+          stv<PPT>(X + o, xa);
+          stv<PPT>(V + o, va);
+        }
+        if (j + 1 < D) {
+          const int64_t o = (int64_t)(j + 1) * ld + i0;
+          if (anyfl) {
+#pragma unroll
+            for (int k = 0; k < PPT; ++k) pbv[k] = fl[k] ? xb[k] : pbv[k];
+            stv<PPT>(P + o, pbv);
+          }
+          const float gd = sg[j + 1], lo = slb[j + 1], hi = sub[j + 1];
+#pragma unroll
+          for (int k = 0; k < PPT; ++k) {
+            vb[k] = velocity(xb[k], vb[k], pbv[k], gd, w, sw.c1, sw.c2, u01(r[k].c), u01(r[k].d));
+            xb[k] = clamp_lb_ub(__fadd_rn(xb[k], vb[k]), lo, hi);
+            acc[k].add(sw.op, j + 1, xb[k]);
+          }
+          stv<PPT>(X + o, xb);
+          stv<PPT>(V + o, vb);
+        }
+#pragma unroll
+        for (int k = 0; k < PPT; ++k) {
+          xa[k] = nxa[k]; va[k] = nva[k]; pa[k] = npa[k];
+          xb[k] = nxb[k]; vb[k] = nvb[k]; pbv[k] = npb[k];
         }
       }
 #pragma unroll
       for (int k = 0; k < PPT; ++k) {
         const int64_t i = i0 + k;
-        const bool valid = i < n;
+        const bool valid = i < pe;
         const float c = finalize<OBJ>(sw.op, acc[k].s1, acc[k].s2);
         const float pc = sw.pcost[i];
         const bool imp = valid && c < pc;
@@ -201,37 +322,33 @@ __device__ void run_swarm(const BatchSwarm& sw, BatchSmem& S, float* sg, float* 
           const unsigned long long key = argmin_key(npc, (uint32_t)i);
           best = key < best ? key : best;
         }
-        flag[i] = imp ? 1 : 0;
+        flag[i - pb] = imp ? 1 : 0;
       }
     }
-    win = block_min(best, S.red);  // also orders this iteration's writes before the gather
+    win = swarm_min(best, S, flag, pb, C, &fromx);  // also orders this iteration's writes before the gather
     const uint32_t gi = (uint32_t)win;
-    const bool from_x = flag[gi] != 0;
-    for (int d = threadIdx.x; d < D; d += blockDim.x) sg[d] = from_x ? X[(int64_t)d * ld + gi] : P[(int64_t)d * ld + gi];
+    for (int d = threadIdx.x; d < D; d += blockDim.x) sg[d] = fromx ? X[(int64_t)d * ld + gi] : P[(int64_t)d * ld + gi];
     if (threadIdx.x == 0) S.gcost = sw.pcost[gi];
-    __syncthreads();
+    swarm_barrier(C);
     w = __fmul_rn(w, sw.wdamp);
   }
   // ---- canonical state and result
-  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
-    if (flag[i]) {
+  for (int64_t i = pb + threadIdx.x; i < pe; i += blockDim.x) {
+    if (flag[i - pb]) {
       for (int d = 0; d < D; ++d) P[(int64_t)d * ld + i] = X[(int64_t)d * ld + i];
     }
   }
-  for (int d = threadIdx.x; d < D; d += blockDim.x) sw.g[d] = sg[d];
-  if (threadIdx.x == 0) {
-    sw.result[0] = S.gcost;
-    sw.result[1] = __uint_as_float((uint32_t)win);
-    sw.result[2] = (float)sw.maxiters;
-  }
+  publish_result(sw, sg, S.gcost, win, rank, C);
 }
 
 // ---------------------------------------------------------------- ODE fits
 template <int MODEL>
 __device__ void run_swarm_ode(const BatchSwarm& sw, BatchSmem& S, float* sg, float* slb, float* sub, uint8_t* flag,
-                              float* data) {
+                              float* data, int rank, int C) {
   const int D = sw.dim;
   const int64_t n = sw.n, ld = sw.ld;
+  const Range R = cta_range(n, C, rank, (int)blockDim.x);
+  const int64_t pb = R.pb, pe = R.pe;
   const uint32_t k0 = (uint32_t)sw.seed, k1 = (uint32_t)(sw.seed >> 32);
   const OdeCfg cfg = ode_cfg(sw.op, sw.ndata);
   for (int k = threadIdx.x; k < 2 * cfg.nsaves; k += blockDim.x) data[k] = sw.data[k];
@@ -239,9 +356,10 @@ __device__ void run_swarm_ode(const BatchSwarm& sw, BatchSmem& S, float* sg, flo
     slb[d] = sw.lb[d];
     sub[d] = sw.ub[d];
   }
+  for (int64_t i = pb + threadIdx.x; i < pe; i += blockDim.x) flag[i - pb] = 0;
   __syncthreads();
   unsigned long long best = ~0ull;
-  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
+  for (int64_t i = pb + threadIdx.x; i < pe; i += blockDim.x) {
     float x[4] = {0.0f, 0.0f, 0.0f, 0.0f};
     const Rand4 r = philox4x32_10((uint32_t)i, 0u, 0u, kTagInit, k0, k1);
     const uint32_t rr[4] = {r.a, r.b, r.c, r.d};
@@ -267,23 +385,23 @@ __device__ void run_swarm_ode(const BatchSwarm& sw, BatchSmem& S, float* sg, flo
     const float c = ode_loss<MODEL>(x, cfg, data);
     sw.cost[i] = c;
     sw.pcost[i] = c;
-    flag[i] = 0;
     const unsigned long long k = argmin_key(c, (uint32_t)i);
     best = k < best ? k : best;
   }
-  unsigned long long win = block_min(best, S.red);
+  int fromx = 0;
+  unsigned long long win = swarm_min(best, S, flag, pb, C, &fromx);
   {
     const uint32_t gi = (uint32_t)win;
     for (int d = threadIdx.x; d < D; d += blockDim.x) sg[d] = sw.P[(int64_t)d * ld + gi];
     if (threadIdx.x == 0) S.gcost = sw.pcost[gi];
   }
-  __syncthreads();
+  swarm_barrier(C);
   float w = sw.w;
   for (int it = 0; it < sw.maxiters; ++it) {
     const uint32_t t = (uint32_t)it;
     best = ~0ull;
-    for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
-      const bool pending = flag[i] != 0;
+    for (int64_t i = pb + threadIdx.x; i < pe; i += blockDim.x) {
+      const bool pending = flag[i - pb] != 0;
       float x[4] = {0.0f, 0.0f, 0.0f, 0.0f};
       const Rand4 r0 = philox4x32_10((uint32_t)i, 0u, t, kTagStep, k0, k1);
       const Rand4 r1 = philox4x32_10((uint32_t)i, 1u, t, kTagStep, k0, k1);
@@ -311,138 +429,113 @@ __device__ void run_swarm_ode(const BatchSwarm& sw, BatchSmem& S, float* sg, flo
       const float npc = imp ? c : pc;
       sw.pcost[i] = npc;
       sw.cost[i] = c;
-      flag[i] = imp ? 1 : 0;
+      flag[i - pb] = imp ? 1 : 0;
       const unsigned long long key = argmin_key(npc, (uint32_t)i);
       best = key < best ? key : best;
     }
-    win = block_min(best, S.red);
+    win = swarm_min(best, S, flag, pb, C, &fromx);
     const uint32_t gi = (uint32_t)win;
-    const bool from_x = flag[gi] != 0;
-    for (int d = threadIdx.x; d < D; d += blockDim.x) sg[d] = from_x ? sw.X[(int64_t)d * ld + gi] : sw.P[(int64_t)d * ld + gi];
+    for (int d = threadIdx.x; d < D; d += blockDim.x)
+      sg[d] = fromx ? sw.X[(int64_t)d * ld + gi] : sw.P[(int64_t)d * ld + gi];
     if (threadIdx.x == 0) S.gcost = sw.pcost[gi];
-    __syncthreads();
+    swarm_barrier(C);
     w = __fmul_rn(w, sw.wdamp);
   }
-  for (int64_t i = threadIdx.x; i < n; i += blockDim.x) {
-    if (flag[i]) {
+  for (int64_t i = pb + threadIdx.x; i < pe; i += blockDim.x) {
+    if (flag[i - pb]) {
       for (int d = 0; d < D; ++d) sw.P[(int64_t)d * ld + i] = sw.X[(int64_t)d * ld + i];
     }
   }
-  for (int d = threadIdx.x; d < D; d += blockDim.x) sw.g[d] = sg[d];
-  if (threadIdx.x == 0) {
-    sw.result[0] = S.gcost;
-    sw.result[1] = __uint_as_float((uint32_t)win);
-    sw.result[2] = (float)sw.maxiters;
-  }
+  publish_result(sw, sg, S.gcost, win, rank, C);
 }
 
-// dynamic shared memory: g, lb, ub (3 * maxdim floats), ODE data
-// (2 * maxsaves floats), flags (max n bytes)
+// One swarm per cluster of C CTAs (C = 1: a plain CTA).  Dynamic shared
+// memory: g, lb, ub (3 * maxdim floats), ODE data (data_floats floats), the
+// flags of this CTA's particles (one chunk of bytes).  Separable objectives
+// and ODE fits are separate kernels so each gets the registers it needs.
 template <int PPT>
-__global__ void k_batch(const BatchSwarm* __restrict__ descs, const int* __restrict__ order, int maxdim,
+__global__ void k_batch(const BatchSwarm* __restrict__ descs, const int* __restrict__ order, int C, int maxdim,
                         int data_floats) {
   extern __shared__ float dsm[];
   __shared__ BatchSmem S;
-  const BatchSwarm sw = descs[order[blockIdx.x]];
+  const int swarm = blockIdx.x / C;
+  const int rank = blockIdx.x - swarm * C;  // == cluster block rank: clusters tile the grid in x
+  const BatchSwarm sw = descs[order[swarm]];
+  float* sg = dsm;
+  float* slb = dsm + maxdim;
+  float* sub = dsm + 2 * maxdim;
+  uint8_t* flag = reinterpret_cast<uint8_t*>(dsm + 3 * maxdim + data_floats);
+  switch (sw.objective) {
+    case kSphere: run_swarm<kSphere, PPT>(sw, S, sg, slb, sub, flag, rank, C); break;
+    case kRosenbrock: run_swarm<kRosenbrock, PPT>(sw, S, sg, slb, sub, flag, rank, C); break;
+    case kRastrigin: run_swarm<kRastrigin, PPT>(sw, S, sg, slb, sub, flag, rank, C); break;
+    case kAckley: run_swarm<kAckley, PPT>(sw, S, sg, slb, sub, flag, rank, C); break;
+    default: break;
+  }
+}
+
+__global__ void __launch_bounds__(1024, 1) k_batch_ode(const BatchSwarm* __restrict__ descs, const int* __restrict__ order, int C, int maxdim,
+                            int data_floats) {
+  extern __shared__ float dsm[];
+  __shared__ BatchSmem S;
+  const int swarm = blockIdx.x / C;
+  const int rank = blockIdx.x - swarm * C;
+  const BatchSwarm sw = descs[order[swarm]];
   float* sg = dsm;
   float* slb = dsm + maxdim;
   float* sub = dsm + 2 * maxdim;
   float* data = dsm + 3 * maxdim;
   uint8_t* flag = reinterpret_cast<uint8_t*>(data + data_floats);
-  switch (sw.objective) {
-    case kSphere: run_swarm<kSphere, PPT>(sw, S, sg, slb, sub, flag); break;
-    case kRosenbrock: run_swarm<kRosenbrock, PPT>(sw, S, sg, slb, sub, flag); break;
-    case kRastrigin: run_swarm<kRastrigin, PPT>(sw, S, sg, slb, sub, flag); break;
-    case kAckley: run_swarm<kAckley, PPT>(sw, S, sg, slb, sub, flag); break;
-    case kLvFit: run_swarm_ode<kOdeLV>(sw, S, sg, slb, sub, flag, data); break;
-    case kFhnFit: run_swarm_ode<kOdeFHN>(sw, S, sg, slb, sub, flag, data); break;
-    default: break;
-  }
+  if (sw.objective == kLvFit)
+    run_swarm_ode<kOdeLV>(sw, S, sg, slb, sub, flag, data, rank, C);
+  else if (sw.objective == kFhnFit)
+    run_swarm_ode<kOdeFHN>(sw, S, sg, slb, sub, flag, data, rank, C);
 }
 
 }  // namespace pps
 
 // ---------------------------------------------------------------------------
-// host side: the batch object, arena, autotuner
+// host side: shared helpers, the batch object, the autotuner
 // ---------------------------------------------------------------------------
-using namespace pps;
+namespace pps {
 
-struct pps_batch {
-  int device = 0;
-  cudaStream_t stream = nullptr;
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  int sm_count = 0;
-  std::vector<BatchSwarm> descs;        // device pointers filled at run time
-  std::vector<std::vector<float>> host;  // per swarm: lb | ub | u0 | data
-  std::vector<size_t> offsets;           // per swarm: arena offset (bytes)
-  size_t arena_bytes = 0;
-  void* arena = nullptr;
-  size_t arena_cap = 0;
-  BatchSwarm* ddescs = nullptr;
-  int* dorder = nullptr;
-  size_t dcap = 0;
-  int tuned_threads = 0, tuned_ppt = 0;
-  int last_threads = 0, last_ppt = 0;
-  bool ran = false;
-};
+static size_t a256(size_t v) { return (v + 255) / 256 * 256; }
 
-namespace {
-
-std::mutex g_tune_mu;
-std::map<std::string, std::pair<int, int>> g_tune_cache;
-
-size_t a256(size_t v) { return (v + 255) / 256 * 256; }
-
-size_t swarm_bytes(int D, int64_t ld, int64_t ndata) {
-  // X, V, P, pcost, cost, lb, ub, u0, g, result, data
+size_t batch_swarm_bytes(int D, int64_t ld, int64_t ndata) {
   return a256(sizeof(float) * (size_t)D * ld) * 3 + a256(sizeof(float) * ld) * 2 + a256(sizeof(float) * D) * 4 +
          256 + a256(sizeof(float) * (size_t)ndata);
 }
 
-double work_estimate(const BatchSwarm& d) {
-  double per = is_ode(d.objective) ? (double)ode_cfg(d.op, d.ndata).nsteps * 12.0 : (double)d.dim;
+void batch_carve(BatchSwarm& d, char* base) {
+  const int D = d.dim;
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    char* p = base + off;
+    off += a256(bytes);
+    return p;
+  };
+  d.X = reinterpret_cast<float*>(take(sizeof(float) * (size_t)D * d.ld));
+  d.V = reinterpret_cast<float*>(take(sizeof(float) * (size_t)D * d.ld));
+  d.P = reinterpret_cast<float*>(take(sizeof(float) * (size_t)D * d.ld));
+  d.pcost = reinterpret_cast<float*>(take(sizeof(float) * d.ld));
+  d.cost = reinterpret_cast<float*>(take(sizeof(float) * d.ld));
+  d.lb = reinterpret_cast<float*>(take(sizeof(float) * D));
+  d.ub = reinterpret_cast<float*>(take(sizeof(float) * D));
+  d.u0 = reinterpret_cast<float*>(take(sizeof(float) * D));
+  d.g = reinterpret_cast<float*>(take(sizeof(float) * D));
+  d.result = reinterpret_cast<float*>(take(256));
+  float* datap = reinterpret_cast<float*>(take(sizeof(float) * (size_t)d.ndata));
+  d.data = d.ndata ? datap : nullptr;
+}
+
+double batch_work_estimate(const BatchSwarm& d) {
+  const double per = is_ode(d.objective) ? (double)ode_cfg(d.op, d.ndata).nsteps * 12.0 : (double)d.dim;
   return (double)d.n * (double)(d.maxiters + 1) * per;
 }
 
-}  // namespace
-
-extern "C" {
-
-int pps_batch_create(pps_batch** out) {
-  if (!out) return set_error(PPS_EINVAL, "out is NULL");
-  *out = nullptr;
-  int ndev = 0;
-  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return set_error(PPS_ENODEV, "no CUDA device");
-  pps_batch* b = new (std::nothrow) pps_batch();
-  if (!b) return set_error(PPS_ENOMEM, "host allocation failed");
-  cudaGetDevice(&b->device);
-  cudaDeviceGetAttribute(&b->sm_count, cudaDevAttrMultiProcessorCount, b->device);
-  cudaError_t e;
-  if ((e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking)) != cudaSuccess ||
-      (e = cudaEventCreate(&b->ev0)) != cudaSuccess || (e = cudaEventCreate(&b->ev1)) != cudaSuccess) {
-    pps_batch_destroy(b);
-    return cuda_error(e, "stream/event creation");
-  }
-  *out = b;
-  return PPS_OK;
-}
-
-int pps_batch_destroy(pps_batch* b) {
-  if (!b) return PPS_OK;
-  if (b->stream) cudaStreamSynchronize(b->stream);
-  if (b->arena) cudaFree(b->arena);
-  if (b->ddescs) cudaFree(b->ddescs);
-  if (b->dorder) cudaFree(b->dorder);
-  if (b->ev0) cudaEventDestroy(b->ev0);
-  if (b->ev1) cudaEventDestroy(b->ev1);
-  if (b->stream) cudaStreamDestroy(b->stream);
-  delete b;
-  return PPS_OK;
-}
-
-int pps_batch_add(pps_batch* b, const pps_problem* prob, int64_t n, uint64_t seed, int32_t maxiters, float w,
-                  float wdamp, float c1, float c2, int32_t* slot) {
-  if (!b || !prob) return set_error(PPS_EINVAL, "NULL argument");
+int batch_describe(const pps_problem* prob, int64_t n, uint64_t seed, int32_t maxiters, float w, float wdamp,
+                   float c1, float c2, BatchSwarm* out, std::vector<float>* host) {
+  if (!prob) return set_error(PPS_EINVAL, "problem is NULL");
   const int obj = prob->objective;
   if (!(obj == kSphere || obj == kRosenbrock || obj == kRastrigin || obj == kAckley || is_ode(obj)))
     return set_error(PPS_ENOTSUP, "objective %d is not supported in batches", obj);
@@ -493,26 +586,174 @@ int pps_batch_add(pps_batch* b, const pps_problem* prob, int64_t n, uint64_t see
   d.op.np = prob->nparams;
   d.op.dim = D;
   d.ndata = is_ode(obj) ? prob->ndata : 0;
-  std::vector<float> h;
-  h.reserve((size_t)3 * D + (size_t)d.ndata);
-  for (int k = 0; k < D; ++k) h.push_back(prob->lb ? prob->lb[k] : -INFINITY);
-  for (int k = 0; k < D; ++k) h.push_back(prob->ub ? prob->ub[k] : INFINITY);
-  for (int k = 0; k < D; ++k) h.push_back(prob->u0 ? prob->u0[k] : 0.0f);
-  for (int64_t k = 0; k < d.ndata; ++k) h.push_back(prob->data[k]);
-  b->offsets.push_back(b->arena_bytes);
-  b->arena_bytes += swarm_bytes(D, d.ld, d.ndata);
-  b->descs.push_back(d);
-  b->host.push_back(std::move(h));
-  b->ran = false;
-  if (slot) *slot = (int32_t)(b->descs.size() - 1);
+  host->clear();
+  host->reserve((size_t)3 * D + (size_t)d.ndata);
+  for (int k = 0; k < D; ++k) host->push_back(prob->lb ? prob->lb[k] : -INFINITY);
+  for (int k = 0; k < D; ++k) host->push_back(prob->ub ? prob->ub[k] : INFINITY);
+  for (int k = 0; k < D; ++k) host->push_back(prob->u0 ? prob->u0[k] : 0.0f);
+  for (int64_t k = 0; k < d.ndata; ++k) host->push_back(prob->data[k]);
+  *out = d;
   return PPS_OK;
 }
 
-}  // extern "C"
+size_t batch_smem_bytes(int maxdim, int data_floats, int64_t maxchunk) {
+  return sizeof(float) * (3 * (size_t)maxdim + (size_t)data_floats) + (size_t)maxchunk + 64;
+}
+
+// Shape limits: PPS_BATCH_MAX_CLUSTER (1..16, default 4) caps the CTAs a swarm
+// is split over, PPS_ODE_THREADS (256/512/1024, default 512) is the largest
+// block of an ODE-fit CTA.  They change how work is placed, never what is
+// computed.  Clusters above 8 CTAs are a non-portable size.
+static int env_int(const char* name, int dflt, int lo, int hi) {
+  const char* e = getenv(name);
+  const int v = e ? atoi(e) : dflt;
+  return (v >= lo && v <= hi) ? v : dflt;
+}
+static int max_cluster() {
+  static const int v = env_int("PPS_BATCH_MAX_CLUSTER", 4, 1, 16);
+  return v;
+}
+static int ode_threads() {
+  static const int v = env_int("PPS_ODE_THREADS", 512, 256, 1024);
+  return v;
+}
+
+LaunchGroup batch_group_of(const BatchSwarm& d, int threads, int ppt) {
+  LaunchGroup g{};
+  const int cmax = max_cluster();
+  if (is_ode(d.objective)) {
+    g.kind = 1;
+    const int tmax = ode_threads();
+    g.T = d.n <= 256 ? 256 : (d.n <= 512 || tmax <= 512 ? (tmax < 512 ? 256 : 512) : 1024);
+    const int64_t c = (d.n + g.T - 1) / g.T;
+    g.C = (int)(c < cmax ? c : cmax);
+  } else {
+    g.kind = 0;
+    g.T = threads;
+    const int64_t width = (int64_t)threads * ppt * 8;
+    const int64_t c = (d.n + width - 1) / width;
+    g.C = (int)(c < cmax ? c : cmax);
+    if (g.C < 1) g.C = 1;
+  }
+  return g;
+}
+
+static int64_t chunk_of(int64_t n, int C, int width) { return cta_chunk(n, C, width); }
+
+void batch_plan(const std::vector<BatchSwarm>& descs, int threads, int ppt, std::vector<int>* order,
+                std::vector<LaunchGroup>* groups) {
+  const int ns = (int)descs.size();
+  std::map<std::tuple<int, int, int>, std::vector<int>> by;
+  for (int k = 0; k < ns; ++k) {
+    const LaunchGroup g = batch_group_of(descs[k], threads, ppt);
+    by[std::make_tuple(-g.C, g.kind, g.T)].push_back(k);  // larger clusters first
+  }
+  order->clear();
+  groups->clear();
+  for (auto& kv : by) {
+    LaunchGroup g{};
+    g.C = -std::get<0>(kv.first);
+    g.kind = std::get<1>(kv.first);
+    g.T = std::get<2>(kv.first);
+    g.offset = (int)order->size();
+    g.maxdim = 1;
+    std::vector<int>& idx = kv.second;
+    std::stable_sort(idx.begin(), idx.end(), [&](int a, int c) {
+      return batch_work_estimate(descs[a]) > batch_work_estimate(descs[c]);
+    });
+    for (int k : idx) {
+      order->push_back(k);
+      g.maxdim = std::max(g.maxdim, descs[k].dim);
+      g.data_floats = std::max(g.data_floats, (int)descs[k].ndata);
+      g.maxn = std::max(g.maxn, descs[k].n);
+    }
+    g.count = (int)idx.size();
+    groups->push_back(g);
+  }
+}
+
+// Launch a group with clusters of g.C CTAs, or of a smaller size when the
+// device cannot co-schedule that many with this block shape.  How a swarm is
+// split over CTAs does not change its result (draws are keyed by particle,
+// the argmin is over the whole swarm), only its speed.
+template <typename Kernel>
+static int launch_clustered(Kernel kernel, cudaStream_t stream, const BatchSwarm* ddescs, const int* dorder,
+                            const LaunchGroup& g, int width) {
+  cudaError_t e = cudaSuccess;
+  for (int C = g.C; C >= 1; C = (C > 8 ? 8 : C / 2)) {
+    const size_t smem = batch_smem_bytes(g.maxdim, g.data_floats, chunk_of(g.maxn, C, width));
+    if (smem > 200 * 1024) continue;
+    if ((e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess)
+      return cuda_error(e, "cudaFuncSetAttribute");
+    if (C > 8 && cudaFuncSetAttribute(kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
+      cudaGetLastError();
+      continue;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)(g.count * C));
+    cfg.blockDim = dim3((unsigned)g.T);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)C;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int active = 0;
+    if (C > 1 && (cudaOccupancyMaxActiveClusters(&active, kernel, &cfg) != cudaSuccess || active < 1)) {
+      cudaGetLastError();  // clear the query's error and try a smaller cluster
+      continue;
+    }
+    e = cudaLaunchKernelEx(&cfg, kernel, ddescs, dorder + g.offset, C, g.maxdim, g.data_floats);
+    if (e != cudaSuccess) return cuda_error(e, "cudaLaunchKernelEx(batch)");
+    return PPS_OK;
+  }
+  return set_error(PPS_ENOTSUP, "batch needs more shared memory than a CTA has (dim, data or n too large)");
+}
+
+int batch_launch_group(cudaStream_t stream, const BatchSwarm* ddescs, const int* dorder, const LaunchGroup& g,
+                       int ppt) {
+  if (g.kind == 1) return launch_clustered(k_batch_ode, stream, ddescs, dorder, g, g.T);
+  if (ppt == 4) return launch_clustered(k_batch<4>, stream, ddescs, dorder, g, g.T * 4);
+  if (ppt == 2) return launch_clustered(k_batch<2>, stream, ddescs, dorder, g, g.T * 2);
+  return launch_clustered(k_batch<1>, stream, ddescs, dorder, g, g.T);
+}
+
+}  // namespace pps
+
+using namespace pps;
+
+struct pps_batch {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  static constexpr int kGroupStreams = 5;  // one per cluster size 16, 8, 4, 2, 1
+  cudaStream_t gstream[kGroupStreams] = {};
+  cudaEvent_t gevent[kGroupStreams] = {};
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  int sm_count = 0;
+  std::vector<BatchSwarm> descs;        // device pointers filled at run time
+  std::vector<std::vector<float>> host;  // per swarm: lb | ub | u0 | data
+  std::vector<size_t> offsets;           // per swarm: arena offset (bytes)
+  size_t arena_bytes = 0;
+  void* arena = nullptr;
+  size_t arena_cap = 0;
+  BatchSwarm* ddescs = nullptr;
+  int* dorder = nullptr;
+  size_t dcap = 0;
+  int tuned_threads = 0, tuned_ppt = 0;
+  int last_threads = 0, last_ppt = 0;
+  int last_groups = 0, last_max_cluster = 0;
+  bool ran = false;
+};
 
 namespace {
 
-int prepare(pps_batch* b, std::vector<int>& order, int& maxdim, int& data_floats, int64_t& maxn) {
+std::mutex g_tune_mu;
+std::map<std::string, std::pair<int, int>> g_tune_cache;
+
+int prepare(pps_batch* b) {
   const size_t ns = b->descs.size();
   if (b->arena_cap < b->arena_bytes) {
     if (b->arena) cudaFree(b->arena);
@@ -531,72 +772,47 @@ int prepare(pps_batch* b, std::vector<int>& order, int& maxdim, int& data_floats
     PPS_CUDA(cudaMalloc(&b->dorder, sizeof(int) * ns));
     b->dcap = ns;
   }
-  maxdim = 1;
-  data_floats = 0;
-  maxn = 1;
   char* base = static_cast<char*>(b->arena);
   for (size_t k = 0; k < ns; ++k) {
     BatchSwarm& d = b->descs[k];
     const int D = d.dim;
-    size_t off = b->offsets[k];
-    auto take = [&](size_t bytes) {
-      char* p = base + off;
-      off += a256(bytes);
-      return p;
-    };
-    d.X = reinterpret_cast<float*>(take(sizeof(float) * (size_t)D * d.ld));
-    d.V = reinterpret_cast<float*>(take(sizeof(float) * (size_t)D * d.ld));
-    d.P = reinterpret_cast<float*>(take(sizeof(float) * (size_t)D * d.ld));
-    d.pcost = reinterpret_cast<float*>(take(sizeof(float) * d.ld));
-    d.cost = reinterpret_cast<float*>(take(sizeof(float) * d.ld));
-    float* lbub = reinterpret_cast<float*>(take(sizeof(float) * D));
-    float* ubp = reinterpret_cast<float*>(take(sizeof(float) * D));
-    float* u0p = reinterpret_cast<float*>(take(sizeof(float) * D));
-    d.g = reinterpret_cast<float*>(take(sizeof(float) * D));
-    d.result = reinterpret_cast<float*>(take(256));
-    float* datap = reinterpret_cast<float*>(take(sizeof(float) * (size_t)d.ndata));
-    d.lb = lbub;
-    d.ub = ubp;
-    d.u0 = u0p;
-    d.data = d.ndata ? datap : nullptr;
+    batch_carve(d, base + b->offsets[k]);
+    d.mail = nullptr;
+    d.done = nullptr;
     const std::vector<float>& h = b->host[k];
-    PPS_CUDA(cudaMemcpyAsync(lbub, h.data(), sizeof(float) * D, cudaMemcpyHostToDevice, b->stream));
-    PPS_CUDA(cudaMemcpyAsync(ubp, h.data() + D, sizeof(float) * D, cudaMemcpyHostToDevice, b->stream));
-    PPS_CUDA(cudaMemcpyAsync(u0p, h.data() + 2 * D, sizeof(float) * D, cudaMemcpyHostToDevice, b->stream));
+    PPS_CUDA(cudaMemcpyAsync(const_cast<float*>(d.lb), h.data(), sizeof(float) * D, cudaMemcpyHostToDevice, b->stream));
+    PPS_CUDA(cudaMemcpyAsync(const_cast<float*>(d.ub), h.data() + D, sizeof(float) * D, cudaMemcpyHostToDevice, b->stream));
+    PPS_CUDA(cudaMemcpyAsync(const_cast<float*>(d.u0), h.data() + 2 * D, sizeof(float) * D, cudaMemcpyHostToDevice,
+                             b->stream));
     if (d.ndata)
-      PPS_CUDA(cudaMemcpyAsync(datap, h.data() + 3 * D, sizeof(float) * (size_t)d.ndata, cudaMemcpyHostToDevice,
-                               b->stream));
-    maxdim = std::max(maxdim, D);
-    data_floats = std::max(data_floats, (int)d.ndata);
-    maxn = std::max(maxn, d.ld);
+      PPS_CUDA(cudaMemcpyAsync(const_cast<float*>(d.data), h.data() + 3 * D, sizeof(float) * (size_t)d.ndata,
+                               cudaMemcpyHostToDevice, b->stream));
   }
-  // longest estimated work first
-  order.resize(ns);
-  for (size_t k = 0; k < ns; ++k) order[k] = (int)k;
-  std::stable_sort(order.begin(), order.end(),
-                   [&](int a, int c) { return work_estimate(b->descs[a]) > work_estimate(b->descs[c]); });
   PPS_CUDA(cudaMemcpyAsync(b->ddescs, b->descs.data(), sizeof(BatchSwarm) * ns, cudaMemcpyHostToDevice, b->stream));
-  PPS_CUDA(cudaMemcpyAsync(b->dorder, order.data(), sizeof(int) * ns, cudaMemcpyHostToDevice, b->stream));
   return PPS_OK;
 }
 
-size_t smem_bytes(int maxdim, int data_floats, int64_t maxn) {
-  return sizeof(float) * (3 * (size_t)maxdim + (size_t)data_floats) + (size_t)maxn + 16;
-}
-
-int launch_batch(pps_batch* b, int threads, int ppt, int ns, int maxdim, int data_floats, int64_t maxn) {
-  const size_t smem = smem_bytes(maxdim, data_floats, maxn);
-  cudaError_t e;
-  if (ppt == 2) {
-    e = cudaFuncSetAttribute(k_batch<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return cuda_error(e, "cudaFuncSetAttribute");
-    k_batch<2><<<ns, threads, smem, b->stream>>>(b->ddescs, b->dorder, maxdim, data_floats);
-  } else {
-    e = cudaFuncSetAttribute(k_batch<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return cuda_error(e, "cudaFuncSetAttribute");
-    k_batch<1><<<ns, threads, smem, b->stream>>>(b->ddescs, b->dorder, maxdim, data_floats);
+// every group on its own stream, joined back into b->stream; ev0/ev1 bracket it
+int run_groups(pps_batch* b, int threads, int ppt, int* ngroups, int* maxc) {
+  std::vector<int> order;
+  std::vector<LaunchGroup> groups;
+  batch_plan(b->descs, threads, ppt, &order, &groups);
+  PPS_CUDA(cudaMemcpyAsync(b->dorder, order.data(), sizeof(int) * order.size(), cudaMemcpyHostToDevice, b->stream));
+  PPS_CUDA(cudaEventRecord(b->ev0, b->stream));
+  int rc = PPS_OK;
+  for (size_t k = 0; k < groups.size(); ++k) {
+    cudaStream_t st = b->gstream[k % pps_batch::kGroupStreams];
+    PPS_CUDA(cudaStreamWaitEvent(st, b->ev0, 0));
+    if ((rc = batch_launch_group(st, b->ddescs, b->dorder, groups[k], ppt))) return rc;
+    PPS_CUDA(cudaEventRecord(b->gevent[k % pps_batch::kGroupStreams], st));
+    PPS_CUDA(cudaStreamWaitEvent(b->stream, b->gevent[k % pps_batch::kGroupStreams], 0));
   }
-  PPS_CUDA(cudaGetLastError());
+  PPS_CUDA(cudaEventRecord(b->ev1, b->stream));
+  if (ngroups) *ngroups = (int)groups.size();
+  if (maxc) {
+    *maxc = 1;
+    for (const auto& g : groups) *maxc = std::max(*maxc, g.C);
+  }
   return PPS_OK;
 }
 
@@ -612,9 +828,9 @@ std::string shape_key(const pps_batch* b) {
   }
   const double ns = (double)std::max<size_t>(1, b->descs.size());
   char buf[256];
-  snprintf(buf, sizeof(buf), "%d,%d,%d,%d,%d,%d|%d|%d|%d|%zu", cnt[0] > 0, cnt[1] > 0, cnt[2] > 0, cnt[3] > 0,
+  snprintf(buf, sizeof(buf), "%d,%d,%d,%d,%d,%d|%d|%d|%d|%d", cnt[0] > 0, cnt[1] > 0, cnt[2] > 0, cnt[3] > 0,
            cnt[4] > 0, cnt[5] > 0, (int)std::log2(1 + dims / ns), (int)std::log2(1 + parts / ns),
-           (int)std::log2(1 + iters / ns), (size_t)std::log2(1.0 + ns));
+           (int)std::log2(1 + iters / ns), (int)std::log2(1.0 + ns));
   return buf;
 }
 
@@ -622,20 +838,77 @@ std::string shape_key(const pps_batch* b) {
 
 extern "C" {
 
+int pps_batch_create(pps_batch** out) {
+  if (!out) return set_error(PPS_EINVAL, "out is NULL");
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return set_error(PPS_ENODEV, "no CUDA device");
+  pps_batch* b = new (std::nothrow) pps_batch();
+  if (!b) return set_error(PPS_ENOMEM, "host allocation failed");
+  cudaGetDevice(&b->device);
+  cudaDeviceGetAttribute(&b->sm_count, cudaDevAttrMultiProcessorCount, b->device);
+  cudaError_t e;
+  if ((e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking)) != cudaSuccess ||
+      (e = cudaEventCreate(&b->ev0)) != cudaSuccess || (e = cudaEventCreate(&b->ev1)) != cudaSuccess) {
+    pps_batch_destroy(b);
+    return cuda_error(e, "stream/event creation");
+  }
+  for (int k = 0; k < pps_batch::kGroupStreams; ++k) {
+    if ((e = cudaStreamCreateWithFlags(&b->gstream[k], cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaEventCreateWithFlags(&b->gevent[k], cudaEventDisableTiming)) != cudaSuccess) {
+      pps_batch_destroy(b);
+      return cuda_error(e, "stream/event creation");
+    }
+  }
+  *out = b;
+  return PPS_OK;
+}
+
+int pps_batch_destroy(pps_batch* b) {
+  if (!b) return PPS_OK;
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  for (int k = 0; k < pps_batch::kGroupStreams; ++k) {
+    if (b->gstream[k]) {
+      cudaStreamSynchronize(b->gstream[k]);
+      cudaStreamDestroy(b->gstream[k]);
+    }
+    if (b->gevent[k]) cudaEventDestroy(b->gevent[k]);
+  }
+  if (b->arena) cudaFree(b->arena);
+  if (b->ddescs) cudaFree(b->ddescs);
+  if (b->dorder) cudaFree(b->dorder);
+  if (b->ev0) cudaEventDestroy(b->ev0);
+  if (b->ev1) cudaEventDestroy(b->ev1);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+  return PPS_OK;
+}
+
+int pps_batch_add(pps_batch* b, const pps_problem* prob, int64_t n, uint64_t seed, int32_t maxiters, float w,
+                  float wdamp, float c1, float c2, int32_t* slot) {
+  if (!b) return set_error(PPS_EINVAL, "batch is NULL");
+  BatchSwarm d;
+  std::vector<float> h;
+  const int rc = batch_describe(prob, n, seed, maxiters, w, wdamp, c1, c2, &d, &h);
+  if (rc) return rc;
+  b->offsets.push_back(b->arena_bytes);
+  b->arena_bytes += batch_swarm_bytes(d.dim, d.ld, d.ndata);
+  b->descs.push_back(d);
+  b->host.push_back(std::move(h));
+  b->ran = false;
+  if (slot) *slot = (int32_t)(b->descs.size() - 1);
+  return PPS_OK;
+}
+
 int pps_batch_run(pps_batch* b, float* device_ms) {
   if (!b) return set_error(PPS_EINVAL, "batch is NULL");
   if (b->descs.empty()) return set_error(PPS_EINVAL, "batch is empty");
   int dev = -1;
   cudaGetDevice(&dev);
   if (dev != b->device) PPS_CUDA(cudaSetDevice(b->device));
-  std::vector<int> order;
-  int maxdim = 1, data_floats = 0;
-  int64_t maxn = 1;
-  int rc = prepare(b, order, maxdim, data_floats, maxn);
+  int rc = prepare(b);
   if (rc) return rc;
   const int ns = (int)b->descs.size();
-  if (smem_bytes(maxdim, data_floats, maxn) > 200 * 1024)
-    return set_error(PPS_ENOTSUP, "batch needs more shared memory than a CTA has (dim, data or n too large)");
   // autotune the block shape for this batch shape (cached)
   int threads = b->tuned_threads, ppt = b->tuned_ppt;
   if (!threads) {
@@ -651,17 +924,19 @@ int pps_batch_run(pps_batch* b, float* device_ms) {
     if (!threads) {
       // time each candidate on this batch with a few iterations per swarm
       std::vector<BatchSwarm> saved = b->descs;
-      for (auto& d : b->descs) d.maxiters = std::min(d.maxiters, 4);
+      bool all_ode = true;
+      for (auto& d : b->descs) {
+        d.maxiters = std::min(d.maxiters, 4);
+        all_ode = all_ode && is_ode(d.objective);
+      }
       PPS_CUDA(cudaMemcpyAsync(b->ddescs, b->descs.data(), sizeof(BatchSwarm) * ns, cudaMemcpyHostToDevice, b->stream));
       const int cand_t[3] = {128, 256, 512};
-      const int cand_p[2] = {1, 2};
+      const int cand_p[3] = {1, 2, 4};
       float best_ms = 1e30f;
       for (int ct : cand_t) {
         for (int cp : cand_p) {
-          if (cp == 2 && data_floats > 0 && maxdim <= 4) continue;  // ODE swarms ignore PPT
-          PPS_CUDA(cudaEventRecord(b->ev0, b->stream));
-          if ((rc = launch_batch(b, ct, cp, ns, maxdim, data_floats, maxn))) return rc;
-          PPS_CUDA(cudaEventRecord(b->ev1, b->stream));
+          if (cp == 2 && all_ode) continue;  // ODE swarms ignore PPT
+          if ((rc = run_groups(b, ct, cp, nullptr, nullptr))) return rc;
           PPS_CUDA(cudaEventSynchronize(b->ev1));
           float ms = 0.0f;
           PPS_CUDA(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
@@ -678,9 +953,7 @@ int pps_batch_run(pps_batch* b, float* device_ms) {
       g_tune_cache[key] = {threads, ppt};
     }
   }
-  PPS_CUDA(cudaEventRecord(b->ev0, b->stream));
-  if ((rc = launch_batch(b, threads, ppt, ns, maxdim, data_floats, maxn))) return rc;
-  PPS_CUDA(cudaEventRecord(b->ev1, b->stream));
+  if ((rc = run_groups(b, threads, ppt, &b->last_groups, &b->last_max_cluster))) return rc;
   PPS_CUDA(cudaEventSynchronize(b->ev1));
   if (device_ms) PPS_CUDA(cudaEventElapsedTime(device_ms, b->ev0, b->ev1));
   b->last_threads = threads;
@@ -695,8 +968,8 @@ int pps_batch_set_shape(pps_batch* b, int32_t threads, int32_t ppt) {
     b->tuned_threads = b->tuned_ppt = 0;
     return PPS_OK;
   }
-  if (!(threads == 128 || threads == 256 || threads == 512) || !(ppt == 1 || ppt == 2))
-    return set_error(PPS_EINVAL, "block shape must be threads in {128, 256, 512} and ppt in {1, 2}");
+  if (!(threads == 128 || threads == 256 || threads == 512) || !(ppt == 1 || ppt == 2 || ppt == 4))
+    return set_error(PPS_EINVAL, "block shape must be threads in {128, 256, 512} and ppt in {1, 2, 4}");
   b->tuned_threads = threads;
   b->tuned_ppt = ppt;
   return PPS_OK;

@@ -13,6 +13,9 @@
 //     du1 = p1 u1 - p2 u1 u2,  du2 = -p3 u2 + p4 u1 u2
 //   FitzHugh-Nagumo benchmarks/Fitzhugh_Nagumo/ode_estimation.jl:6-12
 //     dv = v - v^3/3 - w + l,  dw = tinv (v + a - b w),  p = (a, b, tinv), l fixed
+// evaluated in factored form -- u1 fma(-p2, u2, p1), u2 fma(p4, u1, -p3),
+// (fma(v^3, -1/3, v) - w) + l, tinv fma(-b, w, v + a) -- two roundings per
+// term and no division, which halves the instructions of an RK4 step.
 #pragma once
 #include "pps_device.cuh"
 
@@ -44,12 +47,12 @@ __host__ __device__ inline OdeCfg ode_cfg(const ObjParams& op, int64_t ndata) {
 template <int MODEL>
 __device__ __forceinline__ void ode_rhs(const float* p, float l, float u0, float u1, float& d0, float& d1) {
   if constexpr (MODEL == kOdeLV) {
-    d0 = __fsub_rn(__fmul_rn(p[0], u0), __fmul_rn(__fmul_rn(p[1], u0), u1));
-    d1 = __fadd_rn(__fmul_rn(-p[2], u1), __fmul_rn(__fmul_rn(p[3], u0), u1));
+    d0 = __fmul_rn(u0, __fmaf_rn(-p[1], u1, p[0]));
+    d1 = __fmul_rn(u1, __fmaf_rn(p[3], u0, -p[2]));
   } else {
     const float v3 = __fmul_rn(__fmul_rn(u0, u0), u0);
-    d0 = __fadd_rn(__fsub_rn(__fsub_rn(u0, __fdiv_rn(v3, 3.0f)), u1), l);
-    d1 = __fmul_rn(p[2], __fsub_rn(__fadd_rn(u0, p[0]), __fmul_rn(p[1], u1)));
+    d0 = __fadd_rn(__fsub_rn(__fmaf_rn(v3, -0x1.555556p-2f, u0), u1), l);
+    d1 = __fmul_rn(p[2], __fmaf_rn(-p[1], u1, __fadd_rn(u0, p[0])));
   }
 }
 

@@ -13,6 +13,7 @@ from .solve import (HybridPSOCache, OptimizationSolution, OptimizationStats, PSO
                     solve_)
 from .swarm import Swarm
 from .batch import Batch
+from .serve import Server
 from . import ode
 
 __all__ = [
@@ -21,5 +22,5 @@ __all__ = [
     "PSOCache", "HybridPSOCache", "OptimizationSolution", "OptimizationStats", "Swarm", "PPSError",
     "ArgumentError", "evaluate", "Objective", "REGISTRY", "sphere", "rosenbrock", "rastrigin", "ackley",
     "lotka_volterra_fit", "fitzhugh_nagumo_fit", "mlp_regression", "beale", "booth", "himmelblau",
-    "quadratic", "boundary_quadratic", "CUDA", "Batch", "ode",
+    "quadratic", "boundary_quadratic", "CUDA", "Batch", "Server", "ode",
 ]

@@ -77,6 +77,35 @@ class LocalOpts(ctypes.Structure):
     ]
 
 
+class ServeConfig(ctypes.Structure):
+    _fields_ = [
+        ("memory_budget", ctypes.c_uint64),
+        ("max_launches", ctypes.c_int32),
+        ("max_pack", ctypes.c_int32),
+        ("threads", ctypes.c_int32),
+        ("ppt", ctypes.c_int32),
+        ("tick_us", ctypes.c_double),
+    ]
+
+
+class ServeStats(ctypes.Structure):
+    _fields_ = [
+        ("submitted", ctypes.c_uint64),
+        ("completed", ctypes.c_uint64),
+        ("launches", ctypes.c_uint64),
+        ("solves_per_s", ctypes.c_double),
+        ("p50_ms", ctypes.c_double),
+        ("p99_ms", ctypes.c_double),
+        ("mean_ms", ctypes.c_double),
+        ("max_ms", ctypes.c_double),
+        ("mean_pack", ctypes.c_double),
+        ("arena_bytes", ctypes.c_uint64),
+        ("arena_peak_bytes", ctypes.c_uint64),
+        ("queued", ctypes.c_int32),
+        ("running", ctypes.c_int32),
+    ]
+
+
 class DeviceSwarm(ctypes.Structure):
     """pps_device_swarm: a swarm in device buffers owned by the caller."""
 
@@ -127,6 +156,16 @@ _SIGNATURES = {
                                       ctypes.POINTER(ctypes.c_int32), ctypes.POINTER(ctypes.c_uint64)]),
     "pps_batch_result": (ctypes.c_int, [_P, ctypes.c_int32, c_float_p, c_float_p, ctypes.POINTER(ctypes.c_int64)]),
     "pps_batch_get_state": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_int32, c_float_p]),
+    "pps_serve_start": (ctypes.c_int, [ctypes.POINTER(ServeConfig), ctypes.POINTER(_P)]),
+    "pps_serve_submit": (ctypes.c_int, [_P, ctypes.POINTER(Problem), ctypes.c_int64, ctypes.c_uint64, ctypes.c_int32,
+                                        ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                                        ctypes.POINTER(ctypes.c_uint64)]),
+    "pps_serve_poll": (ctypes.c_int, [_P, ctypes.c_uint64, c_float_p, c_float_p, ctypes.POINTER(ctypes.c_int64),
+                                      ctypes.POINTER(ctypes.c_double)]),
+    "pps_serve_wait": (ctypes.c_int, [_P, ctypes.c_uint64, c_float_p, c_float_p, ctypes.POINTER(ctypes.c_int64),
+                                      ctypes.POINTER(ctypes.c_double), ctypes.c_double]),
+    "pps_serve_stats_get": (ctypes.c_int, [_P, ctypes.POINTER(ServeStats)]),
+    "pps_serve_stop": (ctypes.c_int, [_P]),
     "pps_hybrid_lbfgs": (ctypes.c_int, [_P, ctypes.POINTER(LocalOpts), c_float_p, c_float_p,
                                         ctypes.POINTER(ctypes.c_int64), c_float_p]),
     "pps_hybrid_bfgs": (ctypes.c_int, [_P, ctypes.POINTER(LocalOpts), c_float_p, c_float_p,

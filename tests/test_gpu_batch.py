@@ -13,16 +13,17 @@ def _mixed(pps):
     cases = []
     specs = [("sphere", 3, 1, 5), ("rosenbrock", 3, 1000, 60), ("rastrigin", 17, 257, 40), ("ackley", 64, 100, 30),
              ("rastrigin", 100, 1500, 10), ("rosenbrock", 2, 37, 0), ("ackley", 5, 1, 25), ("sphere", 1, 64, 3),
-             ("rosenbrock", 33, 513, 20), ("rastrigin", 2, 5000, 15)]
+             ("rosenbrock", 33, 513, 20), ("rastrigin", 2, 5000, 15),
+             ("rastrigin", 8, 40000, 6)]  # split over a cluster of 16 CTAs
     for k, (name, D, n, iters) in enumerate(specs):
         prm = pps.REGISTRY[name].default_params
         lo = -5.12 if name == "rastrigin" else -5.0
         prob = pps.OptimizationProblem(pps.REGISTRY[name], np.zeros(D, np.float32), list(prm) or None,
                                        lb=np.full(D, lo, np.float32), ub=np.full(D, -lo, np.float32))
         cases.append((prob, n, iters, 100 + k, float(rng.uniform(0.6, 0.9)), float(rng.choice([1.0, 0.99]))))
-    for k, model in enumerate(("lv", "fhn", "lv")):
+    for k, model in enumerate(("lv", "fhn", "lv", "lv")):
         prob, _ = pps.ode.synthetic_fit(model, 50 + k)
-        cases.append((prob, (64, 33, 256)[k], (8, 4, 6)[k], 200 + k, 0.7298, 1.0))
+        cases.append((prob, (64, 33, 256, 4096)[k], (8, 4, 6, 3)[k], 200 + k, 0.7298, 1.0))
     return cases
 
 
