@@ -15,6 +15,17 @@ Prints ONE JSON line (rank 0).  Extra measurements ride in the same line:
   roofline     the step kernel against the measured HBM copy bandwidth
   cpu_baseline the oracle (C restatement, all host cores) on a bounded sample
   async        ParallelPSOKernel(global_update=false) on the same workload
+  hybrid       HybridPSO: 65,536 x 10-D Rosenbrock and Ackley, 200 sync PSO
+               iterations then L-BFGS (m=10, Armijo 1e-4, <=100 iterations,
+               gtol 1e-5) on every particle
+  ode_batch    512 Lotka-Volterra + 512 FitzHugh-Nagumo fits (particles per fit
+               from {256, 1024, 4096}, 100 iterations, RK4 dt=0.01) in one
+               batched launch, against the same fits solved one at a time
+  served       the mixed request stream (Rosenbrock / Rastrigin / Ackley /
+               Lotka-Volterra fit, dim U{2..64}, particles U{256..16384},
+               maxiters U{100..2000}) through the continuous-batching server:
+               a closed-loop saturation run, a Poisson(2000/s) open-loop run,
+               p50/p99 time to solution, against one-at-a-time plain solves
 With --impl reference the oracle's CPU implementation is timed instead
 (the Julia reference cannot run here: no Julia toolchain).
 """
@@ -31,6 +42,10 @@ import time
 from pathlib import Path
 
 import numpy as np
+
+# the server keeps up to 16 launches in flight on separate streams; give them
+# separate hardware queues (must be set before the CUDA context exists)
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT / "parallelparticleswarms.jl_gb300"))
@@ -180,6 +195,158 @@ def run_reference(args, rank, world):
     return 0
 
 
+# --------------------------------------------------------------------------
+# further workloads (each returns a dict for the JSON line)
+# --------------------------------------------------------------------------
+def run_hybrid(pps) -> dict:
+    """HybridPSO: 65,536 x 10-D Rosenbrock and Ackley, bounds [-5, 5], 200
+    synchronous PSO iterations, then L-BFGS from every particle's best."""
+    out = {"workload": "HybridPSO 65536 x 10-D, 200 sync PSO iterations + per-particle L-BFGS "
+                       "(m=10, Armijo c1=1e-4, <=100 iterations, gtol 1e-5)"}
+    n, D = 65536, 10
+    for name, prm in (("rosenbrock", [1.0, 100.0]), ("ackley", [20.0, 0.2, 1.0])):
+        prob = pps.OptimizationProblem(pps.REGISTRY[name], np.zeros(D, np.float32), prm,
+                                       lb=np.full(D, -5.0, np.float32), ub=np.full(D, 5.0, np.float32))
+        with pps.Swarm(prob, n, seed=7) as sw:
+            sw.init()
+            sw.sync_run(20)  # warm
+            sw.init()
+            pso_ms = sw.sync_run(200)
+            _, pso_cost, _ = sw.gbest()
+            u, f, idx, local_ms = sw.local_stage("lbfgs", history=10, maxiters=100, armijo_c1=1e-4, gtol=1e-5)
+            iters = sw.get(7)
+        out[name] = {"pso_ms": pso_ms, "pso_particle_iters_per_s": n * 200 / (pso_ms / 1e3),
+                     "pso_best": pso_cost, "local_ms": local_ms, "local_particles_per_s": n / (local_ms / 1e3),
+                     "local_mean_iters": float(np.mean(iters)), "best": f, "solve_ms": pso_ms + local_ms}
+    return out
+
+
+def _ode_fits(pps, count_each=512, seed=0):
+    rng = np.random.default_rng(seed)
+    fits = []
+    for k in range(2 * count_each):
+        prob, truth = pps.ode.synthetic_fit("lv" if k < count_each else "fhn", k)
+        fits.append((prob, truth, int(rng.choice([256, 1024, 4096]))))
+    return fits
+
+
+def run_ode_batch(pps, count_each=512) -> dict:
+    """512 LV + 512 FHN fits in one batched launch vs the same fits one at a
+    time (a sample, scaled to all 1024)."""
+    fits = _ode_fits(pps, count_each)
+    with pps.Batch() as b:
+        for k, (p, tr, n) in enumerate(fits):
+            b.add(p, n, maxiters=100, seed=k)
+        b.run()  # autotune + warm
+        t0 = time.perf_counter()
+        ms = b.run()
+        wall = time.perf_counter() - t0
+        res = [b.result(k) for k in range(len(fits))]
+        shape = b.info()
+    rel = [float(np.max(np.abs(r[0] - f[1]) / np.abs(f[1]))) for r, f in zip(res, fits)]
+    # plain: the same fits solved alone, one after another (a stratified sample)
+    sample = list(range(0, count_each, 32)) + list(range(count_each, 2 * count_each, 32))
+    plain_ms = {}
+    same = True
+    for k in sample:
+        p, tr, n = fits[k]
+        with pps.Swarm(p, n, seed=k) as sw:
+            sw.init()
+            t0 = time.perf_counter()
+            sw.sync_run(100)
+            u, c, i = sw.gbest()
+            plain_ms[k] = (time.perf_counter() - t0) * 1e3
+        same &= bool(np.array_equal(u, res[k][0]) and c == res[k][1])
+    lv = [plain_ms[k] for k in sample if k < 512]
+    fhn = [plain_ms[k] for k in sample if k >= 512]
+    plain_total_s = count_each * (np.mean(lv) + np.mean(fhn)) / 1e3
+    return {"workload": f"{count_each} Lotka-Volterra + {count_each} FitzHugh-Nagumo fits, particles per fit from {{256,1024,4096}}, "
+                        "100 iterations, RK4 dt=0.01, SSE",
+            "batched_device_ms": ms, "batched_wall_s": wall, "batched_solves_per_s": len(fits) / wall,
+            "plain_solves_per_s": len(fits) / plain_total_s, "plain_sample": len(sample),
+            "speedup_vs_plain": plain_total_s / wall, "same_result_alone_and_batched": same,
+            "param_rel_err_median": float(np.median(rel)), "param_rel_err_p90": float(np.percentile(rel, 90)),
+            "block_shape": shape}
+
+
+def _request_pool(pps, count, seed):
+    """Mixed requests; LV fits reuse a pool of 64 synthetic datasets."""
+    rng = np.random.default_rng(seed)
+    lv_pool = [pps.ode.synthetic_fit("lv", 10_000 + k)[0] for k in range(64)]
+    reqs = []
+    for _ in range(count):
+        kind = int(rng.integers(4))
+        n = int(rng.integers(256, 16385))
+        iters = int(rng.integers(100, 2001))
+        s = int(rng.integers(0, 2**62))
+        if kind == 3:
+            reqs.append((lv_pool[int(rng.integers(64))], n, iters, s))
+            continue
+        D = int(rng.integers(2, 65))
+        name = ("rosenbrock", "rastrigin", "ackley")[kind]
+        lo = -5.12 if name == "rastrigin" else -5.0
+        obj = pps.REGISTRY[name]
+        reqs.append((pps.OptimizationProblem(obj, np.zeros(D, np.float32), list(obj.default_params),
+                                             lb=np.full(D, lo, np.float32), ub=np.full(D, -lo, np.float32)),
+                     n, iters, s))
+    return reqs
+
+
+def run_served(pps, args) -> dict:
+    cfg = dict(memory_budget=24 << 30, max_launches=16, max_pack=128, threads=256, ppt=2, tick_us=200.0)
+    out = {"workload": "mixed stream: objective U{Rosenbrock, Rastrigin, Ackley, Lotka-Volterra fit}, dim U{2..64}, "
+                       "particles U{256..16384}, maxiters U{100..2000}", "server": dict(cfg)}
+    # closed loop: all requests submitted at once, throughput at saturation
+    reqs = _request_pool(pps, args.serve_requests, 1)
+    with pps.Server(**cfg) as srv:
+        t0 = time.perf_counter()
+        ts = [srv.submit(p, n, maxiters=it, seed=s) for (p, n, it, s) in reqs]
+        res = [srv.wait(t) for t in ts]
+        wall = time.perf_counter() - t0
+        st = srv.stats()
+    out["closed_loop"] = {"requests": len(reqs), "wall_s": wall, "solves_per_s": len(reqs) / wall,
+                          "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "launches": st["launches"],
+                          "mean_pack": st["mean_pack"], "arena_peak_bytes": st["arena_peak_bytes"]}
+    # plain: the same kind of requests one at a time through solve()
+    sample = reqs[:60]
+    t0 = time.perf_counter()
+    same = True
+    for k, (p, n, it, s) in enumerate(sample):
+        sol = pps.solve(p, pps.ParallelSyncPSOKernel(n), maxiters=it, seed=s)
+        same &= bool(np.array_equal(sol.u, res[k][0]))
+    plain = len(sample) / (time.perf_counter() - t0)
+    out["plain_solves_per_s"] = plain
+    out["plain_sample"] = len(sample)
+    out["speedup_vs_plain"] = out["closed_loop"]["solves_per_s"] / plain
+    out["same_result_alone_and_served"] = same
+    # open loop: Poisson arrivals at 2000/s for serve_seconds, then drain
+    rate = 2000.0
+    rng = np.random.default_rng(2)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, int(rate * args.serve_seconds * 1.2)))
+    arrivals = arrivals[arrivals < args.serve_seconds]
+    pool = _request_pool(pps, len(arrivals), 3)
+    with pps.Server(**cfg) as srv:
+        t0 = time.perf_counter()
+        tickets = []
+        for k, at in enumerate(arrivals):
+            while time.perf_counter() - t0 < at:
+                time.sleep(0.0001)
+            p, n, it, s = pool[k]
+            tickets.append(srv.submit(p, n, maxiters=it, seed=s))
+        submit_s = time.perf_counter() - t0
+        for t in tickets:
+            srv.wait(t)
+        wall = time.perf_counter() - t0
+        st = srv.stats()
+    out["open_loop"] = {"offered_per_s": rate, "arrival_window_s": args.serve_seconds, "requests": len(tickets),
+                        "submit_s": submit_s, "drain_wall_s": wall, "solves_per_s": len(tickets) / wall,
+                        "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "max_ms": st["max_ms"],
+                        "launches": st["launches"], "mean_pack": st["mean_pack"],
+                        "arena_peak_bytes": st["arena_peak_bytes"],
+                        "note": "offered load above the measured closed-loop capacity: latency includes queueing"}
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -190,7 +357,13 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-async", action="store_true")
+    ap.add_argument("--no-extras", action="store_true", help="skip the hybrid, ODE-batch and served measurements")
+    ap.add_argument("--only", choices=["sync", "async", "hybrid", "ode", "serve"], default=None,
+                    help="run one workload only (for profiling); prints its result")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU-baseline sample")
+    ap.add_argument("--serve-requests", type=int, default=1500, help="requests of the closed-loop served run")
+    ap.add_argument("--serve-seconds", type=float, default=1.0, help="arrival window of the open-loop served run")
+    ap.add_argument("--ode-fits", type=int, default=512, help="fits of each model in the batched ODE run")
     args = ap.parse_args()
     rank, world, local = dist_env()
 
@@ -213,6 +386,20 @@ def main():
     prob = make_problem(pps)
     iters = args.iters
     seed0 = 1000 * rank
+
+    if args.only in ("hybrid", "ode", "serve"):
+        fn = {"hybrid": lambda: run_hybrid(pps), "ode": lambda: run_ode_batch(pps, args.ode_fits),
+              "serve": lambda: run_served(pps, args)}[args.only]
+        if rank == 0:
+            print(json.dumps({args.only: fn()}), flush=True)
+        return 0
+    if args.only == "async":
+        sa = pps.Swarm(prob, N_PARTICLES, seed=seed0 + 1)
+        sa.init()
+        ams = sa.async_run(iters)
+        if rank == 0:
+            print(json.dumps({"async": {"ms": ams, "particle_iters_per_s": N_PARTICLES * iters / (ams / 1e3)}}))
+        return 0
 
     def barrier():
         if dist:
@@ -249,7 +436,7 @@ def main():
 
     # ---- async at the same size -----------------------------------------
     async_rate = None
-    if rank == 0 and not args.no_async:
+    if rank == 0 and not args.no_async and args.only is None:
         sa = pps.Swarm(prob, N_PARTICLES, seed=seed0 + 1)
         sa.init()
         sa.async_run(50)
@@ -260,7 +447,7 @@ def main():
 
     # ---- end to end through solve() with host buffers --------------------
     e2e = None
-    if not args.no_e2e:
+    if not args.no_e2e and args.only is None:
         alg = pps.ParallelSyncPSOKernel(N_PARTICLES)
         pps.solve(prob, alg, maxiters=iters, seed=seed0)  # warm
         barrier()
@@ -279,8 +466,14 @@ def main():
                        "get_gbest/get_state/eval_objective)"}
 
     # ---- CPU baseline (oracle on the host cores) --------------------------
+    extras = {}
+    if rank == 0 and not args.no_extras and args.only is None:
+        extras["hybrid"] = run_hybrid(pps)
+        extras["ode_batch"] = run_ode_batch(pps, args.ode_fits)
+        extras["served"] = run_served(pps, args)
+
     cpu = None
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+    if rank == 0 and world == 1 and not args.no_cpu_baseline and args.only is None:
         threads = os.cpu_count() or 1
         n_s = 1 << 18
         rate0, _ = cpu_oracle_rate(n_s, 1, threads)  # size the sample to about --cpu-seconds
@@ -312,6 +505,7 @@ def main():
                       "workload": "ParallelPSOKernel(global_update=false), same size, one launch"},
             "final_gbest_cost": gcost,
         }
+        line.update(extras)
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
