@@ -83,6 +83,7 @@ struct pps_swarm {
   int graph_async_lanes = 0;  // run flags the graph was captured with
   float graph_c1 = 0.0f, graph_c2 = 0.0f;
   int sm_count = 0;
+  int sync_passes = 1;  // tiles per block of the step kernel (set by sync_grid)
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   void* local_block = nullptr;  // HybridPSO local-stage results (allocated on first use)
   int local_valid = 0;

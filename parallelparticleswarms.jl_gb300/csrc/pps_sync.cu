@@ -79,11 +79,13 @@ __global__ void __launch_bounds__(kSyncThreads) k_init(SwarmDev s, ObjParams op,
 // and walks the dims in pairs: one Philox call per particle and pair yields
 // r1, r2 for both dims.  The loads of the next pair are issued before the
 // current pair is computed (software prefetch), so every warp keeps six
-// vector loads in flight while it runs Philox and the objective.  A block
-// owns a contiguous, 32-particle-aligned range of the swarm.
+// vector loads in flight while it runs Philox and the objective.  The swarm
+// is cut into tiles of blockDim x PPT particles and every block takes the same
+// number of consecutive tiles (`passes`), so no thread of any block idles at
+// the final barrier while others finish a last partial pass.
 template <int OBJ, int PPT>
 __global__ void __launch_bounds__(kSyncThreads, (PPT == 4 ? 2 : (PPT == 2 ? 3 : 4)))
-    k_sync_step(SwarmDev s, ObjParams op, uint64_t seed, float c1, float c2, int from_position) {
+    k_sync_step(SwarmDev s, ObjParams op, uint64_t seed, float c1, float c2, int from_position, int passes) {
   extern __shared__ float sm[];
   const int D = s.dim;
   float* sg = sm;
@@ -100,10 +102,10 @@ __global__ void __launch_bounds__(kSyncThreads, (PPT == 4 ? 2 : (PPT == 2 ? 3 : 
   __syncthreads();
   const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
   const int64_t npad = s.npad;
-  const int64_t nchunk = npad >> 5;  // 32-particle chunks
-  const int64_t cb = (int64_t)blockIdx.x * nchunk / gridDim.x;
-  const int64_t ce = (int64_t)(blockIdx.x + 1) * nchunk / gridDim.x;
-  const int64_t gb = cb * (32 / PPT), ge = ce * (32 / PPT);  // groups of PPT particles
+  const int64_t ngroups = npad / PPT;  // groups of PPT particles
+  const int64_t gb = (int64_t)blockIdx.x * passes * blockDim.x;
+  int64_t ge = gb + (int64_t)passes * blockDim.x;
+  ge = ge < ngroups ? ge : ngroups;
   float* __restrict__ X = s.X;
   float* __restrict__ V = s.V;
   float* __restrict__ P = s.P;
@@ -315,25 +317,31 @@ int sync_grid(pps_swarm* s) {
     cached_dev = s->device;
     cached_dim = s->dv.dim;
   }
-  int64_t grid = (int64_t)per_sm * s->sm_count;
-  const int64_t chunks = s->dv.npad / 32;
-  if (grid > chunks) grid = chunks;
+  // tiles of kSyncThreads x PPT particles, the same number per block
+  const int64_t resident = (int64_t)per_sm * s->sm_count;
+  const int64_t tile = (int64_t)kSyncThreads * sync_ppt();
+  const int64_t ntiles = (s->dv.npad + tile - 1) / tile;
+  int64_t passes = (ntiles + resident - 1) / resident;
+  if (passes < 1) passes = 1;
+  int64_t grid = (ntiles + passes - 1) / passes;
   if (grid < 1) grid = 1;
+  s->sync_passes = (int)passes;
   return (int)grid;
 }
 
 int launch_sync_step(pps_swarm* s, float c1, float c2) {
   const int grid = sync_grid(s);
+  const int passes = s->sync_passes;
   const size_t smem = 3 * sizeof(float) * (size_t)s->dv.dim;
   const int from_pos = (s->flags & PPS_FLAG_GBEST_FROM_POSITION) ? 1 : 0;
   const int ppt = sync_ppt();
 #define L_STEP(O)                                                                                       \
   if (ppt == 4)                                                                                         \
-    k_sync_step<O, 4><<<grid, kSyncThreads, smem, s->stream>>>(s->dv, s->op, s->seed, c1, c2, from_pos); \
+    k_sync_step<O, 4><<<grid, kSyncThreads, smem, s->stream>>>(s->dv, s->op, s->seed, c1, c2, from_pos, passes); \
   else if (ppt == 2)                                                                                    \
-    k_sync_step<O, 2><<<grid, kSyncThreads, smem, s->stream>>>(s->dv, s->op, s->seed, c1, c2, from_pos); \
+    k_sync_step<O, 2><<<grid, kSyncThreads, smem, s->stream>>>(s->dv, s->op, s->seed, c1, c2, from_pos, passes); \
   else                                                                                                  \
-    k_sync_step<O, 1><<<grid, kSyncThreads, smem, s->stream>>>(s->dv, s->op, s->seed, c1, c2, from_pos)
+    k_sync_step<O, 1><<<grid, kSyncThreads, smem, s->stream>>>(s->dv, s->op, s->seed, c1, c2, from_pos, passes)
   PPS_DISPATCH_SEPARABLE(s->objective, L_STEP)
 #undef L_STEP
   PPS_CUDA(cudaGetLastError());
