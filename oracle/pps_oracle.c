@@ -297,6 +297,12 @@ float orc_objective(const orc_problem* prob, const float* x, int64_t stride, int
     for (int d = 0; d < D && d < 8; ++d) p[d] = x[d * stride];
     return orc_ode_loss(prob->ode, p);
   }
+  if (prob->objective == ORC_OBJ_MLP) {
+    float p[577];
+    for (int d = 0; d < 577; ++d) p[d] = x[d * stride];
+    const int S = prob->mlp_samples;
+    return (float)orc_mlp_loss(p, prob->mlp_data, prob->mlp_data + (int64_t)S * 16, S);
+  }
   if (lanes <= 1) {
     float s1, s2;
     slice_sums(prob, x, stride, 0, D, &s1, &s2);

@@ -58,6 +58,7 @@ enum {
   ORC_OBJ_ACKLEY = 3,
   ORC_OBJ_LV_FIT = 4,   /* SSE of an RK4 Lotka-Volterra solve vs data */
   ORC_OBJ_FHN_FIT = 5,  /* SSE of an RK4 FitzHugh-Nagumo solve vs data */
+  ORC_OBJ_MLP = 6,      /* MLP regression loss (16 -> 32 tanh -> 1, MSE) */
   /* closed-form objectives of the reference's L-BFGS tests (test/lbfgs.jl:20-26) */
   ORC_OBJ_BEALE = 16,
   ORC_OBJ_BOOTH = 17,
@@ -78,6 +79,8 @@ typedef struct orc_problem {
   float params[8];      /* objective parameters */
   int32_t nparams;
   const struct orc_ode_fit* ode;  /* ORC_OBJ_LV_FIT / ORC_OBJ_FHN_FIT only */
+  const float* mlp_data;          /* ORC_OBJ_MLP: S x 16 samples then S targets */
+  int32_t mlp_samples;
 } orc_problem;
 
 /* structure-of-arrays swarm state: x[d*n + i] */
@@ -171,6 +174,16 @@ void orc_reduce_losses(int32_t m, int32_t ncomp, int64_t n, const float* data,
  * (orc_problem.ode points at the fit): orc_init + orc_sync_run give the
  * parameter_estim_ode! loop of src/ode_pso.jl:113-170 with an elementwise
  * clamp and RK4 in place of GPUTsit5. */
+
+/* ---- MLP regression objective (tensor-core path) ----
+ * particle x (577 floats): W1[i][j] at i*32 + j (16 inputs x 32 hidden),
+ * b1 at 512.., w2 at 544.., b2 at 576.  Loss = mean_s (w2 . tanh(W1^T X_s + b1)
+ * + b2 - y_s)^2 with X_s and W1 rounded to bfloat16 (the GEMM operands) and
+ * everything else in double: the reference value the kernel's BF16 GEMM with
+ * FP32 accumulation and approximate tanh is compared against within a
+ * tolerance. */
+double orc_mlp_loss(const float* x, const float* X, const float* y, int32_t samples);
+float orc_bf16_round(float v);
 
 #ifdef __cplusplus
 }

@@ -35,7 +35,7 @@ class OdeFit(ctypes.Structure):
 class Problem(ctypes.Structure):
     _fields_ = [("objective", ctypes.c_int32), ("dim", ctypes.c_int32), ("lb", _fp), ("ub", _fp),
                 ("u0", _fp), ("params", ctypes.c_float * 8), ("nparams", ctypes.c_int32),
-                ("ode", ctypes.POINTER(OdeFit))]
+                ("ode", ctypes.POINTER(OdeFit)), ("mlp_data", _fp), ("mlp_samples", ctypes.c_int32)]
 
 
 class SwarmC(ctypes.Structure):
@@ -93,6 +93,10 @@ def load() -> ctypes.CDLL:
         L.orc_ode_loss.argtypes = [ctypes.POINTER(OdeFit), _fp]
         L.orc_ode_solve.argtypes = [ctypes.POINTER(OdeFit), _fp, _fp]
         L.orc_reduce_losses.argtypes = [ctypes.c_int32, ctypes.c_int32, ctypes.c_int64, _fp, _fp, _fp]
+        L.orc_mlp_loss.restype = ctypes.c_double
+        L.orc_mlp_loss.argtypes = [_fp, _fp, _fp, ctypes.c_int32]
+        L.orc_bf16_round.restype = ctypes.c_float
+        L.orc_bf16_round.argtypes = [ctypes.c_float]
         _lib = L
     return _lib
 
@@ -126,7 +130,7 @@ def default_threads() -> int:
 class OracleProblem:
     """orc_problem over numpy buffers (objective ids are include/pps.h's)."""
 
-    def __init__(self, objective: int, dim: int, lb=None, ub=None, u0=None, params=(), ode=None):
+    def __init__(self, objective: int, dim: int, lb=None, ub=None, u0=None, params=(), ode=None, mlp_data=None):
         self.dim = int(dim)
         self.lb = np.ascontiguousarray(np.full(dim, -np.inf, np.float32) if lb is None else np.asarray(lb, np.float32))
         self.ub = np.ascontiguousarray(np.full(dim, np.inf, np.float32) if ub is None else np.asarray(ub, np.float32))
@@ -142,6 +146,11 @@ class OracleProblem:
         self.ode = ode
         if ode is not None:
             self.c.ode = ctypes.pointer(ode.c)
+        self.mlp_data = None
+        if mlp_data is not None:  # S x 16 samples followed by S targets
+            self.mlp_data = np.ascontiguousarray(np.asarray(mlp_data, np.float32).reshape(-1))
+            self.c.mlp_data = fp(self.mlp_data)
+            self.c.mlp_samples = self.mlp_data.size // 17
 
     def objective(self, x, lanes: int = 1) -> float:
         x = np.ascontiguousarray(np.asarray(x, np.float32))
@@ -256,3 +265,11 @@ def reduce_losses(data, us) -> np.ndarray:
     out = np.empty(n, np.float32)
     load().orc_reduce_losses(m, k, n, fp(data), fp(us), fp(out))
     return out
+
+
+def mlp_loss(x, X, y) -> float:
+    """MLP regression loss of particle x (577) on samples X (S, 16), y (S,)."""
+    x = np.ascontiguousarray(np.asarray(x, np.float32))
+    X = np.ascontiguousarray(np.asarray(X, np.float32))
+    y = np.ascontiguousarray(np.asarray(y, np.float32))
+    return float(load().orc_mlp_loss(fp(x), fp(X), fp(y), int(y.size)))

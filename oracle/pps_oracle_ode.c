@@ -21,6 +21,7 @@
  *     dv  = (fma(v*v*v, -1/3, v) - w) + l  dw  = tinv * fma(-b, w, v + a)
  */
 #include <math.h>
+#include <string.h>
 
 #include "pps_oracle.h"
 
@@ -103,4 +104,32 @@ void orc_reduce_losses(int32_t m, int32_t ncomp, int64_t n, const float* data, c
     }
     losses[i] = acc;
   }
+}
+
+/* ---- MLP objective ---- */
+float orc_bf16_round(float v) {
+  uint32_t b;
+  memcpy(&b, &v, 4);
+  if ((b & 0x7f800000u) == 0x7f800000u) return v;  /* inf / nan */
+  const uint32_t lsb = (b >> 16) & 1u;
+  b += 0x7fffu + lsb; /* round to nearest even */
+  b &= 0xffff0000u;
+  float r;
+  memcpy(&r, &b, 4);
+  return r;
+}
+
+double orc_mlp_loss(const float* x, const float* X, const float* y, int32_t samples) {
+  double acc = 0.0;
+  for (int s = 0; s < samples; ++s) {
+    double o = x[576];
+    for (int j = 0; j < 32; ++j) {
+      double h = x[512 + j];
+      for (int i = 0; i < 16; ++i) h += (double)orc_bf16_round(X[s * 16 + i]) * (double)orc_bf16_round(x[i * 32 + j]);
+      o += (double)x[544 + j] * tanh(h);
+    }
+    const double e = o - (double)y[s];
+    acc += e * e;
+  }
+  return acc / samples;
 }

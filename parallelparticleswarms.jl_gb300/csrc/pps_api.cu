@@ -12,6 +12,7 @@
 #include <cstring>
 #include <limits>
 #include <new>
+#include <vector>
 
 #include "pps_internal.h"
 
@@ -47,6 +48,7 @@ static bool supported_objective(int obj) {
     case kBoundaryQuadratic:
     case kLvFit:
     case kFhnFit:
+    case kMlp:
       return true;
     default:
       return false;
@@ -66,6 +68,10 @@ static int check_problem(const pps_problem* prob) {
     return set_error(PPS_EINVAL, "objective %d is defined for dim <= 2", prob->objective);
   if (is_ode(prob->objective)) {
     const int rc = ode_check(prob);
+    if (rc) return rc;
+  }
+  if (prob->objective == kMlp) {
+    const int rc = mlp_check(prob);
     if (rc) return rc;
   }
   for (int d = 0; d < prob->dim; ++d) {
@@ -146,6 +152,8 @@ int pps_swarm_create(const pps_problem* prob, int64_t n, uint64_t seed, uint32_t
   const size_t oU0 = take(sizeof(float) * D);
   const size_t oSt = take(sizeof(IterState));
   const size_t oData = take(sizeof(float) * (prob->data ? (size_t)prob->ndata : 0));
+  const int mlp_samples = prob->objective == kMlp ? (int)(prob->ndata / 17) : 0;
+  const size_t oMlpA = take(mlp_samples ? mlp_a_bytes(mlp_samples) : 0);
   s->bytes = off;
   cudaError_t e = cudaMalloc(&s->block, s->bytes);
   if (e != cudaSuccess) {
@@ -167,6 +175,7 @@ int pps_swarm_create(const pps_problem* prob, int64_t n, uint64_t seed, uint32_t
   s->data_dev = reinterpret_cast<float*>(b + oData);
   s->od.data = s->data_dev;
   s->od.ndata = prob->data ? prob->ndata : 0;
+  if (mlp_samples) s->mlp_a_dev = b + oMlpA;
   s->dv.n = n;
   s->dv.npad = npad;
   s->dv.dim = D;
@@ -208,6 +217,14 @@ int pps_swarm_create(const pps_problem* prob, int64_t n, uint64_t seed, uint32_t
       rc = cuda_error(e, "cudaMemcpy(data)");
       break;
     }
+    if (mlp_samples) {
+      std::vector<uint8_t> packed(mlp_a_bytes(mlp_samples));
+      mlp_pack_a(prob->data, mlp_samples, packed.data());
+      if ((e = cudaMemcpy(s->mlp_a_dev, packed.data(), packed.size(), cudaMemcpyHostToDevice)) != cudaSuccess) {
+        rc = cuda_error(e, "cudaMemcpy(MLP samples)");
+        break;
+      }
+    }
     if ((e = cudaStreamSynchronize(s->stream)) != cudaSuccess) { rc = cuda_error(e, "cudaStreamSynchronize"); break; }
   } while (0);
   if (rc) {
@@ -233,6 +250,15 @@ int pps_swarm_destroy(pps_swarm* s) {
   free(s->host_lb);
   if (dev >= 0 && dev != s->device) cudaSetDevice(dev);
   delete s;
+  return PPS_OK;
+}
+
+// bit 1 of IterState::status: a bounded wait of the tensor-core kernel gave up
+static int check_device_status(pps_swarm* s) {
+  if (s->objective != kMlp) return PPS_OK;
+  unsigned int status = 0;
+  PPS_CUDA(cudaMemcpy(&status, &s->dv.st->status, sizeof(status), cudaMemcpyDeviceToHost));
+  if (status & 2u) return set_error(PPS_ETIMEOUT, "the MLP tensor-core kernel timed out waiting for an MMA");
   return PPS_OK;
 }
 
@@ -264,7 +290,9 @@ int pps_swarm_init(pps_swarm* s, int32_t sampler) {
   if ((rc = launch_set_iter(s, 0u, 0.7298f, 1.0f))) return rc;
   if ((rc = is_ode(s->objective) ? launch_init_ode(s, sampler, s->u0_dev) : launch_init(s, sampler, s->u0_dev)))
     return rc;
+  if (s->objective == kMlp && (rc = launch_mlp_init_eval(s))) return rc;
   PPS_CUDA(cudaStreamSynchronize(s->stream));
+  if ((rc = check_device_status(s))) return rc;
   s->t = 0;
   s->initialized = 1;
   s->local_valid = 0;
@@ -310,7 +338,10 @@ static int finish_timing(pps_swarm* s, float* device_ms) {
 static constexpr int kGraphChunk = 32;
 
 static int step_once(pps_swarm* s, float c1, float c2) {
-  return is_ode(s->objective) ? launch_sync_step_ode(s, c1, c2) : launch_sync_step(s, c1, c2);
+  if (is_ode(s->objective)) return launch_sync_step_ode(s, c1, c2);
+  const int rc = launch_sync_step(s, c1, c2);
+  if (rc || s->objective != kMlp) return rc;
+  return launch_mlp_step_eval(s);
 }
 
 static int run_steps(pps_swarm* s, int32_t maxiters, float c1, float c2, uint32_t run_flags) {
@@ -378,7 +409,7 @@ static int sync_like_run(pps_swarm* s, int32_t maxiters, float w, float wdamp, f
   if ((rc = finish_timing(s, device_ms))) return rc;
   PPS_CUDA(cudaStreamSynchronize(s->stream));
   s->t += (uint32_t)maxiters;
-  return PPS_OK;
+  return check_device_status(s);
 }
 
 int pps_sync_run(pps_swarm* s, int32_t maxiters, float w, float wdamp, float c1, float c2,
@@ -399,6 +430,8 @@ int pps_async_run(pps_swarm* s, int32_t maxiters, float w, float wdamp, float c1
   if (rc) return rc;
   if (is_ode(s->objective))
     return set_error(PPS_ENOTSUP, "ODE fits run synchronously (parameter_estim_ode!); use pps_sync_run");
+  if (s->objective == kMlp)
+    return set_error(PPS_ENOTSUP, "the MLP objective runs synchronously (tensor-core evaluation); use pps_sync_run");
   if ((rc = launch_set_iter(s, s->t, w, wdamp))) return rc;
   PPS_CUDA(cudaEventRecord(s->ev0, s->stream));
   int lanes = 0;
@@ -495,15 +528,45 @@ int pps_eval_objective(const pps_problem* prob, int64_t npoints, const float* x,
     od.data = ddata;
     od.ndata = prob->ndata;
   }
+  uint8_t* da = nullptr;  // MLP: packed samples followed by the status word
+  std::vector<uint8_t> packed;
+  if (!rc && prob->objective == kMlp) {
+    const int S = (int)(prob->ndata / 17);
+    packed.resize(mlp_a_bytes(S));
+    mlp_pack_a(prob->data, S, packed.data());
+    if ((e = cudaMallocAsync(&ddata, sizeof(float) * (size_t)prob->ndata, st)) != cudaSuccess ||
+        (e = cudaMallocAsync(&da, packed.size() + 256, st)) != cudaSuccess)
+      rc = cuda_error(e, "cudaMallocAsync");
+    if (!rc && ((e = cudaMemcpyAsync(ddata, prob->data, sizeof(float) * (size_t)prob->ndata, cudaMemcpyHostToDevice,
+                                     st)) != cudaSuccess ||
+                (e = cudaMemcpyAsync(da, packed.data(), packed.size(), cudaMemcpyHostToDevice, st)) != cudaSuccess ||
+                (e = cudaMemsetAsync(da + packed.size(), 0, 256, st)) != cudaSuccess))
+      rc = cuda_error(e, "cudaMemcpy");
+    od.data = ddata;
+    od.ndata = prob->ndata;
+  }
   if (!rc && (e = cudaMemcpyAsync(dx, x, bx, cudaMemcpyHostToDevice, st)) != cudaSuccess) rc = cuda_error(e, "cudaMemcpy");
-  if (!rc) rc = is_ode(prob->objective) ? launch_eval_ode(op, od, prob->objective, dx, npoints, npoints, df, st)
-                                        : launch_eval(op, od, prob->objective, dx, npoints, npoints, df, st);
+  unsigned int status = 0;
+  if (!rc) {
+    if (prob->objective == kMlp) {
+      unsigned int* dstatus = reinterpret_cast<unsigned int*>(da + packed.size());
+      rc = launch_mlp_points(ddata, prob->ndata, da, dx, npoints, npoints, df, dstatus, st);
+      if (!rc && (e = cudaMemcpyAsync(&status, dstatus, sizeof(status), cudaMemcpyDeviceToHost, st)) != cudaSuccess)
+        rc = cuda_error(e, "cudaMemcpy");
+    } else if (is_ode(prob->objective)) {
+      rc = launch_eval_ode(op, od, prob->objective, dx, npoints, npoints, df, st);
+    } else {
+      rc = launch_eval(op, od, prob->objective, dx, npoints, npoints, df, st);
+    }
+  }
   if (!rc && (e = cudaMemcpyAsync(f, df, sizeof(float) * npoints, cudaMemcpyDeviceToHost, st)) != cudaSuccess)
     rc = cuda_error(e, "cudaMemcpy");
   cudaFreeAsync(dx, st);
   if (ddata) cudaFreeAsync(ddata, st);
+  if (da) cudaFreeAsync(da, st);
   if ((e = cudaStreamSynchronize(st)) != cudaSuccess && !rc) rc = cuda_error(e, "cudaStreamSynchronize");
   cudaStreamDestroy(st);
+  if (!rc && (status & 2u)) rc = set_error(PPS_ETIMEOUT, "the MLP tensor-core kernel timed out waiting for an MMA");
   return rc;
 }
 

@@ -193,6 +193,8 @@ struct Acc {
     } else if constexpr (OBJ == kAckley) {
       s1 = __fadd_rn(s1, __fmul_rn(x, x));
       s2 = __fadd_rn(s2, cos2pi(__fmul_rn(prm(o, 2, 1.0f), x)));
+    } else if constexpr (OBJ == kMlp) {
+      // evaluated by the tensor-core kernel after the position update
     } else {
       // closed-form low-dimensional objectives keep x1, x2
       if (d == 0) s1 = x;

@@ -87,6 +87,7 @@ struct pps_swarm {
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   void* local_block = nullptr;  // HybridPSO local-stage results (allocated on first use)
   int local_valid = 0;
+  void* mlp_a_dev = nullptr;  // MLP objective: the samples as bf16 tensor-core tiles
 };
 
 namespace pps {
@@ -118,5 +119,15 @@ int launch_sync_step_ode(pps_swarm* s, float c1, float c2);
 int launch_eval_ode(const ObjParams& op, const ObjData& od, int objective, const float* x, int64_t npts,
                     int64_t stride, float* f, cudaStream_t stream);
 inline bool is_ode(int objective) { return objective == kLvFit || objective == kFhnFit; }
+// MLP-regression objective on the tensor cores (pps_mlp.cu); the step kernel
+// moves the particles and k_mlp_eval evaluates, updates personal bests and
+// publishes the argmin
+int mlp_check(const pps_problem* prob);
+size_t mlp_a_bytes(int samples);
+void mlp_pack_a(const float* X, int samples, uint8_t* out);
+int launch_mlp_init_eval(pps_swarm* s);
+int launch_mlp_step_eval(pps_swarm* s);
+int launch_mlp_points(const float* data_dev, int64_t ndata, const uint8_t* a_dev, const float* x, int64_t npts,
+                      int64_t stride, float* f, unsigned int* status, cudaStream_t stream);
 
 }  // namespace pps

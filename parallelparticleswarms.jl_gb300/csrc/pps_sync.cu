@@ -64,13 +64,18 @@ __global__ void __launch_bounds__(kSyncThreads) k_init(SwarmDev s, ObjParams op,
         acc.add(op, d, x);
       }
     }
-    const float c = valid ? finalize<OBJ>(op, acc.s1, acc.s2) : __int_as_float(0x7f800000);
-    s.cost[i] = c;
-    s.pcost[i] = c;
-    s.flag[i] = 0;
-    if (valid) key = argmin_key(c, (uint32_t)i);
+    if constexpr (OBJ != kMlp) {
+      const float c = valid ? finalize<OBJ>(op, acc.s1, acc.s2) : __int_as_float(0x7f800000);
+      s.cost[i] = c;
+      s.pcost[i] = c;
+      s.flag[i] = 0;
+      if (valid) key = argmin_key(c, (uint32_t)i);
+    }
   }
-  if (publish_block_min(key, s.st)) finish_iteration(s, false, 0u, s.st->w);
+  // the MLP objective is evaluated (and published) by the tensor-core kernel
+  if constexpr (OBJ != kMlp) {
+    if (publish_block_min(key, s.st)) finish_iteration(s, false, 0u, s.st->w);
+  }
 }
 
 // ------------------------------------------------------------------ step
@@ -187,26 +192,32 @@ __global__ void __launch_bounds__(kSyncThreads, (PPT == 4 ? 2 : (PPT == 2 ? 3 : 
         xb[k] = nxb[k]; vb[k] = nvb[k]; pb[k] = npb[k];
       }
     }
-    float pc[PPT], cc[PPT];
-    ldv<PPT>(pc, s.pcost + i0);
+    if constexpr (OBJ != kMlp) {
+      float pc[PPT], cc[PPT];
+      ldv<PPT>(pc, s.pcost + i0);
 #pragma unroll
-    for (int k = 0; k < PPT; ++k) {
-      cc[k] = finalize<OBJ>(op, acc[k].s1, acc[k].s2);
-      const bool valid = i0 + k < n;
-      // if cost < best_cost: best = position (strict <, src/kernels.jl:21-24)
-      fl[k] = (valid && cc[k] < pc[k]) ? 1 : 0;
-      pc[k] = fl[k] ? cc[k] : pc[k];
-      if (valid) {
-        const unsigned long long key = argmin_key(pc[k], (uint32_t)(i0 + k));
-        best = key < best ? key : best;
+      for (int k = 0; k < PPT; ++k) {
+        cc[k] = finalize<OBJ>(op, acc[k].s1, acc[k].s2);
+        const bool valid = i0 + k < n;
+        // if cost < best_cost: best = position (strict <, src/kernels.jl:21-24)
+        fl[k] = (valid && cc[k] < pc[k]) ? 1 : 0;
+        pc[k] = fl[k] ? cc[k] : pc[k];
+        if (valid) {
+          const unsigned long long key = argmin_key(pc[k], (uint32_t)(i0 + k));
+          best = key < best ? key : best;
+        }
       }
+      stv<PPT>(s.pcost + i0, pc);
+      stv<PPT>(s.cost + i0, cc);
+      stflags<PPT>(s.flag + i0, fl);
     }
-    stv<PPT>(s.pcost + i0, pc);
-    stv<PPT>(s.cost + i0, cc);
-    stflags<PPT>(s.flag + i0, fl);
   }
-  if (publish_block_min(best, st)) {
-    finish_iteration(s, from_position != 0, t + 1u, __fmul_rn(w, st->wdamp));
+  // MLP: position update only; k_mlp_eval evaluates, updates the personal
+  // bests and flags, publishes the argmin and advances (t, w)
+  if constexpr (OBJ != kMlp) {
+    if (publish_block_min(best, st)) {
+      finish_iteration(s, from_position != 0, t + 1u, __fmul_rn(w, st->wdamp));
+    }
   }
 }
 
@@ -259,7 +270,11 @@ __global__ void k_eval(ObjParams op, const float* __restrict__ x, int64_t npts, 
 int launch_init(pps_swarm* s, int sampler, const float* u0_dev) {
   const int64_t blocks = (s->dv.npad + kSyncThreads - 1) / kSyncThreads;
 #define L_INIT(O) k_init<O><<<(unsigned)blocks, kSyncThreads, 0, s->stream>>>(s->dv, s->op, s->seed, sampler, u0_dev)
-  PPS_DISPATCH_SEPARABLE(s->objective, L_INIT)
+  if (s->objective == kMlp) {
+    L_INIT(kMlp);
+  } else {
+    PPS_DISPATCH_SEPARABLE(s->objective, L_INIT)
+  }
 #undef L_INIT
   PPS_CUDA(cudaGetLastError());
   return PPS_OK;
@@ -309,6 +324,7 @@ int sync_grid(pps_swarm* s) {
       case kRosenbrock: per_sm = occupancy_of<kRosenbrock>(ppt, smem); break;
       case kRastrigin: per_sm = occupancy_of<kRastrigin>(ppt, smem); break;
       case kAckley: per_sm = occupancy_of<kAckley>(ppt, smem); break;
+      case kMlp: per_sm = occupancy_of<kMlp>(ppt, smem); break;
       default: per_sm = occupancy_of<kBeale>(ppt, smem); break;
     }
     if (per_sm < 1) per_sm = 1;
@@ -342,7 +358,11 @@ int launch_sync_step(pps_swarm* s, float c1, float c2) {
     k_sync_step<O, 2><<<grid, kSyncThreads, smem, s->stream>>>(s->dv, s->op, s->seed, c1, c2, from_pos, passes); \
   else                                                                                                  \
     k_sync_step<O, 1><<<grid, kSyncThreads, smem, s->stream>>>(s->dv, s->op, s->seed, c1, c2, from_pos, passes)
-  PPS_DISPATCH_SEPARABLE(s->objective, L_STEP)
+  if (s->objective == kMlp) {
+    L_STEP(kMlp);
+  } else {
+    PPS_DISPATCH_SEPARABLE(s->objective, L_STEP)
+  }
 #undef L_STEP
   PPS_CUDA(cudaGetLastError());
   return PPS_OK;

@@ -14,7 +14,7 @@ from .solve import (HybridPSOCache, OptimizationSolution, OptimizationStats, PSO
 from .swarm import Swarm
 from .batch import Batch
 from .serve import Server
-from . import ode
+from . import mlp, ode
 
 __all__ = [
     "ParallelPSOKernel", "ParallelSyncPSOKernel", "PSOAlgorithm", "HybridPSO", "SimpleLBFGS", "BFGS",
@@ -22,5 +22,5 @@ __all__ = [
     "PSOCache", "HybridPSOCache", "OptimizationSolution", "OptimizationStats", "Swarm", "PPSError",
     "ArgumentError", "evaluate", "Objective", "REGISTRY", "sphere", "rosenbrock", "rastrigin", "ackley",
     "lotka_volterra_fit", "fitzhugh_nagumo_fit", "mlp_regression", "beale", "booth", "himmelblau",
-    "quadratic", "boundary_quadratic", "CUDA", "Batch", "Server", "ode",
+    "quadratic", "boundary_quadratic", "CUDA", "Batch", "Server", "ode", "mlp",
 ]

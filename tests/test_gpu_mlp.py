@@ -1,0 +1,117 @@
+"""The MLP-regression objective on the tensor cores vs the oracle.
+
+The kernel computes the hidden layer as a bf16 x bf16 -> fp32 tcgen05 GEMM
+and tanh with tanh.approx.f32; the oracle rounds the GEMM operands to bf16 the
+same way and does everything else in float64.  Tolerance on a loss:
+|gpu - oracle| <= 3e-3 * |oracle| + 1e-4 (tanh.approx's error, summed over 32
+hidden units).  The position and velocity updates do not depend on the
+objective's arithmetic and stay bit-exact, checked step by step from the
+GPU's own state."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+RTOL, ATOL = 3e-3, 1e-4
+
+
+def _close(got, want):
+    got = np.asarray(got, np.float64)
+    want = np.asarray(want, np.float64)
+    return np.abs(got - want) <= RTOL * np.abs(want) + ATOL
+
+
+def _task(pps, samples, seed):
+    data, teacher = pps.mlp.teacher_task(samples, seed=seed)
+    X = data[:samples * 16].reshape(samples, 16)
+    y = data[samples * 16:]
+    return data, teacher, X, y
+
+
+@pytest.mark.parametrize("samples,npts", [(128, 1), (1024, 37), (4096, 9), (256, 1000)])
+def test_eval_matches_oracle(pps, orc, samples, npts):
+    data, teacher, X, y = _task(pps, samples, 3)
+    prob = pps.mlp.mlp_problem(data)
+    rng = np.random.default_rng(samples + npts)
+    pts = rng.uniform(-1, 1, (npts, 577)).astype(np.float32)
+    pts[0] = teacher
+    got = np.atleast_1d(pps.evaluate(prob, pts))
+    want = np.array([orc.mlp_loss(p, X, y) for p in pts])
+    bad = ~_close(got, want)
+    assert not bad.any(), f"{bad.sum()} of {npts} losses out of tolerance, e.g. {got[bad][:3]} vs {want[bad][:3]}"
+    assert got[0] < 1e-3 * float(np.var(y))  # the teacher fits its own data
+
+
+def test_eval_is_deterministic_and_tile_independent(pps):
+    """The same point gives the same loss in any tile position (the sample
+    reduction has a fixed order)."""
+    data, _, _, _ = _task(pps, 1024, 4)
+    prob = pps.mlp.mlp_problem(data)
+    p = np.random.default_rng(0).uniform(-1, 1, 577).astype(np.float32)
+    many = np.tile(p, (19, 1))
+    out = pps.evaluate(prob, many)
+    assert np.all(out == out[0])
+    assert pps.evaluate(prob, p) == out[0]
+
+
+@pytest.mark.parametrize("n,samples,iters", [(45, 256, 6), (1000, 1024, 3)])
+def test_sync_steps_match_oracle(pps, orc, n, samples, iters):
+    data, _, X, y = _task(pps, samples, 8)
+    prob = pps.mlp.mlp_problem(data)
+    oprob = orc.OracleProblem(6, 577, prob.lb, prob.ub, mlp_data=data)
+    ref = orc.OracleSwarm(oprob, n, 21)
+    with pps.Swarm(prob, n, seed=21) as sw:
+        sw.init()
+        ref.init(orc.SAMPLER_UNIFORM)
+        st = sw.state()
+        assert np.array_equal(st["x"], ref.x) and np.array_equal(st["v"], ref.v)
+        assert _close(st["cost"], ref.cost).all()
+        assert np.array_equal(st["pcost"], st["cost"])
+        for it in range(iters):
+            before = sw.state()
+            g0, gc0, gi0 = sw.gbest()
+            # the oracle steps from the GPU's state
+            for k in ("x", "v", "pbest", "pcost", "cost"):
+                getattr(ref, k)[...] = before[k]
+            ref.g[...] = g0
+            ref.c.gcost, ref.c.gidx = gc0, gi0
+            ref.t = it
+            ref.sync_run(1)
+            sw.sync_run(1)
+            st = sw.state()
+            # position and velocity updates: bit-exact
+            assert np.array_equal(st["x"], ref.x), f"iteration {it + 1}: positions differ"
+            assert np.array_equal(st["v"], ref.v), f"iteration {it + 1}: velocities differ"
+            # losses within the tensor-core tolerance
+            assert _close(st["cost"], ref.cost).all(), f"iteration {it + 1}: losses out of tolerance"
+            # personal bests follow the GPU's own losses (strict <)
+            improved = st["cost"] < before["pcost"]
+            assert np.array_equal(st["pcost"], np.where(improved, st["cost"], before["pcost"]))
+            assert np.array_equal(st["pbest"], np.where(improved[None, :], st["x"], before["pbest"]))
+            # the global best is the lowest-index argmin of the personal bests
+            g, gc, gi = sw.gbest()
+            assert gi == int(np.argmin(st["pcost"])) and gc == st["pcost"].min()
+            assert np.array_equal(g, st["pbest"][:, gi])
+
+
+def test_pso_trains_the_network(pps, orc):
+    """ParallelSyncPSOKernel on the workload's task (1024 samples) lowers the
+    loss, and the reported best loss is the loss of the reported best point."""
+    data, _, X, y = _task(pps, 1024, 11)
+    prob = pps.mlp.mlp_problem(data)
+    with pps.Swarm(prob, 4096, seed=5) as sw:
+        sw.init()
+        _, first, _ = sw.gbest()
+        sw.sync_run(200)
+        g, last, _ = sw.gbest()
+    assert last < 0.5 * first
+    assert _close(last, orc.mlp_loss(g, X, y))
+    assert last == pps.evaluate(prob, g)
+
+
+def test_mlp_rejects_async(pps):
+    data, _, _, _ = _task(pps, 128, 1)
+    with pps.Swarm(pps.mlp.mlp_problem(data), 64, seed=1) as sw:
+        sw.init()
+        with pytest.raises(pps.PPSError):
+            sw.async_run(2)
