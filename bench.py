@@ -269,6 +269,60 @@ def run_ode_batch(pps, count_each=512) -> dict:
             "block_shape": shape}
 
 
+MLP_PARTICLES = 16384
+MLP_SAMPLES = 1024
+SFU_PER_CLK_PER_SM = 16  # tanh.approx results per clock per SM (special-function pipe)
+
+
+def run_mlp(pps, iters: int = 100, cpu_seconds: float = 3.0) -> dict:
+    """Training the 16 -> 32 tanh -> 1 MLP by ParallelSyncPSOKernel: 16,384
+    particles x 577 parameters, 1024 samples of a synthetic teacher, bounds
+    [-1, 1].  Each iteration is the position update plus the tensor-core loss
+    kernel (bf16 tcgen05 GEMM of the hidden layer, tanh, output layer, MSE)."""
+    data, _ = pps.mlp.teacher_task(MLP_SAMPLES, seed=0)
+    prob = pps.mlp.mlp_problem(data)
+    n = MLP_PARTICLES
+    with pps.Swarm(prob, n, seed=3) as sw:
+        sw.init()
+        sw.sync_run(10)  # warm
+        sw.init()
+        _, first, _ = sw.gbest()
+        with ClockSampler(0) as clk:
+            ms = sw.sync_run(iters)
+        clocks = clk.summary()
+        _, last, _ = sw.gbest()
+    evals = n * iters
+    sec = ms / 1e3
+    gemm_flops = 2.0 * MLP_SAMPLES * 16 * 32 * evals
+    tanh = MLP_SAMPLES * 32.0 * evals
+    sm_mhz = clocks.get("sm_mhz") or 2070.0
+    sfu_peak = SFU_PER_CLK_PER_SM * 152 * sm_mhz * 1e6
+    out = {"workload": f"MLP fit by sync PSO: {n} particles x 577 parameters (16 -> 32 tanh -> 1), "
+                       f"{MLP_SAMPLES} samples of a synthetic teacher, MSE, {iters} iterations",
+           "device_ms": ms, "particle_iters_per_s": evals / sec, "ms_per_iteration": ms / iters,
+           "hidden_gemm_tflops": gemm_flops / sec / 1e12, "tanh_per_s": tanh / sec,
+           "sfu_peak_tanh_per_s": sfu_peak, "sfu_frac": tanh / sec / sfu_peak,
+           "loss_first": first, "loss_after": last, "clocks": clocks}
+    # the oracle on the host cores (float64 loss), a bounded sample
+    try:
+        sys.path.insert(0, str(ROOT / "oracle"))
+        import pps_oracle as orc
+        op = orc.OracleProblem(6, 577, prob.lb, prob.ub, mlp_data=data)
+        ns = 64
+        ref = orc.OracleSwarm(op, ns, 3).init()
+        t0 = time.perf_counter()
+        k = 0
+        while time.perf_counter() - t0 < cpu_seconds:
+            ref.sync_run(1)
+            k += 1
+        cs = time.perf_counter() - t0
+        out["cpu_oracle"] = {"particle_iters_per_s": ns * k / cs, "cores": os.cpu_count(),
+                             "sample": f"{ns} particles x {k} iterations"}
+    except Exception as e:  # the oracle is optional on a machine without its build
+        out["cpu_oracle"] = {"unavailable": str(e)}
+    return out
+
+
 def _request_pool(pps, count, seed):
     """Mixed requests; LV fits reuse a pool of 64 synthetic datasets."""
     rng = np.random.default_rng(seed)
@@ -358,7 +412,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-async", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the hybrid, ODE-batch and served measurements")
-    ap.add_argument("--only", choices=["sync", "async", "hybrid", "ode", "serve"], default=None,
+    ap.add_argument("--mlp-iters", type=int, default=100, help="iterations of the MLP-fit measurement")
+    ap.add_argument("--only", choices=["sync", "async", "hybrid", "ode", "serve", "mlp"], default=None,
                     help="run one workload only (for profiling); prints its result")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU-baseline sample")
     ap.add_argument("--serve-requests", type=int, default=1500, help="requests of the closed-loop served run")
@@ -387,9 +442,9 @@ def main():
     iters = args.iters
     seed0 = 1000 * rank
 
-    if args.only in ("hybrid", "ode", "serve"):
+    if args.only in ("hybrid", "ode", "serve", "mlp"):
         fn = {"hybrid": lambda: run_hybrid(pps), "ode": lambda: run_ode_batch(pps, args.ode_fits),
-              "serve": lambda: run_served(pps, args)}[args.only]
+              "serve": lambda: run_served(pps, args), "mlp": lambda: run_mlp(pps, args.mlp_iters)}[args.only]
         if rank == 0:
             print(json.dumps({args.only: fn()}), flush=True)
         return 0
@@ -471,6 +526,7 @@ def main():
         extras["hybrid"] = run_hybrid(pps)
         extras["ode_batch"] = run_ode_batch(pps, args.ode_fits)
         extras["served"] = run_served(pps, args)
+        extras["mlp"] = run_mlp(pps, args.mlp_iters)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline and args.only is None:

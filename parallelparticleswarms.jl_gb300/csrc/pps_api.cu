@@ -339,9 +339,8 @@ static constexpr int kGraphChunk = 32;
 
 static int step_once(pps_swarm* s, float c1, float c2) {
   if (is_ode(s->objective)) return launch_sync_step_ode(s, c1, c2);
-  const int rc = launch_sync_step(s, c1, c2);
-  if (rc || s->objective != kMlp) return rc;
-  return launch_mlp_step_eval(s);
+  if (s->objective == kMlp) return launch_mlp_step(s, c1, c2);
+  return launch_sync_step(s, c1, c2);
 }
 
 static int run_steps(pps_swarm* s, int32_t maxiters, float c1, float c2, uint32_t run_flags) {
@@ -510,13 +509,15 @@ int pps_eval_objective(const pps_problem* prob, int64_t npoints, const float* x,
   float* dx = nullptr;
   cudaStream_t st = nullptr;
   PPS_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
-  const size_t bx = sizeof(float) * (size_t)D * (size_t)npoints;
-  cudaError_t e = cudaMallocAsync(&dx, bx + sizeof(float) * (size_t)npoints, st);
+  // device layout x[d * stride + i]; the stride is padded to 64 points
+  const int64_t stride = (int64_t)align_up((size_t)npoints, 64);
+  const size_t bx = sizeof(float) * (size_t)D * (size_t)stride;
+  cudaError_t e = cudaMallocAsync(&dx, bx + sizeof(float) * (size_t)stride, st);
   if (e != cudaSuccess) {
     cudaStreamDestroy(st);
     return cuda_error(e, "cudaMallocAsync");
   }
-  float* df = dx + (size_t)D * (size_t)npoints;
+  float* df = dx + (size_t)D * (size_t)stride;
   ObjParams op = make_params(prob);
   ObjData od{};
   float* ddata = nullptr;
@@ -545,18 +546,22 @@ int pps_eval_objective(const pps_problem* prob, int64_t npoints, const float* x,
     od.data = ddata;
     od.ndata = prob->ndata;
   }
-  if (!rc && (e = cudaMemcpyAsync(dx, x, bx, cudaMemcpyHostToDevice, st)) != cudaSuccess) rc = cuda_error(e, "cudaMemcpy");
+  if (!rc && (e = cudaMemsetAsync(dx, 0, bx, st)) != cudaSuccess) rc = cuda_error(e, "cudaMemset");
+  if (!rc && (e = cudaMemcpy2DAsync(dx, sizeof(float) * (size_t)stride, x, sizeof(float) * (size_t)npoints,
+                                    sizeof(float) * (size_t)npoints, (size_t)D, cudaMemcpyHostToDevice, st)) !=
+                 cudaSuccess)
+    rc = cuda_error(e, "cudaMemcpy");
   unsigned int status = 0;
   if (!rc) {
     if (prob->objective == kMlp) {
       unsigned int* dstatus = reinterpret_cast<unsigned int*>(da + packed.size());
-      rc = launch_mlp_points(ddata, prob->ndata, da, dx, npoints, npoints, df, dstatus, st);
+      rc = launch_mlp_points(ddata, prob->ndata, da, dx, npoints, stride, df, dstatus, st);
       if (!rc && (e = cudaMemcpyAsync(&status, dstatus, sizeof(status), cudaMemcpyDeviceToHost, st)) != cudaSuccess)
         rc = cuda_error(e, "cudaMemcpy");
     } else if (is_ode(prob->objective)) {
-      rc = launch_eval_ode(op, od, prob->objective, dx, npoints, npoints, df, st);
+      rc = launch_eval_ode(op, od, prob->objective, dx, npoints, stride, df, st);
     } else {
-      rc = launch_eval(op, od, prob->objective, dx, npoints, npoints, df, st);
+      rc = launch_eval(op, od, prob->objective, dx, npoints, stride, df, st);
     }
   }
   if (!rc && (e = cudaMemcpyAsync(f, df, sizeof(float) * npoints, cudaMemcpyDeviceToHost, st)) != cudaSuccess)

@@ -119,14 +119,14 @@ int launch_sync_step_ode(pps_swarm* s, float c1, float c2);
 int launch_eval_ode(const ObjParams& op, const ObjData& od, int objective, const float* x, int64_t npts,
                     int64_t stride, float* f, cudaStream_t stream);
 inline bool is_ode(int objective) { return objective == kLvFit || objective == kFhnFit; }
-// MLP-regression objective on the tensor cores (pps_mlp.cu); the step kernel
-// moves the particles and k_mlp_eval evaluates, updates personal bests and
-// publishes the argmin
+// MLP-regression objective on the tensor cores (pps_mlp.cu): one kernel per
+// iteration moves the particles, evaluates them, updates the personal bests
+// and publishes the argmin
 int mlp_check(const pps_problem* prob);
 size_t mlp_a_bytes(int samples);
 void mlp_pack_a(const float* X, int samples, uint8_t* out);
 int launch_mlp_init_eval(pps_swarm* s);
-int launch_mlp_step_eval(pps_swarm* s);
+int launch_mlp_step(pps_swarm* s, float c1, float c2);
 int launch_mlp_points(const float* data_dev, int64_t ndata, const uint8_t* a_dev, const float* x, int64_t npts,
                       int64_t stride, float* f, unsigned int* status, cudaStream_t stream);
 

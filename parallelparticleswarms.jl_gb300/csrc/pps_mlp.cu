@@ -7,22 +7,40 @@
 //   W1[i][j] at i*32 + j (input i, hidden j), b1 at 512 + j, w2 at 544 + j, b2 at 576.
 //   loss = (1/S) sum_s (w2 . tanh(W1^T x_s + b1) + b2 - y_s)^2
 //
-// GB300 design.  For a tile of 8 particles the hidden pre-activations of all S
-// samples are one GEMM, [S x 16] (samples, bf16) x [16 x 256] (8 particles x 32
-// hidden units, bf16) -> [S x 256] fp32: per 128-sample block one
-// tcgen05.mma.cta_group::1.kind::f16 (M = 128, N = 256, K = 16) issued by one
-// thread, operands in shared memory (canonical K-major layout, no swizzle:
-// 8-row x 16-byte core matrices), the accumulator in tensor memory (256
-// columns).  The epilogue warps read it back with tcgen05.ld (warp w owns TMEM
-// lanes 32 (w % 4) .. +31 = samples, warps 0-3 particles 0-3 and warps 4-7
-// particles 4-7), apply b1, tanh (tanh.approx.f32), the output layer and the
-// squared error, and reduce per particle in a fixed order.  The samples (A
+// GB300 design.  One launch per PSO iteration does everything: the position
+// update (src/kernels.jl:1-26, the arithmetic and Philox counters of the
+// other step kernels), the loss, the personal best and the argmin publication.
+// For a tile of 8 particles the hidden pre-activations of all S samples are a
+// GEMM, [S x 16] (samples, bf16) x [16 x 256] (8 particles x 32 hidden units,
+// bf16) -> [S x 256] fp32, plus the bias: per 128-sample block one
+// tcgen05.mma.cta_group::1.kind::f16 (M = 128, N = 256, K = 16) of samples x
+// W1 and a second one that adds b1 as the product of a constant operand (ones
+// in K columns 0-2) with b1 split into three bf16 terms hi + mid + lo (exact
+// for a float).  Thread 0 issues both from shared memory (canonical K-major
+// layout, no swizzle: 8-row x 16-byte core matrices) into one of two
+// tensor-memory accumulator buffers (2 x 256 of the SM's 512 columns), so the
+// MMAs of block m + 1 run while the 16 warps drain block m: "full" mbarriers
+// (tcgen05.commit) hand a buffer to the warps, "empty" mbarriers (one arrival
+// per warp) hand it back to the issuing thread.  Warp w reads TMEM lanes
+// 32 (w % 4) .. +31 (its samples) and the 64 columns of particles 2 (w / 4)
+// and 2 (w / 4) + 1, computes b2 + sum_j w2_j tanh(h_j) (tanh.approx.f32) and
+// the squared error, and keeps one running sum per particle.  The
+// per-particle losses are reduced in a fixed order (lanes by a shuffle tree,
+// then the four sample quarters in order), so a particle's loss does not
+// depend on its tile or block.  While a tile computes, every thread moves (or
+// in the other modes loads) one dim pair of the next tile per sample block
+// and stores its parameters into the second operand buffer.  The samples (A
 // operand) are converted to the core-matrix layout once per swarm and copied
 // into shared memory once per CTA.
 //
-// Every wait on the MMA-completion mbarrier is bounded by %globaltimer; a
-// timeout sets bit 1 of a status word (IterState::status for a swarm) and the
-// host reports PPS_ETIMEOUT.
+// The epilogue is bound by the special-function pipe (one tanh per sample,
+// particle and hidden unit: 16 per clock per SM); the GEMM is 2 x 16 flops
+// per tanh.
+//
+// Every mbarrier wait is bounded by %globaltimer; a timeout ends the launch
+// for the block, sets bit 1 of a status word (IterState::status for a swarm)
+// and the host reports PPS_ETIMEOUT.
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 
@@ -38,11 +56,13 @@ constexpr int kMlpHidden = 32;
 constexpr int kMlpDim = kMlpIn * kMlpHidden + 2 * kMlpHidden + 1;  // 577
 constexpr int kMlpTileParticles = 8;
 constexpr int kMlpN = kMlpTileParticles * kMlpHidden;  // 256 accumulator columns
-constexpr int kMlpThreads = 256;
+constexpr int kMlpWarps = 16;
+constexpr int kMlpThreads = 32 * kMlpWarps;
 constexpr int kMlpMaxSamples = 4096;
-constexpr uint32_t kMlpTmemCols = 256;
+constexpr uint32_t kMlpTmemCols = 2 * kMlpN;  // two accumulator buffers
 constexpr size_t kMlpATileBytes = 128 * kMlpIn * 2;  // 4 KB per 128 samples
 constexpr size_t kMlpBBytes = (size_t)kMlpN * kMlpIn * 2;  // 8 KB
+constexpr uint64_t kMlpWaitNs = 2000000000ull;
 
 // ---------------------------------------------------------------- PTX helpers
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -88,7 +108,10 @@ __device__ __forceinline__ void mma_commit(uint32_t mbar) {
 }
 __device__ __forceinline__ void mbar_init(uint32_t mbar, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(mbar), "r"(count) : "memory");
-  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t mbar) {
+  asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.release.cta.shared::cta.b64 st, [%0];\n\t}\n" ::"r"(mbar)
+               : "memory");
 }
 __device__ __forceinline__ bool mbar_try_wait(uint32_t mbar, uint32_t parity) {
   uint32_t ok;
@@ -100,22 +123,40 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t mbar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
+// bounded wait: false when the time limit passed or another thread gave up
+// (the clock and the abort flag are looked at every 64 polls)
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t mbar, uint32_t parity, volatile int* abort_flag) {
+  if (mbar_try_wait(mbar, parity)) return true;
+  const uint64_t t0 = globaltimer();
+  for (uint32_t i = 1;; ++i) {
+    if (mbar_try_wait(mbar, parity)) return true;
+    if ((i & 63u) == 0 && (*abort_flag || globaltimer() - t0 > kMlpWaitNs)) {
+      *abort_flag = 1;
+      return false;
+    }
+  }
+}
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 __device__ __forceinline__ void tc_before_sync() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_after_sync() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
-// 16 consecutive fp32 columns of this thread's TMEM lane
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
-  uint32_t r[16];
+// 32 consecutive fp32 columns of this thread's TMEM lane; the load and the
+// wait are one asm statement, so no use of a value precedes the wait
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
+  uint32_t r[32];
   asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n\t"
+      "tcgen05.wait::ld.sync.aligned;"
       : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
       : "r"(taddr)
       : "memory");
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-  for (int k = 0; k < 16; ++k) v[k] = __uint_as_float(r[k]);
+  for (int k = 0; k < 32; ++k) v[k] = __uint_as_float(r[k]);
 }
 __device__ __forceinline__ float tanh_fast(float x) {
   float y;
@@ -124,6 +165,9 @@ __device__ __forceinline__ float tanh_fast(float x) {
 }
 __device__ __forceinline__ uint16_t bf16_bits(float v) {
   return __bfloat16_as_ushort(__float2bfloat16_rn(v));
+}
+__device__ __forceinline__ float bf16_value(float v) {
+  return __bfloat162float(__float2bfloat16_rn(v));
 }
 
 // byte offset of element (row r, k) of a K-major operand tile with K = 16:
@@ -134,7 +178,8 @@ __host__ __device__ __forceinline__ uint32_t kmajor_offset(uint32_t r, uint32_t 
 
 // ---------------------------------------------------------------- the kernel
 // MODE 0: init (cost -> pcost, flag 0, argmin publication)
-// MODE 1: step (cost, personal-best update, argmin publication)
+// MODE 1: step: position update (src/kernels.jl:1-26), loss, personal best,
+//         argmin publication, (t, w) advanced
 // MODE 2: evaluate points (write f only; X = points, npad = stride)
 struct MlpArgs {
   const uint8_t* A;      // S/128 tiles of the samples in the core-matrix layout (bf16)
@@ -143,133 +188,287 @@ struct MlpArgs {
   int from_position;     // gbest gathered from positions (PPS_FLAG_GBEST_FROM_POSITION)
   float* f;              // MODE 2 output
   unsigned int* status;  // bit 1 set when a wait for the tensor core gave up
+  uint64_t seed;         // MODE 1: Philox key
+  float c1, c2;
 };
+
+constexpr int kMlpPairs = (kMlpDim + 1) / 2;                    // 289 dim pairs per particle
+constexpr int kMlpTilePairs = kMlpTileParticles * kMlpPairs;    // 2312 per tile
+constexpr int kMlpChunks = (kMlpTilePairs + kMlpThreads - 1) / kMlpThreads;  // 5 per thread
+constexpr int kMlpW2Stride = 36;  // per particle: w2[32], b2, pad (16-byte rows)
+
+// A thread owns the pairs e = tid + 512 c (c < 5) of a tile: particle e % 8,
+// dims 2 (e / 8) and 2 (e / 8) + 1; a warp's accesses are 32-byte sectors (8
+// consecutive particles of one dim).
+struct PairLoad {
+  float x0, v0, p0, x1, v1, p1;
+  uint8_t flag;
+};
+
+template <bool MOVE>
+__device__ __forceinline__ void pair_issue(const SwarmDev& s, int64_t tile, int64_t ntiles, int e, PairLoad& L) {
+  const int p = e & 7, pr = e >> 3;
+  const int64_t pi = tile * kMlpTileParticles + p;
+  const bool live = tile < ntiles && e < kMlpTilePairs && pi < s.n;
+  const int d0 = 2 * pr, d1 = d0 + 1;
+  const bool has1 = d1 < kMlpDim;
+  const int64_t o0 = (int64_t)d0 * s.npad + pi, o1 = o0 + s.npad;
+  L.x0 = live ? s.X[o0] : 0.0f;
+  L.x1 = (live && has1) ? s.X[o1] : 0.0f;
+  if constexpr (MOVE) {
+    L.v0 = live ? s.V[o0] : 0.0f;
+    L.p0 = live ? s.P[o0] : 0.0f;
+    L.v1 = (live && has1) ? s.V[o1] : 0.0f;
+    L.p1 = (live && has1) ? s.P[o1] : 0.0f;
+    L.flag = live ? s.flag[pi] : 0;
+  }
+}
+
+// the position update of one pair (k_sync_step's arithmetic and Philox
+// counters); returns the new positions in L.x0, L.x1
+__device__ __forceinline__ void pair_move(const SwarmDev& s, const MlpArgs& a, int64_t tile, int64_t ntiles, int e,
+                                          uint32_t t, float w, const float* sG, const float* sLb, const float* sUb,
+                                          PairLoad& L) {
+  const int p = e & 7, pr = e >> 3;
+  const int64_t pi = tile * kMlpTileParticles + p;
+  if (!(tile < ntiles && e < kMlpTilePairs && pi < s.n)) return;
+  const int d0 = 2 * pr, d1 = d0 + 1;
+  const int64_t o0 = (int64_t)d0 * s.npad + pi, o1 = o0 + s.npad;
+  const Rand4 r = philox4x32_10((uint32_t)pi, (uint32_t)pr, t, kTagStep, (uint32_t)a.seed, (uint32_t)(a.seed >> 32));
+  if (L.flag) {  // deferred personal-best copy of the previous step
+    L.p0 = L.x0;
+    s.P[o0] = L.x0;
+  }
+  L.v0 = velocity(L.x0, L.v0, L.p0, sG[d0], w, a.c1, a.c2, u01(r.a), u01(r.b));
+  L.x0 = clamp_lb_ub(__fadd_rn(L.x0, L.v0), sLb[d0], sUb[d0]);
+  s.X[o0] = L.x0;
+  s.V[o0] = L.v0;
+  if (d1 < kMlpDim) {
+    if (L.flag) {
+      L.p1 = L.x1;
+      s.P[o1] = L.x1;
+    }
+    L.v1 = velocity(L.x1, L.v1, L.p1, sG[d1], w, a.c1, a.c2, u01(r.c), u01(r.d));
+    L.x1 = clamp_lb_ub(__fadd_rn(L.x1, L.v1), sLb[d1], sUb[d1]);
+    s.X[o1] = L.x1;
+    s.V[o1] = L.v1;
+  }
+}
+
+// one parameter of particle p into the tile's operand buffers: W1 (bf16) into
+// B, b1 as three bf16 terms hi + mid + lo (exact) into the bias operand, w2
+// and b2 into the epilogue's table
+__device__ __forceinline__ void put_param(int p, int d, float x, uint8_t* sB, uint8_t* sBb, float* sW2) {
+  if (d < kMlpIn * kMlpHidden) {
+    const int i = d / kMlpHidden, j = d % kMlpHidden;
+    *reinterpret_cast<uint16_t*>(sB + kmajor_offset((uint32_t)(p * kMlpHidden + j), (uint32_t)i)) = bf16_bits(x);
+  } else if (d < kMlpIn * kMlpHidden + kMlpHidden) {
+    const int j = d - kMlpIn * kMlpHidden;
+    const float hi = bf16_value(x);
+    const float mid = bf16_value(__fsub_rn(x, hi));
+    const float lo = bf16_value(__fsub_rn(__fsub_rn(x, hi), mid));
+    const uint32_t row = (uint32_t)(p * kMlpHidden + j);
+    *reinterpret_cast<uint16_t*>(sBb + kmajor_offset(row, 0)) = bf16_bits(hi);
+    *reinterpret_cast<uint16_t*>(sBb + kmajor_offset(row, 1)) = bf16_bits(mid);
+    *reinterpret_cast<uint16_t*>(sBb + kmajor_offset(row, 2)) = bf16_bits(lo);
+  } else {
+    sW2[p * kMlpW2Stride + (d - kMlpIn * kMlpHidden - kMlpHidden)] = x;  // w2[0..31], b2 at 32
+  }
+}
+
+__device__ __forceinline__ void pair_put(int e, const PairLoad& L, uint8_t* sB, uint8_t* sBb, float* sW2) {
+  if (e >= kMlpTilePairs) return;
+  const int p = e & 7, d0 = 2 * (e >> 3);
+  put_param(p, d0, L.x0, sB, sBb, sW2);
+  if (d0 + 1 < kMlpDim) put_param(p, d0 + 1, L.x1, sB, sBb, sW2);
+}
 
 template <int MODE>
 __global__ void __launch_bounds__(kMlpThreads, 1) k_mlp_eval(SwarmDev s, MlpArgs a) {
+  constexpr bool MOVE = MODE == 1;
   extern __shared__ __align__(1024) uint8_t smem[];
-  const int mtiles = a.S / 128;
-  uint8_t* sA = smem;                                             // mtiles x 4 KB
-  uint8_t* sB = sA + (size_t)mtiles * kMlpATileBytes;             // 8 KB
-  float* sPrm = reinterpret_cast<float*>(sB + kMlpBBytes);        // 8 x (32 b1 + 32 w2 + 1 b2)
-  float* sY = sPrm + kMlpTileParticles * 65;                      // S
-  float* sRed = sY + a.S;                                         // 8 warps x 4
-  __shared__ uint64_t mbar;
+  const int S = a.S;
+  const int mtiles = S / 128;
+  uint8_t* sA = smem;                                                  // mtiles x 4 KB
+  uint8_t* sOnes = sA + (size_t)mtiles * kMlpATileBytes;               // 4 KB
+  uint8_t* sB = sOnes + kMlpATileBytes;                                // 2 x 8 KB (W1)
+  uint8_t* sBb = sB + 2 * kMlpBBytes;                                  // 2 x 8 KB (b1 terms)
+  float* sW2 = reinterpret_cast<float*>(sBb + 2 * kMlpBBytes);         // 2 x 8 x 36
+  float* sY = sW2 + 2 * kMlpTileParticles * kMlpW2Stride;              // S
+  float* sRed = sY + S;                                                // 2 x 16 warps x 2
+  float* sG = sRed + 2 * kMlpWarps * 2;                                // 3 x 580 (MODE 1)
+  float* sLb = sG + 580;
+  float* sUb = sLb + 580;
+  __shared__ uint64_t full_bar[2], empty_bar[2];
   __shared__ uint32_t tmem_base;
+  __shared__ volatile int abort_flag;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  IterState* st = s.st;
+  const int q = warp & 3;    // TMEM lane quarter: samples 32 q .. 32 q + 31 of each block
+  const int pg = warp >> 2;  // particles 2 pg, 2 pg + 1 of the tile
+  const int64_t n = s.n;
+  const int64_t ntiles = (n + kMlpTileParticles - 1) / kMlpTileParticles;
+  int64_t tile = blockIdx.x;
+  uint32_t t = 0;
+  float w = 0.0f;
+  if constexpr (MOVE) {
+    t = s.st->t;
+    w = s.st->w;
+  }
 
-  // samples and targets into shared memory (16-byte copies)
+  // samples, targets, the constant operand of the bias MMA (ones in K columns
+  // 0-2), zeroed bias operands, and (MODE 1) gbest and the bounds
   {
     const uint4* src = reinterpret_cast<const uint4*>(a.A);
     uint4* dst = reinterpret_cast<uint4*>(sA);
     const int n16 = (int)((size_t)mtiles * kMlpATileBytes / 16);
-    for (int k = tid; k < n16; k += blockDim.x) dst[k] = src[k];
-    for (int k = tid; k < a.S; k += blockDim.x) sY[k] = a.y[k];
+    for (int k = tid; k < n16; k += kMlpThreads) dst[k] = src[k];
+    for (int k = tid; k < S; k += kMlpThreads) sY[k] = a.y[k];
+    uint4* zb = reinterpret_cast<uint4*>(sBb);
+    for (int k = tid; k < (int)(2 * kMlpBBytes / 16); k += kMlpThreads) zb[k] = make_uint4(0u, 0u, 0u, 0u);
+    for (int k = tid; k < 128 * kMlpIn; k += kMlpThreads) {
+      const int r = k / kMlpIn, c = k % kMlpIn;
+      *reinterpret_cast<uint16_t*>(sOnes + kmajor_offset((uint32_t)r, (uint32_t)c)) = (c < 3) ? 0x3F80u : 0u;
+    }
+    if constexpr (MOVE) {
+      for (int d = tid; d < kMlpDim; d += kMlpThreads) {
+        sG[d] = s.g[d];
+        sLb[d] = s.lb[d];
+        sUb[d] = s.ub[d];
+      }
+    }
+  }
+  __syncthreads();  // zeroed bias operands and gbest before the first tile's parameters
+  // the first tile's parameters (moved in MODE 1)
+#pragma unroll 1
+  for (int c = 0; c < kMlpChunks; ++c) {
+    const int e = tid + kMlpThreads * c;
+    PairLoad L;
+    pair_issue<MOVE>(s, tile, ntiles, e, L);
+    if constexpr (MOVE) pair_move(s, a, tile, ntiles, e, t, w, sG, sLb, sUb, L);
+    pair_put(e, L, sB, sBb, sW2);
   }
   if (warp == 0) tmem_alloc(smem_u32(&tmem_base), kMlpTmemCols);
-  if (tid == 0) mbar_init(smem_u32(&mbar), 1);
+  if (tid == 0) {
+    mbar_init(smem_u32(&full_bar[0]), 1);
+    mbar_init(smem_u32(&full_bar[1]), 1);
+    mbar_init(smem_u32(&empty_bar[0]), kMlpWarps);
+    mbar_init(smem_u32(&empty_bar[1]), kMlpWarps);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    abort_flag = 0;
+  }
+  fence_async_smem();  // operands written by the generic proxy, read by the tensor core
   tc_before_sync();
   __syncthreads();
   tc_after_sync();
   const uint32_t tmem = tmem_base;
-  const uint32_t mbar_a = smem_u32(&mbar);
   const uint32_t idesc = mlp_idesc(128, kMlpN);
-  const uint64_t bdesc = smem_desc(smem_u32(sB), 128, 256);
-  uint32_t phase = 0;
-  bool timed_out = false;
-
-  const int64_t n = s.n;
-  const int64_t ntiles = (n + kMlpTileParticles - 1) / kMlpTileParticles;
+  uint32_t issued = 0;    // blocks issued by thread 0 (block g goes to buffer g & 1)
+  uint32_t consumed = 0;  // blocks this thread has drained
   unsigned long long best = ~0ull;
-  const int q = warp & 3;        // TMEM lane quarter: samples 32q .. 32q + 31 of each block
-  const int pgroup = warp >> 2;  // particles 4 pgroup .. 4 pgroup + 3 of the tile
+  int tb = 0;  // operand buffer of the current tile
 
-  for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    const int64_t i0 = tile * kMlpTileParticles;
-    // ---- B: the tile's W1 as bf16, K-major (row = particle*32 + hidden unit)
-    for (int e = tid; e < kMlpTileParticles * kMlpIn * kMlpHidden; e += blockDim.x) {
-      const int p = e & 7, d = e >> 3;  // 8 consecutive particles of one parameter
-      const int i = d / kMlpHidden, j = d % kMlpHidden;
-      const int64_t pi = i0 + p;
-      const float w = (pi < n) ? s.X[(int64_t)d * s.npad + pi] : 0.0f;
-      *reinterpret_cast<uint16_t*>(sB + kmajor_offset((uint32_t)(p * kMlpHidden + j), (uint32_t)i)) = bf16_bits(w);
-    }
-    for (int e = tid; e < kMlpTileParticles * 65; e += blockDim.x) {
-      const int p = e & 7, r = e >> 3;  // r: b1 (0..31), w2 (32..63), b2 (64)
-      const int64_t pi = i0 + p;
-      sPrm[p * 65 + r] = (pi < n) ? s.X[(int64_t)(512 + r) * s.npad + pi] : 0.0f;
-    }
-    fence_async_smem();  // the generic-proxy writes of B become visible to the tensor core
-    tc_before_sync();
-    __syncthreads();
+  // thread 0: D = X W1 + b1 of block g (sample block m of the current tile)
+  auto issue = [&](int m) {
+    const uint32_t g = issued;
+    const uint32_t b = g & 1u, use = g >> 1;
+    if (use >= 1 && !mbar_wait_bounded(smem_u32(&empty_bar[b]), (use - 1u) & 1u, &abort_flag)) return;
     tc_after_sync();
+    const uint32_t d = tmem + b * (uint32_t)kMlpN;
+    mma_bf16_ss(d, smem_desc(smem_u32(sA + (size_t)m * kMlpATileBytes), 128, 256),
+                smem_desc(smem_u32(sB + (size_t)tb * kMlpBBytes), 128, 256), idesc, 0u);
+    mma_bf16_ss(d, smem_desc(smem_u32(sOnes), 128, 256), smem_desc(smem_u32(sBb + (size_t)tb * kMlpBBytes), 128, 256),
+                idesc, 1u);
+    mma_commit(smem_u32(&full_bar[b]));
+    issued = g + 1;
+  };
 
-    float lacc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+  for (; tile < ntiles; tile += gridDim.x, tb ^= 1) {
+    const int64_t i0 = tile * kMlpTileParticles;
+    const int64_t next = tile + gridDim.x;
+    if (tid == 0) issue(0);
+    const float* w2base = sW2 + (size_t)tb * kMlpTileParticles * kMlpW2Stride + (2 * pg) * kMlpW2Stride;
+    uint8_t* nB = sB + (size_t)(tb ^ 1) * kMlpBBytes;
+    uint8_t* nBb = sBb + (size_t)(tb ^ 1) * kMlpBBytes;
+    float* nW2 = sW2 + (size_t)(tb ^ 1) * kMlpTileParticles * kMlpW2Stride;
+    float acc[2] = {0.0f, 0.0f};
     for (int m = 0; m < mtiles; ++m) {
-      if (tid == 0) {
-        tc_after_sync();
-        const uint64_t adesc = smem_desc(smem_u32(sA + (size_t)m * kMlpATileBytes), 128, 256);
-        mma_bf16_ss(tmem, adesc, bdesc, idesc, 0u);
-        mma_commit(mbar_a);
-      }
-      // bounded wait for the MMA (2 s of %globaltimer); a timeout ends the
-      // launch for the whole block at the barrier below
-      bool ok = true;
-      {
-        const uint64_t t0 = globaltimer();
-        while (!mbar_try_wait(mbar_a, phase)) {
-          if (globaltimer() - t0 > 2000000000ull) {
-            ok = false;
-            break;
-          }
-        }
-      }
-      phase ^= 1u;
-      tc_after_sync();
-      // ---- epilogue: this thread's sample row, 4 particles of its group
-      const int srow = m * 128 + q * 32 + lane;
-      const float ys = sY[srow];
-#pragma unroll
-      for (int pp = 0; pp < 4; ++pp) {
-        const int p = pgroup * 4 + pp;
-        const float* prm = sPrm + p * 65;
-        float o = prm[64];
-#pragma unroll
-        for (int half = 0; half < 2; ++half) {
-          float v[16];
-          tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(p * kMlpHidden + half * 16), v);
-#pragma unroll
-          for (int k = 0; k < 16; ++k) {
-            const int jj = half * 16 + k;
-            o = __fmaf_rn(prm[32 + jj], tanh_fast(__fadd_rn(v[k], prm[jj])), o);
-          }
-        }
-        const float e = __fsub_rn(o, ys);
-        lacc[pp] = __fmaf_rn(e, e, lacc[pp]);
-      }
-      tc_before_sync();
-      // TMEM reads done before the next MMA overwrites the accumulator
-      if (__syncthreads_or(!ok)) {
-        timed_out = true;
+      if (tid == 0 && m + 1 < mtiles) issue(m + 1);
+      // one chunk of the next tile's parameters per block: loads issued here,
+      // used after the epilogue
+      PairLoad L;
+      const int e = tid + kMlpThreads * m;
+      const bool chunk = m < kMlpChunks;
+      if (chunk) pair_issue<MOVE>(s, next, ntiles, e, L);
+      __syncwarp();
+      const uint32_t g = consumed;
+      const uint32_t b = g & 1u;
+      // every lane waits; the warp goes on only if all of them saw the phase
+      // (tcgen05.ld below is a warp-wide instruction)
+      int okl = 1;
+      if (lane == 0) okl = mbar_wait_bounded(smem_u32(&full_bar[b]), (g >> 1) & 1u, &abort_flag) ? 1 : 0;
+      const bool ok = __shfl_sync(0xffffffffu, okl, 0) != 0;
+      __syncwarp();
+      if (!ok) {
+        abort_flag = 1;
         break;
       }
-    }
-    if (timed_out) break;  // block-uniform
-    // ---- per-particle loss: warp tree over samples, then the 4 warps in order
+      tc_after_sync();
+      const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + b * (uint32_t)kMlpN + (uint32_t)(pg * 64);
+      const float ys = sY[m * 128 + q * 32 + lane];
 #pragma unroll
-    for (int pp = 0; pp < 4; ++pp) {
-      float vsum = lacc[pp];
+      for (int pp = 0; pp < 2; ++pp) {
+        float v[32];
+        tmem_ld32(taddr + (uint32_t)(pp * 32), v);
+        if (pp == 1) {  // both halves read: hand the buffer back
+          tc_before_sync();
+          __syncwarp();
+          if (lane == 0) mbar_arrive(smem_u32(&empty_bar[b]));
+        }
+        const float* w2 = w2base + pp * kMlpW2Stride;
+        float o = w2[32];  // b2
+#pragma unroll
+        for (int j = 0; j < kMlpHidden; j += 4) {
+          const float4 ww = *reinterpret_cast<const float4*>(w2 + j);
+          o = __fmaf_rn(ww.x, tanh_fast(v[j]), o);
+          o = __fmaf_rn(ww.y, tanh_fast(v[j + 1]), o);
+          o = __fmaf_rn(ww.z, tanh_fast(v[j + 2]), o);
+          o = __fmaf_rn(ww.w, tanh_fast(v[j + 3]), o);
+        }
+        const float err = __fsub_rn(o, ys);
+        acc[pp] = __fmaf_rn(err, err, acc[pp]);
+      }
+      consumed = g + 1;
+      if (chunk) {
+        if constexpr (MOVE) pair_move(s, a, next, ntiles, e, t, w, sG, sLb, sUb, L);
+        pair_put(e, L, nB, nBb, nW2);
+      }
+    }
+    // chunks left when the tile has fewer sample blocks than chunks
+#pragma unroll 1
+    for (int c = mtiles; c < kMlpChunks; ++c) {
+      const int e = tid + kMlpThreads * c;
+      PairLoad L;
+      pair_issue<MOVE>(s, next, ntiles, e, L);
+      if constexpr (MOVE) pair_move(s, a, next, ntiles, e, t, w, sG, sLb, sUb, L);
+      pair_put(e, L, nB, nBb, nW2);
+    }
+    // ---- per-particle loss: shuffle tree over the lanes, then the quarters in order
+    float* red = sRed + (size_t)tb * kMlpWarps * 2;
+#pragma unroll
+    for (int pp = 0; pp < 2; ++pp) {
+      float vsum = acc[pp];
 #pragma unroll
       for (int off = 16; off > 0; off >>= 1) vsum = __fadd_rn(vsum, __shfl_xor_sync(0xffffffffu, vsum, off));
-      if (lane == 0) sRed[warp * 4 + pp] = vsum;
+      if (lane == 0) red[warp * 2 + pp] = vsum;
     }
+    fence_async_smem();  // the next tile's operands, written above, for the tensor core
     __syncthreads();
+    if (abort_flag) break;  // block-uniform after the barrier
     if (tid < kMlpTileParticles) {
-      const int p = tid, g = p >> 2, pp = p & 3;
+      const int p = tid, g4 = p >> 1, pp = p & 1;
       float tot = 0.0f;
-      for (int w = 0; w < 4; ++w) tot = __fadd_rn(tot, sRed[(g * 4 + w) * 4 + pp]);
-      const float c = __fdiv_rn(tot, (float)a.S);
+      for (int qq = 0; qq < 4; ++qq) tot = __fadd_rn(tot, red[(g4 * 4 + qq) * 2 + pp]);
+      const float c = __fdiv_rn(tot, (float)S);
       const int64_t pi = i0 + p;
       if (pi < n) {
         if (MODE == 2) {
@@ -290,14 +489,16 @@ __global__ void __launch_bounds__(kMlpThreads, 1) k_mlp_eval(SwarmDev s, MlpArgs
         }
       }
     }
-    __syncthreads();  // sB / sPrm / sRed reused by the next tile
   }
-  if (timed_out && tid == 0) {
+  if (abort_flag && tid == 0) {
     atomicOr(a.status, 2u);
-    // the MMA in flight still writes the accumulator: wait for it (bounded)
+    // the last block issued may still write its buffer: wait for it (bounded)
     // before the columns are released
-    const uint64_t t0 = globaltimer();
-    while (!mbar_try_wait(mbar_a, phase ^ 1u) && globaltimer() - t0 < 1000000000ull) {
+    if (issued > 0) {
+      const uint32_t g = issued - 1;
+      const uint64_t t0 = globaltimer();
+      while (!mbar_try_wait(smem_u32(&full_bar[g & 1u]), (g >> 1) & 1u) && globaltimer() - t0 < 1000000000ull) {
+      }
     }
   }
   tc_before_sync();
@@ -305,11 +506,12 @@ __global__ void __launch_bounds__(kMlpThreads, 1) k_mlp_eval(SwarmDev s, MlpArgs
   tc_after_sync();
   if (warp == 0) tmem_dealloc(tmem, kMlpTmemCols);
   if (MODE != 2) {
-    if (publish_block_min(best, st)) {
+    if (publish_block_min(best, s.st)) {
+      IterState* st = s.st;
       if (MODE == 0)
         finish_iteration(s, a.from_position != 0, 0u, st->w);
       else
-        finish_iteration(s, a.from_position != 0, st->t + 1u, __fmul_rn(st->w, st->wdamp));
+        finish_iteration(s, a.from_position != 0, t + 1u, __fmul_rn(w, st->wdamp));
     }
   }
 }
@@ -327,7 +529,7 @@ void mlp_pack_a(const float* X, int S, uint8_t* out) {
       memcpy(&b, &v, 4);
       uint16_t h;
       if ((b & 0x7f800000u) == 0x7f800000u) {
-        h = (uint16_t)(b >> 16) | ((b & 0x7fffffu) ? 0x40u : 0u);
+        h = (uint16_t)((b >> 16) | ((b & 0x7fffffu) ? 0x40u : 0u));
       } else {
         b += 0x7fffu + ((b >> 16) & 1u);  // round to nearest even
         h = (uint16_t)(b >> 16);
@@ -351,15 +553,17 @@ int mlp_check(const pps_problem* prob) {
 }
 
 static size_t mlp_smem(int S) {
-  const size_t need = mlp_a_bytes(S) + kMlpBBytes + sizeof(float) * (kMlpTileParticles * 65 + S + 32) + 1024;
-  // at least 100 KB so that at most two CTAs share an SM: each holds 256 of
-  // the SM's 512 tensor-memory columns, so an allocation never has to wait
-  return need > 100 * 1024 ? need : 100 * 1024;
+  const size_t need = mlp_a_bytes(S) + kMlpATileBytes + 4 * kMlpBBytes +
+                      sizeof(float) * (2 * kMlpTileParticles * kMlpW2Stride + S + 2 * kMlpWarps * 2 + 3 * 580) + 1024;
+  // at least 120 KB so that no two CTAs share an SM: each holds all 512
+  // tensor-memory columns, so an allocation never has to wait
+  return need > 120 * 1024 ? need : 120 * 1024;
 }
 
-static int mlp_grid(pps_swarm* s, int64_t n) {
+// one CTA per SM (tensor memory), at most one per tile
+static int mlp_grid_for(int sm_count, int64_t n) {
   const int64_t ntiles = (n + kMlpTileParticles - 1) / kMlpTileParticles;
-  int64_t grid = 2 * (int64_t)s->sm_count;
+  int64_t grid = sm_count;
   if (grid > ntiles) grid = ntiles;
   return (int)(grid < 1 ? 1 : grid);
 }
@@ -392,22 +596,30 @@ static int launch_mlp(const SwarmDev& dv, const MlpArgs& a, int grid, cudaStream
 }
 
 static MlpArgs args_of(pps_swarm* s) {
-  MlpArgs a;
+  MlpArgs a{};
   a.S = (int)(s->od.ndata / 17);
   a.A = reinterpret_cast<const uint8_t*>(s->mlp_a_dev);
   a.y = s->od.data + (size_t)a.S * kMlpIn;
   a.from_position = (s->flags & PPS_FLAG_GBEST_FROM_POSITION) ? 1 : 0;
   a.f = nullptr;
   a.status = &s->dv.st->status;
+  a.seed = s->seed;
   return a;
 }
 
 int launch_mlp_init_eval(pps_swarm* s) {
   const int rc = mlp_set_smem_limit();  // init precedes every captured run of this swarm
   if (rc) return rc;
-  return launch_mlp<0>(s->dv, args_of(s), mlp_grid(s, s->dv.n), s->stream);
+  return launch_mlp<0>(s->dv, args_of(s), mlp_grid_for(s->sm_count, s->dv.n), s->stream);
 }
-int launch_mlp_step_eval(pps_swarm* s) { return launch_mlp<1>(s->dv, args_of(s), mlp_grid(s, s->dv.n), s->stream); }
+
+// one synchronous iteration: move, evaluate, personal bests, argmin
+int launch_mlp_step(pps_swarm* s, float c1, float c2) {
+  MlpArgs a = args_of(s);
+  a.c1 = c1;
+  a.c2 = c2;
+  return launch_mlp<1>(s->dv, a, mlp_grid_for(s->sm_count, s->dv.n), s->stream);
+}
 
 // objective values at npts points x[d * stride + i]; a_dev holds the samples
 // packed by mlp_pack_a, status one zeroed word
@@ -418,7 +630,7 @@ int launch_mlp_points(const float* data_dev, int64_t ndata, const uint8_t* a_dev
   dv.n = npts;
   dv.npad = stride;
   dv.dim = kMlpDim;
-  MlpArgs a;
+  MlpArgs a{};
   a.S = (int)(ndata / 17);
   a.A = a_dev;
   a.y = data_dev + (size_t)a.S * kMlpIn;
@@ -430,10 +642,7 @@ int launch_mlp_points(const float* data_dev, int64_t ndata, const uint8_t* a_dev
   int sm = 0, dev = 0;
   PPS_CUDA(cudaGetDevice(&dev));
   PPS_CUDA(cudaDeviceGetAttribute(&sm, cudaDevAttrMultiProcessorCount, dev));
-  const int64_t ntiles = (npts + kMlpTileParticles - 1) / kMlpTileParticles;
-  int64_t grid = 2 * (int64_t)sm;
-  if (grid > ntiles) grid = ntiles;
-  return launch_mlp<2>(dv, a, (int)(grid < 1 ? 1 : grid), stream);
+  return launch_mlp<2>(dv, a, mlp_grid_for(sm, npts), stream);
 }
 
 }  // namespace pps

@@ -192,32 +192,26 @@ __global__ void __launch_bounds__(kSyncThreads, (PPT == 4 ? 2 : (PPT == 2 ? 3 : 
         xb[k] = nxb[k]; vb[k] = nvb[k]; pb[k] = npb[k];
       }
     }
-    if constexpr (OBJ != kMlp) {
-      float pc[PPT], cc[PPT];
-      ldv<PPT>(pc, s.pcost + i0);
+    float pc[PPT], cc[PPT];
+    ldv<PPT>(pc, s.pcost + i0);
 #pragma unroll
-      for (int k = 0; k < PPT; ++k) {
-        cc[k] = finalize<OBJ>(op, acc[k].s1, acc[k].s2);
-        const bool valid = i0 + k < n;
-        // if cost < best_cost: best = position (strict <, src/kernels.jl:21-24)
-        fl[k] = (valid && cc[k] < pc[k]) ? 1 : 0;
-        pc[k] = fl[k] ? cc[k] : pc[k];
-        if (valid) {
-          const unsigned long long key = argmin_key(pc[k], (uint32_t)(i0 + k));
-          best = key < best ? key : best;
-        }
+    for (int k = 0; k < PPT; ++k) {
+      cc[k] = finalize<OBJ>(op, acc[k].s1, acc[k].s2);
+      const bool valid = i0 + k < n;
+      // if cost < best_cost: best = position (strict <, src/kernels.jl:21-24)
+      fl[k] = (valid && cc[k] < pc[k]) ? 1 : 0;
+      pc[k] = fl[k] ? cc[k] : pc[k];
+      if (valid) {
+        const unsigned long long key = argmin_key(pc[k], (uint32_t)(i0 + k));
+        best = key < best ? key : best;
       }
-      stv<PPT>(s.pcost + i0, pc);
-      stv<PPT>(s.cost + i0, cc);
-      stflags<PPT>(s.flag + i0, fl);
     }
+    stv<PPT>(s.pcost + i0, pc);
+    stv<PPT>(s.cost + i0, cc);
+    stflags<PPT>(s.flag + i0, fl);
   }
-  // MLP: position update only; k_mlp_eval evaluates, updates the personal
-  // bests and flags, publishes the argmin and advances (t, w)
-  if constexpr (OBJ != kMlp) {
-    if (publish_block_min(best, st)) {
-      finish_iteration(s, from_position != 0, t + 1u, __fmul_rn(w, st->wdamp));
-    }
+  if (publish_block_min(best, st)) {
+    finish_iteration(s, from_position != 0, t + 1u, __fmul_rn(w, st->wdamp));
   }
 }
 
@@ -324,7 +318,6 @@ int sync_grid(pps_swarm* s) {
       case kRosenbrock: per_sm = occupancy_of<kRosenbrock>(ppt, smem); break;
       case kRastrigin: per_sm = occupancy_of<kRastrigin>(ppt, smem); break;
       case kAckley: per_sm = occupancy_of<kAckley>(ppt, smem); break;
-      case kMlp: per_sm = occupancy_of<kMlp>(ppt, smem); break;
       default: per_sm = occupancy_of<kBeale>(ppt, smem); break;
     }
     if (per_sm < 1) per_sm = 1;
@@ -358,11 +351,7 @@ int launch_sync_step(pps_swarm* s, float c1, float c2) {
     k_sync_step<O, 2><<<grid, kSyncThreads, smem, s->stream>>>(s->dv, s->op, s->seed, c1, c2, from_pos, passes); \
   else                                                                                                  \
     k_sync_step<O, 1><<<grid, kSyncThreads, smem, s->stream>>>(s->dv, s->op, s->seed, c1, c2, from_pos, passes)
-  if (s->objective == kMlp) {
-    L_STEP(kMlp);
-  } else {
-    PPS_DISPATCH_SEPARABLE(s->objective, L_STEP)
-  }
+  PPS_DISPATCH_SEPARABLE(s->objective, L_STEP)
 #undef L_STEP
   PPS_CUDA(cudaGetLastError());
   return PPS_OK;

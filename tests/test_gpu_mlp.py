@@ -3,16 +3,17 @@
 The kernel computes the hidden layer as a bf16 x bf16 -> fp32 tcgen05 GEMM
 and tanh with tanh.approx.f32; the oracle rounds the GEMM operands to bf16 the
 same way and does everything else in float64.  Tolerance on a loss:
-|gpu - oracle| <= 3e-3 * |oracle| + 1e-4 (tanh.approx's error, summed over 32
-hidden units).  The position and velocity updates do not depend on the
-objective's arithmetic and stay bit-exact, checked step by step from the
-GPU's own state."""
+|gpu - oracle| <= 2e-5 * |oracle| + 1e-8 (observed on GB300: at most 6.5e-7
+relative over 800 random particles at 1024 and 4096 samples), inside the 1e-4
+relative bar on final objectives.  The position and velocity updates do not
+depend on the objective's arithmetic and stay bit-exact, checked step by step
+from the GPU's own state."""
 import numpy as np
 import pytest
 
 pytestmark = pytest.mark.gpu
 
-RTOL, ATOL = 3e-3, 1e-4
+RTOL, ATOL = 2e-5, 1e-8
 
 
 def _close(got, want):
