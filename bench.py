@@ -21,11 +21,16 @@ Prints ONE JSON line (rank 0).  Extra measurements ride in the same line:
   ode_batch    512 Lotka-Volterra + 512 FitzHugh-Nagumo fits (particles per fit
                from {256, 1024, 4096}, 100 iterations, RK4 dt=0.01) in one
                batched launch, against the same fits solved one at a time
-  served       the mixed request stream (Rosenbrock / Rastrigin / Ackley /
-               Lotka-Volterra fit, dim U{2..64}, particles U{256..16384},
-               maxiters U{100..2000}) through the continuous-batching server:
-               a closed-loop saturation run, a Poisson(2000/s) open-loop run,
-               p50/p99 time to solution, against one-at-a-time plain solves
+  served       the mixed request stream of the served workload (Rosenbrock /
+               Rastrigin / Ackley / Lotka-Volterra fit / MLP fit, dim U{2..64},
+               particles U{256..16384}, maxiters U{100..2000}) through the
+               continuous-batching server: a closed-loop saturation run, a
+               Poisson(2000/s) open-loop run, p50/p99 time to solution, against
+               one-at-a-time plain solves; served_without_mlp the same without
+               MLP fits (whose tensor-core kernel fills the GPU on its own)
+  mlp          the MLP fit (16,384 particles x 577 parameters, 1024 samples)
+               by sync PSO: particle-iters/s and the tanh rate against the
+               special-function pipe
 With --impl reference the oracle's CPU implementation is timed instead
 (the Julia reference cannot run here: no Julia toolchain).
 """
@@ -323,18 +328,26 @@ def run_mlp(pps, iters: int = 100, cpu_seconds: float = 3.0) -> dict:
     return out
 
 
-def _request_pool(pps, count, seed):
-    """Mixed requests; LV fits reuse a pool of 64 synthetic datasets."""
+def _request_pool(pps, count, seed, with_mlp=True):
+    """Mixed requests: objective uniform over Rosenbrock, Rastrigin, Ackley,
+    the Lotka-Volterra fit and (with_mlp) the MLP fit; LV fits reuse a pool of
+    64 synthetic datasets, MLP fits a pool of 8 teacher tasks (1024 samples)."""
     rng = np.random.default_rng(seed)
     lv_pool = [pps.ode.synthetic_fit("lv", 10_000 + k)[0] for k in range(64)]
+    mlp_pool = [pps.mlp.mlp_problem(pps.mlp.teacher_task(MLP_SAMPLES, seed=20_000 + k)[0]) for k in range(8)] \
+        if with_mlp else []
+    kinds = 5 if with_mlp else 4
     reqs = []
     for _ in range(count):
-        kind = int(rng.integers(4))
+        kind = int(rng.integers(kinds))
         n = int(rng.integers(256, 16385))
         iters = int(rng.integers(100, 2001))
         s = int(rng.integers(0, 2**62))
         if kind == 3:
             reqs.append((lv_pool[int(rng.integers(64))], n, iters, s))
+            continue
+        if kind == 4:
+            reqs.append((mlp_pool[int(rng.integers(8))], n, iters, s))
             continue
         D = int(rng.integers(2, 65))
         name = ("rosenbrock", "rastrigin", "ackley")[kind]
@@ -346,12 +359,19 @@ def _request_pool(pps, count, seed):
     return reqs
 
 
-def run_served(pps, args) -> dict:
+def run_served(pps, args, with_mlp=True) -> dict:
+    """The served mixed stream through the continuous-batching server: a
+    closed-loop saturation run, a Poisson(2000/s) open-loop run, p50/p99 time
+    to solution, against the same requests solved one at a time (plain)."""
     cfg = dict(memory_budget=24 << 30, max_launches=16, max_pack=128, threads=256, ppt=2, tick_us=200.0)
-    out = {"workload": "mixed stream: objective U{Rosenbrock, Rastrigin, Ackley, Lotka-Volterra fit}, dim U{2..64}, "
-                       "particles U{256..16384}, maxiters U{100..2000}", "server": dict(cfg)}
+    mix = "Rosenbrock, Rastrigin, Ackley, Lotka-Volterra fit" + (", MLP fit (577 parameters, 1024 samples)"
+                                                                 if with_mlp else "")
+    out = {"workload": f"mixed stream: objective U{{{mix}}}, dim U{{2..64}}, particles U{{256..16384}}, "
+                       "maxiters U{100..2000}", "server": dict(cfg)}
+    count = args.serve_requests_mlp if with_mlp else args.serve_requests
+    window = args.serve_seconds_mlp if with_mlp else args.serve_seconds
     # closed loop: all requests submitted at once, throughput at saturation
-    reqs = _request_pool(pps, args.serve_requests, 1)
+    reqs = _request_pool(pps, count, 1, with_mlp)
     with pps.Server(**cfg) as srv:
         t0 = time.perf_counter()
         ts = [srv.submit(p, n, maxiters=it, seed=s) for (p, n, it, s) in reqs]
@@ -361,8 +381,8 @@ def run_served(pps, args) -> dict:
     out["closed_loop"] = {"requests": len(reqs), "wall_s": wall, "solves_per_s": len(reqs) / wall,
                           "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "launches": st["launches"],
                           "mean_pack": st["mean_pack"], "arena_peak_bytes": st["arena_peak_bytes"]}
-    # plain: the same kind of requests one at a time through solve()
-    sample = reqs[:60]
+    # plain: the same requests one at a time through solve()
+    sample = reqs[:min(len(reqs), 100)]
     t0 = time.perf_counter()
     same = True
     for k, (p, n, it, s) in enumerate(sample):
@@ -373,12 +393,12 @@ def run_served(pps, args) -> dict:
     out["plain_sample"] = len(sample)
     out["speedup_vs_plain"] = out["closed_loop"]["solves_per_s"] / plain
     out["same_result_alone_and_served"] = same
-    # open loop: Poisson arrivals at 2000/s for serve_seconds, then drain
+    # open loop: Poisson arrivals at 2000/s over the window, then drain
     rate = 2000.0
     rng = np.random.default_rng(2)
-    arrivals = np.cumsum(rng.exponential(1.0 / rate, int(rate * args.serve_seconds * 1.2)))
-    arrivals = arrivals[arrivals < args.serve_seconds]
-    pool = _request_pool(pps, len(arrivals), 3)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, int(rate * window * 1.2) + 8))
+    arrivals = arrivals[arrivals < window]
+    pool = _request_pool(pps, len(arrivals), 3, with_mlp)
     with pps.Server(**cfg) as srv:
         t0 = time.perf_counter()
         tickets = []
@@ -392,7 +412,7 @@ def run_served(pps, args) -> dict:
             srv.wait(t)
         wall = time.perf_counter() - t0
         st = srv.stats()
-    out["open_loop"] = {"offered_per_s": rate, "arrival_window_s": args.serve_seconds, "requests": len(tickets),
+    out["open_loop"] = {"offered_per_s": rate, "arrival_window_s": window, "requests": len(tickets),
                         "submit_s": submit_s, "drain_wall_s": wall, "solves_per_s": len(tickets) / wall,
                         "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "max_ms": st["max_ms"],
                         "launches": st["launches"], "mean_pack": st["mean_pack"],
@@ -416,8 +436,14 @@ def main():
     ap.add_argument("--only", choices=["sync", "async", "hybrid", "ode", "serve", "mlp"], default=None,
                     help="run one workload only (for profiling); prints its result")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU-baseline sample")
-    ap.add_argument("--serve-requests", type=int, default=1500, help="requests of the closed-loop served run")
-    ap.add_argument("--serve-seconds", type=float, default=1.0, help="arrival window of the open-loop served run")
+    ap.add_argument("--serve-requests", type=int, default=1500,
+                    help="requests of the closed-loop served run without MLP fits")
+    ap.add_argument("--serve-seconds", type=float, default=1.0,
+                    help="arrival window of the open-loop served run without MLP fits")
+    ap.add_argument("--serve-requests-mlp", type=int, default=400,
+                    help="requests of the closed-loop served run of the full mix (MLP fits included)")
+    ap.add_argument("--serve-seconds-mlp", type=float, default=0.25,
+                    help="arrival window of the open-loop served run of the full mix")
     ap.add_argument("--ode-fits", type=int, default=512, help="fits of each model in the batched ODE run")
     args = ap.parse_args()
     rank, world, local = dist_env()
@@ -444,7 +470,9 @@ def main():
 
     if args.only in ("hybrid", "ode", "serve", "mlp"):
         fn = {"hybrid": lambda: run_hybrid(pps), "ode": lambda: run_ode_batch(pps, args.ode_fits),
-              "serve": lambda: run_served(pps, args), "mlp": lambda: run_mlp(pps, args.mlp_iters)}[args.only]
+              "serve": lambda: {"served": run_served(pps, args, True),
+                                "served_without_mlp": run_served(pps, args, False)},
+              "mlp": lambda: run_mlp(pps, args.mlp_iters)}[args.only]
         if rank == 0:
             print(json.dumps({args.only: fn()}), flush=True)
         return 0
@@ -525,7 +553,8 @@ def main():
     if rank == 0 and not args.no_extras and args.only is None:
         extras["hybrid"] = run_hybrid(pps)
         extras["ode_batch"] = run_ode_batch(pps, args.ode_fits)
-        extras["served"] = run_served(pps, args)
+        extras["served"] = run_served(pps, args, True)
+        extras["served_without_mlp"] = run_served(pps, args, False)
         extras["mlp"] = run_mlp(pps, args.mlp_iters)
 
     cpu = None

@@ -117,78 +117,86 @@ int pps_set_device(int32_t device) {
   return PPS_OK;
 }
 
-int pps_swarm_create(const pps_problem* prob, int64_t n, uint64_t seed, uint32_t flags,
-                     pps_swarm** out) {
-  if (!out) return set_error(PPS_EINVAL, "out is NULL");
-  *out = nullptr;
-  int rc = check_problem(prob);
-  if (rc) return rc;
-  if (n < 1 || n > (int64_t)0xFFFFFF00LL) return set_error(PPS_EINVAL, "n must be in [1, 2^32-256] (got %lld)", (long long)n);
-  int ndev = 0;
-  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return set_error(PPS_ENODEV, "no CUDA device");
+}  // extern "C"
 
-  pps_swarm* s = new (std::nothrow) pps_swarm();
-  if (!s) return set_error(PPS_ENOMEM, "host allocation failed");
-  cudaGetDevice(&s->device);
-  cudaDeviceGetAttribute(&s->sm_count, cudaDevAttrMultiProcessorCount, s->device);
+namespace pps {
+
+// One device block per swarm, carved into 256-byte-aligned arrays.
+struct SwarmLayout {
+  size_t oX, oV, oP, oPc, oC, oF, oG, oLb, oUb, oU0, oSt, oData, oMlpA, bytes;
+  int64_t npad;
+  int mlp_samples;
+};
+
+static SwarmLayout swarm_layout(const pps_problem* prob, int64_t n) {
+  SwarmLayout L{};
   const int D = prob->dim;
-  const int64_t npad = (int64_t)align_up((size_t)n, 64);
-  // carve one allocation
+  L.npad = (int64_t)align_up((size_t)n, 64);
   size_t off = 0;
   auto take = [&](size_t bytes) {
     const size_t at = off;
     off = align_up(off + bytes, 256);
     return at;
   };
-  const size_t oX = take(sizeof(float) * D * npad);
-  const size_t oV = take(sizeof(float) * D * npad);
-  const size_t oP = take(sizeof(float) * D * npad);
-  const size_t oPc = take(sizeof(float) * npad);
-  const size_t oC = take(sizeof(float) * npad);
-  const size_t oF = take(npad);
-  const size_t oG = take(sizeof(float) * D);
-  const size_t oLb = take(sizeof(float) * D);
-  const size_t oUb = take(sizeof(float) * D);
-  const size_t oU0 = take(sizeof(float) * D);
-  const size_t oSt = take(sizeof(IterState));
-  const size_t oData = take(sizeof(float) * (prob->data ? (size_t)prob->ndata : 0));
-  const int mlp_samples = prob->objective == kMlp ? (int)(prob->ndata / 17) : 0;
-  const size_t oMlpA = take(mlp_samples ? mlp_a_bytes(mlp_samples) : 0);
-  s->bytes = off;
-  cudaError_t e = cudaMalloc(&s->block, s->bytes);
-  if (e != cudaSuccess) {
-    delete s;
-    return cuda_error(e, "cudaMalloc(swarm state)");
-  }
-  char* b = static_cast<char*>(s->block);
-  s->dv.X = reinterpret_cast<float*>(b + oX);
-  s->dv.V = reinterpret_cast<float*>(b + oV);
-  s->dv.P = reinterpret_cast<float*>(b + oP);
-  s->dv.pcost = reinterpret_cast<float*>(b + oPc);
-  s->dv.cost = reinterpret_cast<float*>(b + oC);
-  s->dv.flag = reinterpret_cast<uint8_t*>(b + oF);
-  s->dv.g = reinterpret_cast<float*>(b + oG);
-  s->dv.lb = reinterpret_cast<float*>(b + oLb);
-  s->dv.ub = reinterpret_cast<float*>(b + oUb);
-  s->dv.st = reinterpret_cast<IterState*>(b + oSt);
-  s->u0_dev = reinterpret_cast<float*>(b + oU0);
-  s->data_dev = reinterpret_cast<float*>(b + oData);
+  L.oX = take(sizeof(float) * D * L.npad);
+  L.oV = take(sizeof(float) * D * L.npad);
+  L.oP = take(sizeof(float) * D * L.npad);
+  L.oPc = take(sizeof(float) * L.npad);
+  L.oC = take(sizeof(float) * L.npad);
+  L.oF = take(L.npad);
+  L.oG = take(sizeof(float) * D);
+  L.oLb = take(sizeof(float) * D);
+  L.oUb = take(sizeof(float) * D);
+  L.oU0 = take(sizeof(float) * D);
+  L.oSt = take(sizeof(IterState));
+  L.oData = take(sizeof(float) * (prob->data ? (size_t)prob->ndata : 0));
+  L.mlp_samples = prob->objective == kMlp ? (int)(prob->ndata / 17) : 0;
+  L.oMlpA = take(L.mlp_samples ? mlp_a_bytes(L.mlp_samples) : 0);
+  L.bytes = off;
+  return L;
+}
+
+int swarm_check(const pps_problem* prob, int64_t n) {
+  const int rc = check_problem(prob);
+  if (rc) return rc;
+  if (n < 1 || n > (int64_t)0xFFFFFF00LL)
+    return set_error(PPS_EINVAL, "n must be in [1, 2^32-256] (got %lld)", (long long)n);
+  return PPS_OK;
+}
+
+size_t swarm_device_bytes(const pps_problem* prob, int64_t n) { return swarm_layout(prob, n).bytes; }
+
+// Points the swarm at device block `b` (layout L), copies the bounds, start
+// point and data asynchronously on s->stream and zeroes the rest.  Host
+// buffers are pageable, so each copy has left them when the call returns.
+static int swarm_setup(pps_swarm* s, const pps_problem* prob, int64_t n, uint64_t seed, uint32_t flags, char* b,
+                       const SwarmLayout& L) {
+  const int D = prob->dim;
+  s->bytes = L.bytes;
+  s->dv.X = reinterpret_cast<float*>(b + L.oX);
+  s->dv.V = reinterpret_cast<float*>(b + L.oV);
+  s->dv.P = reinterpret_cast<float*>(b + L.oP);
+  s->dv.pcost = reinterpret_cast<float*>(b + L.oPc);
+  s->dv.cost = reinterpret_cast<float*>(b + L.oC);
+  s->dv.flag = reinterpret_cast<uint8_t*>(b + L.oF);
+  s->dv.g = reinterpret_cast<float*>(b + L.oG);
+  s->dv.lb = reinterpret_cast<float*>(b + L.oLb);
+  s->dv.ub = reinterpret_cast<float*>(b + L.oUb);
+  s->dv.st = reinterpret_cast<IterState*>(b + L.oSt);
+  s->u0_dev = reinterpret_cast<float*>(b + L.oU0);
+  s->data_dev = reinterpret_cast<float*>(b + L.oData);
   s->od.data = s->data_dev;
   s->od.ndata = prob->data ? prob->ndata : 0;
-  if (mlp_samples) s->mlp_a_dev = b + oMlpA;
+  if (L.mlp_samples) s->mlp_a_dev = b + L.oMlpA;
   s->dv.n = n;
-  s->dv.npad = npad;
+  s->dv.npad = L.npad;
   s->dv.dim = D;
   s->op = make_params(prob);
   s->objective = prob->objective;
   s->seed = seed;
   s->flags = flags;
   s->host_lb = static_cast<float*>(malloc(sizeof(float) * 3 * D));
-  if (!s->host_lb) {
-    cudaFree(s->block);
-    delete s;
-    return set_error(PPS_ENOMEM, "host allocation failed");
-  }
+  if (!s->host_lb) return set_error(PPS_ENOMEM, "host allocation failed");
   s->host_ub = s->host_lb + D;
   s->host_u0 = s->host_lb + 2 * D;
   for (int d = 0; d < D; ++d) {
@@ -196,36 +204,86 @@ int pps_swarm_create(const pps_problem* prob, int64_t n, uint64_t seed, uint32_t
     s->host_ub[d] = prob->ub ? prob->ub[d] : INFINITY;
     s->host_u0[d] = prob->u0 ? prob->u0[d] : 0.0f;
   }
+  PPS_CUDA(cudaMemsetAsync(b, 0, L.bytes, s->stream));
+  PPS_CUDA(cudaMemcpyAsync(s->dv.lb, s->host_lb, sizeof(float) * D, cudaMemcpyHostToDevice, s->stream));
+  PPS_CUDA(cudaMemcpyAsync(s->dv.ub, s->host_ub, sizeof(float) * D, cudaMemcpyHostToDevice, s->stream));
+  PPS_CUDA(cudaMemcpyAsync(s->u0_dev, s->host_u0, sizeof(float) * D, cudaMemcpyHostToDevice, s->stream));
+  if (prob->data && prob->ndata > 0)
+    PPS_CUDA(cudaMemcpyAsync(s->data_dev, prob->data, sizeof(float) * (size_t)prob->ndata, cudaMemcpyHostToDevice,
+                             s->stream));
+  if (L.mlp_samples) {
+    std::vector<uint8_t> packed(mlp_a_bytes(L.mlp_samples));
+    mlp_pack_a(prob->data, L.mlp_samples, packed.data());
+    PPS_CUDA(cudaMemcpyAsync(s->mlp_a_dev, packed.data(), packed.size(), cudaMemcpyHostToDevice, s->stream));
+  }
+  return PPS_OK;
+}
+
+// A swarm over caller-owned device memory (at least swarm_device_bytes) and
+// a caller-owned stream: used by the server, which carves swarms from its
+// arena.  Nothing is synchronised.
+int swarm_attach(const pps_problem* prob, int64_t n, uint64_t seed, uint32_t flags, void* mem, cudaStream_t stream,
+                 pps_swarm** out) {
+  *out = nullptr;
+  int rc = swarm_check(prob, n);
+  if (rc) return rc;
+  pps_swarm* s = new (std::nothrow) pps_swarm();
+  if (!s) return set_error(PPS_ENOMEM, "host allocation failed");
+  s->owns_memory = false;
+  cudaGetDevice(&s->device);
+  cudaDeviceGetAttribute(&s->sm_count, cudaDevAttrMultiProcessorCount, s->device);
+  s->stream = stream;
+  if ((rc = swarm_setup(s, prob, n, seed, flags, static_cast<char*>(mem), swarm_layout(prob, n)))) {
+    swarm_detach(s);
+    return rc;
+  }
+  *out = s;
+  return PPS_OK;
+}
+
+// releases what an attached swarm owns on the host (its graph included);
+// the caller makes sure its stream has finished with it
+void swarm_detach(pps_swarm* s) {
+  if (!s) return;
+  if (s->graph) cudaGraphExecDestroy(s->graph);
+  free(s->host_lb);
+  delete s;
+}
+
+}  // namespace pps
+
+extern "C" {
+
+int pps_swarm_create(const pps_problem* prob, int64_t n, uint64_t seed, uint32_t flags,
+                     pps_swarm** out) {
+  if (!out) return set_error(PPS_EINVAL, "out is NULL");
+  *out = nullptr;
+  int rc = swarm_check(prob, n);
+  if (rc) return rc;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return set_error(PPS_ENODEV, "no CUDA device");
+  pps_swarm* s = new (std::nothrow) pps_swarm();
+  if (!s) return set_error(PPS_ENOMEM, "host allocation failed");
+  cudaGetDevice(&s->device);
+  cudaDeviceGetAttribute(&s->sm_count, cudaDevAttrMultiProcessorCount, s->device);
+  const SwarmLayout L = swarm_layout(prob, n);
+  cudaError_t e = cudaMalloc(&s->block, L.bytes);
+  if (e != cudaSuccess) {
+    delete s;
+    return cuda_error(e, "cudaMalloc(swarm state)");
+  }
   rc = PPS_OK;
   do {
-    e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
-    if (e != cudaSuccess) { rc = cuda_error(e, "cudaStreamCreate"); break; }
+    if ((e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking)) != cudaSuccess) {
+      rc = cuda_error(e, "cudaStreamCreate");
+      break;
+    }
     if ((e = cudaEventCreate(&s->ev0)) != cudaSuccess || (e = cudaEventCreate(&s->ev1)) != cudaSuccess) {
       rc = cuda_error(e, "cudaEventCreate");
       break;
     }
-    if ((e = cudaMemsetAsync(s->block, 0, s->bytes, s->stream)) != cudaSuccess) { rc = cuda_error(e, "cudaMemset"); break; }
-    if ((e = cudaMemcpyAsync(s->dv.lb, s->host_lb, sizeof(float) * D, cudaMemcpyHostToDevice, s->stream)) != cudaSuccess ||
-        (e = cudaMemcpyAsync(s->dv.ub, s->host_ub, sizeof(float) * D, cudaMemcpyHostToDevice, s->stream)) != cudaSuccess ||
-        (e = cudaMemcpyAsync(b + oU0, s->host_u0, sizeof(float) * D, cudaMemcpyHostToDevice, s->stream)) != cudaSuccess) {
-      rc = cuda_error(e, "cudaMemcpy(bounds)");
-      break;
-    }
-    if (prob->data && prob->ndata > 0 &&
-        (e = cudaMemcpyAsync(s->data_dev, prob->data, sizeof(float) * (size_t)prob->ndata, cudaMemcpyHostToDevice,
-                             s->stream)) != cudaSuccess) {
-      rc = cuda_error(e, "cudaMemcpy(data)");
-      break;
-    }
-    if (mlp_samples) {
-      std::vector<uint8_t> packed(mlp_a_bytes(mlp_samples));
-      mlp_pack_a(prob->data, mlp_samples, packed.data());
-      if ((e = cudaMemcpy(s->mlp_a_dev, packed.data(), packed.size(), cudaMemcpyHostToDevice)) != cudaSuccess) {
-        rc = cuda_error(e, "cudaMemcpy(MLP samples)");
-        break;
-      }
-    }
-    if ((e = cudaStreamSynchronize(s->stream)) != cudaSuccess) { rc = cuda_error(e, "cudaStreamSynchronize"); break; }
+    if ((rc = swarm_setup(s, prob, n, seed, flags, static_cast<char*>(s->block), L))) break;
+    if ((e = cudaStreamSynchronize(s->stream)) != cudaSuccess) rc = cuda_error(e, "cudaStreamSynchronize");
   } while (0);
   if (rc) {
     pps_swarm_destroy(s);
@@ -237,6 +295,7 @@ int pps_swarm_create(const pps_problem* prob, int64_t n, uint64_t seed, uint32_t
 
 int pps_swarm_destroy(pps_swarm* s) {
   if (!s) return PPS_OK;
+  if (!s->owns_memory) return set_error(PPS_EINVAL, "swarm belongs to a server");
   int dev = -1;
   cudaGetDevice(&dev);
   if (dev != s->device) cudaSetDevice(s->device);
@@ -576,3 +635,35 @@ int pps_eval_objective(const pps_problem* prob, int64_t npoints, const float* x,
 }
 
 }  // extern "C"
+
+namespace pps {
+
+int swarm_enqueue_init(pps_swarm* s) {
+  int sampler = PPS_SAMPLER_UNIFORM;
+  bool all_inf = true;
+  for (int d = 0; d < s->dv.dim; ++d)
+    if (!(std::isinf(s->host_lb[d]) && std::isinf(s->host_ub[d]))) all_inf = false;
+  if (all_inf) sampler = PPS_SAMPLER_UNBOUNDED;
+  for (int d = 0; sampler == PPS_SAMPLER_UNIFORM && d < s->dv.dim; ++d)
+    if (!std::isfinite(s->host_lb[d]) || !std::isfinite(s->host_ub[d]))
+      return set_error(PPS_EINVAL, "uniform sampler needs finite bounds (dim %d)", d);
+  int rc;
+  if ((rc = launch_set_iter(s, 0u, 0.7298f, 1.0f))) return rc;
+  if ((rc = is_ode(s->objective) ? launch_init_ode(s, sampler, s->u0_dev) : launch_init(s, sampler, s->u0_dev)))
+    return rc;
+  if (s->objective == kMlp && (rc = launch_mlp_init_eval(s))) return rc;
+  s->t = 0;
+  s->initialized = 1;
+  return PPS_OK;
+}
+
+int swarm_enqueue_run(pps_swarm* s, int32_t maxiters, float w, float wdamp, float c1, float c2) {
+  int rc = check_run(s, maxiters, w, wdamp, c1, c2);
+  if (rc) return rc;
+  if ((rc = launch_set_iter(s, s->t, w, wdamp))) return rc;
+  if ((rc = run_steps(s, maxiters, c1, c2, s->flags & PPS_FLAG_GBEST_FROM_POSITION))) return rc;
+  s->t += (uint32_t)maxiters;
+  return PPS_OK;
+}
+
+}  // namespace pps

@@ -88,6 +88,7 @@ struct pps_swarm {
   void* local_block = nullptr;  // HybridPSO local-stage results (allocated on first use)
   int local_valid = 0;
   void* mlp_a_dev = nullptr;  // MLP objective: the samples as bf16 tensor-core tiles
+  bool owns_memory = true;    // false: device block and stream belong to a server
 };
 
 namespace pps {
@@ -127,6 +128,17 @@ size_t mlp_a_bytes(int samples);
 void mlp_pack_a(const float* X, int samples, uint8_t* out);
 int launch_mlp_init_eval(pps_swarm* s);
 int launch_mlp_step(pps_swarm* s, float c1, float c2);
+// swarms over caller-owned memory and streams (pps_api.cu), for the server:
+// nothing below synchronises
+int swarm_check(const pps_problem* prob, int64_t n);
+size_t swarm_device_bytes(const pps_problem* prob, int64_t n);
+int swarm_attach(const pps_problem* prob, int64_t n, uint64_t seed, uint32_t flags, void* mem, cudaStream_t stream,
+                 pps_swarm** out);
+void swarm_detach(pps_swarm* s);
+int swarm_enqueue_init(pps_swarm* s);
+int swarm_enqueue_run(pps_swarm* s, int32_t maxiters, float w, float wdamp, float c1, float c2);
+// gbest (dim floats), its cost and index into mail, then done = 1, visible to the host
+int launch_publish_result(pps_swarm* s, float* mail, int* done);
 int launch_mlp_points(const float* data_dev, int64_t ndata, const uint8_t* a_dev, const float* x, int64_t npts,
                       int64_t stride, float* f, unsigned int* status, cudaStream_t stream);
 

@@ -2,7 +2,12 @@
 //
 // The reference has no serving layer: each solve() owns the device for its
 // duration.  This server admits optimization problems as they arrive and
-// solves them in the batched kernel (one CTA per swarm, pps_batch.cu):
+// solves them in the batched kernel (one CTA or cluster per swarm,
+// pps_batch.cu); MLP-fit requests, whose loss runs on the tensor cores with
+// one CTA per SM and tile (pps_mlp.cu), run instead as a swarm of their own on
+// a launch slot (state carved from the same arena, iterations replayed as a
+// CUDA graph, the result written to the request's mailbox by a last kernel),
+// concurrently with the batched launches on the other slots:
 //
 //   submit()  validates the problem, stamps the arrival time and queues it.
 //   worker    one host thread that, in a loop,
@@ -27,6 +32,7 @@
 // not depend on the launch, slot or CTA that computes it.  Nothing on the
 // device waits for the host or for another CTA.
 #include <algorithm>
+#include <cmath>
 #include <atomic>
 #include <chrono>
 #include <condition_variable>
@@ -49,6 +55,16 @@ struct Request {
   uint64_t ticket = 0;
   BatchSwarm desc{};
   std::vector<float> host;  // lb | ub | u0 | data
+  // a request solved as a swarm of its own (MLP fit): its problem, run
+  // parameters and, while it runs, the swarm
+  bool single = false;
+  pps_problem prob{};
+  float params[8] = {};
+  int64_t n = 0;
+  uint64_t seed = 0;
+  int32_t maxiters = 0;
+  float w = 0, wdamp = 0, c1 = 0, c2 = 0;
+  pps_swarm* sw = nullptr;
   size_t bytes = 0, offset = 0;
   Clock::time_point t_submit, t_done;
   int state = 0;  // 0 queued, 1 running, 2 done
@@ -199,6 +215,29 @@ int launch_pack(pps_server* s, Slot& sl, std::vector<Request*>& pack, const Laun
   return PPS_OK;
 }
 
+// a request solved as a swarm of its own on slot `sl`: attach it to its arena
+// block, init, the iterations (graph replays) and the mailbox write
+int launch_single(pps_server* s, Slot& sl, Request* r) {
+  int rc = swarm_attach(&r->prob, r->n, r->seed, 0u, static_cast<char*>(s->arena_mem) + r->offset, sl.stream, &r->sw);
+  if (rc) return rc;
+  sl.flags[0] = 0;
+  if ((rc = swarm_enqueue_init(r->sw)) || (rc = swarm_enqueue_run(r->sw, r->maxiters, r->w, r->wdamp, r->c1, r->c2)) ||
+      (rc = launch_publish_result(r->sw, sl.mail_dev, sl.flags_dev))) {
+    cudaStreamSynchronize(sl.stream);
+    swarm_detach(r->sw);
+    r->sw = nullptr;
+    return rc;
+  }
+  PPS_CUDA(cudaEventRecord(sl.done, sl.stream));
+  sl.reqs.assign(1, r);
+  sl.open = 1;
+  sl.busy = true;
+  r->state = 1;
+  s->launches++;
+  s->packed += 1;
+  return PPS_OK;
+}
+
 // retire the requests of `sl` whose swarms have finished; free the slot when
 // its launch has ended and every request is retired
 bool retire_ready(pps_server* s, Slot& sl) {
@@ -218,6 +257,10 @@ bool retire_ready(pps_server* s, Slot& sl) {
     r->idx = (int64_t)bits;
     r->t_done = now;
     r->state = 2;
+    if (r->sw) {  // its stream has passed the mailbox write: the graph is idle
+      swarm_detach(r->sw);
+      r->sw = nullptr;
+    }
     s->arena.release(r->offset, r->bytes);
     s->completed++;
     s->lat_ms.push_back(std::chrono::duration<double, std::milli>(r->t_done - r->t_submit).count());
@@ -256,7 +299,26 @@ void worker_main(pps_server* s) {
       else if (!free_slot)
         free_slot = &sl;
     }
-    if (free_slot && !s->queue.empty()) {
+    if (free_slot && !s->queue.empty() && s->queue.front()->single) {
+      Request* r = s->queue.front();
+      size_t off;
+      if (s->arena.alloc(r->bytes, &off)) {
+        s->queue.pop_front();
+        r->offset = off;
+        const int rc = launch_single(s, *free_slot, r);
+        if (rc) {
+          s->worker_error = rc;
+          snprintf(s->worker_msg, sizeof(s->worker_msg), "%s", pps_last_error());
+          s->arena.release(r->offset, r->bytes);
+          r->state = 2;
+          r->cost = NAN;
+          r->idx = -1;
+          r->t_done = Clock::now();
+          s->cv_done.notify_all();
+        }
+        continue;
+      }
+    } else if (free_slot && !s->queue.empty()) {
       const auto waited = Clock::now() - s->queue.front()->t_submit;
       if (inflight == 0 || waited >= tick || (int)s->queue.size() >= s->cfg.max_pack) {
         // the head of the queue fixes the launch shape (kernel, block and
@@ -269,6 +331,10 @@ void worker_main(pps_server* s) {
                                          scanned < 4 * (size_t)s->cfg.max_pack;
              ++scanned) {
           Request* r = *it;
+          if (r->single) {
+            ++it;
+            continue;
+          }
           const LaunchGroup gr = batch_group_of(r->desc, s->cfg.threads, s->cfg.ppt);
           if (gr.kind != key.kind || gr.T != key.T || gr.C != key.C) {
             ++it;
@@ -363,12 +429,49 @@ int pps_serve_submit(pps_server* s, const pps_problem* prob, int64_t n, uint64_t
   if (!s || !ticket) return set_error(PPS_EINVAL, "NULL argument");
   Request* r = new (std::nothrow) Request();
   if (!r) return set_error(PPS_ENOMEM, "host allocation failed");
-  const int rc = batch_describe(prob, n, seed, maxiters, w, wdamp, c1, c2, &r->desc, &r->host);
-  if (rc) {
-    delete r;
-    return rc;
+  if (prob && prob->objective == kMlp) {
+    // solved as a swarm of its own (the tensor-core kernel wants whole SMs)
+    int rc = swarm_check(prob, n);
+    if (!rc && maxiters < 0) rc = set_error(PPS_EINVAL, "maxiters must be >= 0");
+    if (!rc && !(std::isfinite(w) && std::isfinite(wdamp) && std::isfinite(c1) && std::isfinite(c2)))
+      rc = set_error(PPS_EINVAL, "coefficients must be finite");
+    if (rc) {
+      delete r;
+      return rc;
+    }
+    const int D = prob->dim;
+    r->single = true;
+    r->host.resize((size_t)3 * D + (size_t)prob->ndata);
+    for (int d = 0; d < D; ++d) {
+      r->host[d] = prob->lb ? prob->lb[d] : -INFINITY;
+      r->host[D + d] = prob->ub ? prob->ub[d] : INFINITY;
+      r->host[2 * D + d] = prob->u0 ? prob->u0[d] : 0.0f;
+    }
+    memcpy(r->host.data() + 3 * D, prob->data, sizeof(float) * (size_t)prob->ndata);
+    for (int k = 0; k < prob->nparams; ++k) r->params[k] = prob->params[k];
+    r->prob = *prob;
+    r->prob.lb = r->host.data();
+    r->prob.ub = r->host.data() + D;
+    r->prob.u0 = r->host.data() + 2 * D;
+    r->prob.data = r->host.data() + 3 * D;
+    r->prob.params = r->params;
+    r->n = n;
+    r->seed = seed;
+    r->maxiters = maxiters;
+    r->w = w;
+    r->wdamp = wdamp;
+    r->c1 = c1;
+    r->c2 = c2;
+    r->desc.dim = D;
+    r->bytes = (swarm_device_bytes(prob, n) + 255) / 256 * 256;
+  } else {
+    const int rc = batch_describe(prob, n, seed, maxiters, w, wdamp, c1, c2, &r->desc, &r->host);
+    if (rc) {
+      delete r;
+      return rc;
+    }
+    r->bytes = batch_swarm_bytes(r->desc.dim, r->desc.ld, r->desc.ndata);
   }
-  r->bytes = batch_swarm_bytes(r->desc.dim, r->desc.ld, r->desc.ndata);
   if (r->bytes > s->cfg.memory_budget) {
     delete r;
     return set_error(PPS_ENOMEM, "request needs %zu bytes, more than the serving arena (%llu)", r->bytes,
@@ -483,7 +586,10 @@ int pps_serve_stop(pps_server* s) {
     if (sl.mail) cudaFreeHost(sl.mail);
     if (sl.flags) cudaFreeHost(sl.flags);
   }
-  for (auto& kv : s->reqs) delete kv.second;
+  for (auto& kv : s->reqs) {
+    if (kv.second->sw) swarm_detach(kv.second->sw);
+    delete kv.second;
+  }
   if (s->arena_mem) cudaFree(s->arena_mem);
   delete s;
   return PPS_OK;

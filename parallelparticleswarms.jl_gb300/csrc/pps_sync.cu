@@ -357,6 +357,27 @@ int launch_sync_step(pps_swarm* s, float c1, float c2) {
   return PPS_OK;
 }
 
+// the swarm's result for a host that polls mapped memory: gbest, its cost
+// and index, then the done flag after a system-scope fence
+__global__ void k_publish_result(SwarmDev s, float* __restrict__ mail, int* done) {
+  for (int d = threadIdx.x; d < s.dim; d += blockDim.x) mail[d] = s.g[d];
+  if (threadIdx.x == 0) {
+    mail[s.dim] = s.st->gcost;
+    mail[s.dim + 1] = __uint_as_float(s.st->gidx);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence_system();
+    *reinterpret_cast<volatile int*>(done) = 1;
+  }
+}
+
+int launch_publish_result(pps_swarm* s, float* mail, int* done) {
+  k_publish_result<<<1, 256, 0, s->stream>>>(s->dv, mail, done);
+  PPS_CUDA(cudaGetLastError());
+  return PPS_OK;
+}
+
 int launch_materialize(pps_swarm* s) {
   const int64_t blocks = (s->dv.npad + 255) / 256;
   k_materialize<<<(unsigned)blocks, 256, 0, s->stream>>>(s->dv);

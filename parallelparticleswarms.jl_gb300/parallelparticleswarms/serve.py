@@ -79,12 +79,12 @@ class Server:
             pass
 
 
-def mixed_request(rng: np.random.Generator, objectives=("rosenbrock", "rastrigin", "ackley", "lv")):
+def mixed_request(rng: np.random.Generator, objectives=("rosenbrock", "rastrigin", "ackley", "lv", "mlp")):
     """One request of the served mixed stream: objective uniform over
-    ``objectives``, dim ~ U{2..64} (an ODE fit uses its own parameter count),
-    particles ~ U{256..16384}, maxiters ~ U{100..2000}.  Returns
+    ``objectives``, dim ~ U{2..64} (an ODE or MLP fit has its own parameter
+    count), particles ~ U{256..16384}, maxiters ~ U{100..2000}.  Returns
     (problem, n, maxiters, seed)."""
-    from . import ode
+    from . import mlp, ode
     from .problem import REGISTRY
 
     kind = objectives[int(rng.integers(len(objectives)))]
@@ -94,6 +94,9 @@ def mixed_request(rng: np.random.Generator, objectives=("rosenbrock", "rastrigin
     if kind == "lv":
         prob, _ = ode.synthetic_fit("lv", int(rng.integers(0, 2**31)))
         return prob, n, iters, seed
+    if kind == "mlp":
+        data, _ = mlp.teacher_task(1024, seed=int(rng.integers(0, 2**31)))
+        return mlp.mlp_problem(data), n, iters, seed
     D = int(rng.integers(2, 65))
     obj = REGISTRY[kind]
     lo = {"rosenbrock": -5.0, "rastrigin": -5.12, "ackley": -5.0}[kind]

@@ -15,11 +15,15 @@ def _alone(pps, prob, n, iters, seed):
         return sw.gbest()
 
 
-def _stream(pps, count, seed=0, small=True):
+NO_MLP = ("rosenbrock", "rastrigin", "ackley", "lv")
+
+
+def _stream(pps, count, seed=0, small=True, objectives=None):
     rng = np.random.default_rng(seed)
     out = []
     for _ in range(count):
-        prob, n, iters, s = pps.serve.mixed_request(rng)
+        prob, n, iters, s = (pps.serve.mixed_request(rng) if objectives is None
+                             else pps.serve.mixed_request(rng, objectives))
         if small:  # keep the test short: scale the draws down
             n = max(16, n // 64)
             iters = max(5, iters // 40)
@@ -47,7 +51,7 @@ def test_each_result_same_alone_and_in_the_mix(pps):
 def test_memory_bound_admission_queues_then_completes(pps):
     """A budget that fits about two requests at a time: the rest wait in the
     queue and are admitted as memory frees up."""
-    reqs = _stream(pps, 12, seed=3)
+    reqs = _stream(pps, 12, seed=3, objectives=NO_MLP)
     budget = 600 << 10  # the largest scaled request needs about 200 KiB
     with pps.Server(memory_budget=budget, max_launches=8, max_pack=64, tick_us=0.0) as srv:
         tickets = [srv.submit(p, n, maxiters=it, seed=s) for (p, n, it, s) in reqs]
@@ -59,8 +63,26 @@ def test_memory_bound_admission_queues_then_completes(pps):
     assert all(np.isfinite(c) for (_, c, _, _) in out)
 
 
+def test_mlp_fits_served_beside_batched_requests(pps):
+    """MLP fits run as swarms of their own on launch slots, concurrently with
+    batched launches; each result equals the fit solved alone."""
+    rng = np.random.default_rng(11)
+    reqs = []
+    for k in range(12):
+        kind = ("mlp",) if k % 3 == 0 else NO_MLP
+        prob, n, iters, s = pps.serve.mixed_request(rng, kind)
+        reqs.append((prob, max(16, n // 16), max(5, iters // 50), s))
+    assert sum(p.f.name == "mlp_regression" for p, _, _, _ in reqs) == 4
+    with pps.Server(memory_budget=1 << 30, max_launches=4, max_pack=16, tick_us=50.0) as srv:
+        tickets = [srv.submit(p, n, maxiters=it, seed=s) for (p, n, it, s) in reqs]
+        results = [srv.wait(t) for t in tickets]
+    for (prob, n, iters, s), (u, c, i, lat) in zip(reqs, results):
+        au, ac, ai = _alone(pps, prob, n, iters, s)
+        assert i == ai and np.float32(c) == np.float32(ac) and np.array_equal(u, au)
+
+
 def test_poll_and_errors(pps):
-    reqs = _stream(pps, 1, seed=5)
+    reqs = _stream(pps, 1, seed=5, objectives=NO_MLP)
     prob, n, iters, s = reqs[0]
     with pps.Server(memory_budget=16 << 20) as srv:
         t = srv.submit(prob, n, maxiters=iters, seed=s)
