@@ -26,7 +26,8 @@ struct IterState {
   float gcost;             // global best cost
   unsigned int gidx;       // global best particle
   unsigned int status;     // nonzero: a kernel detected a bad launch
-  unsigned int pad[7];
+  unsigned int tile_next;  // step kernel: next tile to hand out (0 at launch start)
+  unsigned int pad[6];
 };
 
 // Swarm state in HBM (structure of arrays, particle index fastest):
@@ -83,7 +84,6 @@ struct pps_swarm {
   int graph_async_lanes = 0;  // run flags the graph was captured with
   float graph_c1 = 0.0f, graph_c2 = 0.0f;
   int sm_count = 0;
-  int sync_passes = 1;  // tiles per block of the step kernel (set by sync_grid)
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   void* local_block = nullptr;  // HybridPSO local-stage results (allocated on first use)
   int local_valid = 0;

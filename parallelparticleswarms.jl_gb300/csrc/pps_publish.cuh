@@ -60,6 +60,7 @@ __device__ __forceinline__ void finish_iteration(const SwarmDev& s, bool from_po
     st->gidx = gi;
     st->key = ~0ull;
     st->count = 0u;
+    st->tile_next = 0u;  // every block has taken its last tile
     st->t = t_next;
     st->w = w_next;
   }

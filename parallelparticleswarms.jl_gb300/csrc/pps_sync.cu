@@ -85,12 +85,14 @@ __global__ void __launch_bounds__(kSyncThreads) k_init(SwarmDev s, ObjParams op,
 // r1, r2 for both dims.  The loads of the next pair are issued before the
 // current pair is computed (software prefetch), so every warp keeps six
 // vector loads in flight while it runs Philox and the objective.  The swarm
-// is cut into tiles of blockDim x PPT particles and every block takes the same
-// number of consecutive tiles (`passes`), so no thread of any block idles at
-// the final barrier while others finish a last partial pass.
+// is cut into tiles of blockDim x PPT particles that the resident blocks take
+// one at a time from a counter (IterState::tile_next), the next index fetched
+// while the current tile runs: blocks on busier SMs or farther from the
+// memory take fewer tiles, and all finish within about one tile of each
+// other.  A particle's arithmetic does not depend on which block takes it.
 template <int OBJ, int PPT>
 __global__ void __launch_bounds__(kSyncThreads, (PPT == 4 ? 2 : (PPT == 2 ? 3 : 4)))
-    k_sync_step(SwarmDev s, ObjParams op, uint64_t seed, float c1, float c2, int from_position, int passes) {
+    k_sync_step(SwarmDev s, ObjParams op, uint64_t seed, float c1, float c2, int from_position) {
   extern __shared__ float sm[];
   const int D = s.dim;
   float* sg = sm;
@@ -108,107 +110,117 @@ __global__ void __launch_bounds__(kSyncThreads, (PPT == 4 ? 2 : (PPT == 2 ? 3 : 
   const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
   const int64_t npad = s.npad;
   const int64_t ngroups = npad / PPT;  // groups of PPT particles
-  const int64_t gb = (int64_t)blockIdx.x * passes * blockDim.x;
-  int64_t ge = gb + (int64_t)passes * blockDim.x;
-  ge = ge < ngroups ? ge : ngroups;
+  const uint32_t ntiles = (uint32_t)((ngroups + blockDim.x - 1) / blockDim.x);
   float* __restrict__ X = s.X;
   float* __restrict__ V = s.V;
   float* __restrict__ P = s.P;
   const int64_t n = s.n;
   unsigned long long best = ~0ull;
+  __shared__ uint32_t s_tile[2];
+  if (threadIdx.x == 0) s_tile[0] = atomicAdd(&st->tile_next, 1u);
+  __syncthreads();
 
-  for (int64_t q = gb + threadIdx.x; q < ge; q += blockDim.x) {
-    const int64_t i0 = q * PPT;
-    uint8_t fl[PPT];
-    ldflags<PPT>(fl, s.flag + i0);
-    bool anyfl = false;
+  for (int slot = 0;; slot ^= 1) {
+    const uint32_t tl = s_tile[slot];
+    if (tl >= ntiles) break;  // block-uniform
+    if (threadIdx.x == 0) s_tile[slot ^ 1] = atomicAdd(&st->tile_next, 1u);  // the next tile, fetched early
+    const int64_t q = (int64_t)tl * blockDim.x + threadIdx.x;
+    // the tile's last warps may hold fewer groups: the body is conditional,
+    // the barrier after it is not (every thread reaches the same barrier)
+    if (q < ngroups) {
+      const int64_t i0 = q * PPT;
+      uint8_t fl[PPT];
+      ldflags<PPT>(fl, s.flag + i0);
+      bool anyfl = false;
 #pragma unroll
-    for (int k = 0; k < PPT; ++k) anyfl |= (fl[k] != 0);
-    Acc<OBJ> acc[PPT];
-    // current pair (dims j, j+1) and the prefetched next pair
-    float xa[PPT], va[PPT], pa[PPT], xb[PPT], vb[PPT], pb[PPT];
-    ldv<PPT>(xa, X + i0);
-    ldv<PPT>(va, V + i0);
-    ldv<PPT>(pa, P + i0);
-    if (D > 1) {
-      ldv<PPT>(xb, X + npad + i0);
-      ldv<PPT>(vb, V + npad + i0);
-      ldv<PPT>(pb, P + npad + i0);
-    }
-    for (int j = 0; j < D; j += 2) {
-      float nxa[PPT], nva[PPT], npa[PPT], nxb[PPT], nvb[PPT], npb[PPT];
-      if (j + 2 < D) {
-        const int64_t o = (int64_t)(j + 2) * npad + i0;
-        ldv<PPT>(nxa, X + o);
-        ldv<PPT>(nva, V + o);
-        ldv<PPT>(npa, P + o);
+      for (int k = 0; k < PPT; ++k) anyfl |= (fl[k] != 0);
+      Acc<OBJ> acc[PPT];
+      // current pair (dims j, j+1) and the prefetched next pair
+      float xa[PPT], va[PPT], pa[PPT], xb[PPT], vb[PPT], pb[PPT];
+      ldv<PPT>(xa, X + i0);
+      ldv<PPT>(va, V + i0);
+      ldv<PPT>(pa, P + i0);
+      if (D > 1) {
+        ldv<PPT>(xb, X + npad + i0);
+        ldv<PPT>(vb, V + npad + i0);
+        ldv<PPT>(pb, P + npad + i0);
       }
-      if (j + 3 < D) {
-        const int64_t o = (int64_t)(j + 3) * npad + i0;
-        ldv<PPT>(nxb, X + o);
-        ldv<PPT>(nvb, V + o);
-        ldv<PPT>(npb, P + o);
-      }
-      Rand4 r[PPT];
-#pragma unroll
-      for (int k = 0; k < PPT; ++k) r[k] = philox4x32_10((uint32_t)(i0 + k), (uint32_t)(j >> 1), t, kTagStep, k0, k1);
-      {  // dim j
-        const int64_t o = (int64_t)j * npad + i0;
-        if (anyfl) {
-#pragma unroll
-          for (int k = 0; k < PPT; ++k) pa[k] = fl[k] ? xa[k] : pa[k];
-          stv<PPT>(P + o, pa);
+      for (int j = 0; j < D; j += 2) {
+        float nxa[PPT], nva[PPT], npa[PPT], nxb[PPT], nvb[PPT], npb[PPT];
+        if (j + 2 < D) {
+          const int64_t o = (int64_t)(j + 2) * npad + i0;
+          ldv<PPT>(nxa, X + o);
+          ldv<PPT>(nva, V + o);
+          ldv<PPT>(npa, P + o);
         }
-        const float gd = sg[j], lo = slb[j], hi = sub[j];
+        if (j + 3 < D) {
+          const int64_t o = (int64_t)(j + 3) * npad + i0;
+          ldv<PPT>(nxb, X + o);
+          ldv<PPT>(nvb, V + o);
+          ldv<PPT>(npb, P + o);
+        }
+        Rand4 r[PPT];
+#pragma unroll
+        for (int k = 0; k < PPT; ++k) r[k] = philox4x32_10((uint32_t)(i0 + k), (uint32_t)(j >> 1), t, kTagStep, k0, k1);
+        {  // dim j
+          const int64_t o = (int64_t)j * npad + i0;
+          if (anyfl) {
+#pragma unroll
+            for (int k = 0; k < PPT; ++k) pa[k] = fl[k] ? xa[k] : pa[k];
+            stv<PPT>(P + o, pa);
+          }
+          const float gd = sg[j], lo = slb[j], hi = sub[j];
+#pragma unroll
+          for (int k = 0; k < PPT; ++k) {
+            va[k] = velocity(xa[k], va[k], pa[k], gd, w, c1, c2, u01(r[k].a), u01(r[k].b));
+            xa[k] = clamp_lb_ub(__fadd_rn(xa[k], va[k]), lo, hi);
+            acc[k].add(op, j, xa[k]);
+          }
+          stv<PPT>(X + o, xa);
+          stv<PPT>(V + o, va);
+        }
+        if (j + 1 < D) {  // dim j + 1
+          const int64_t o = (int64_t)(j + 1) * npad + i0;
+          if (anyfl) {
+#pragma unroll
+            for (int k = 0; k < PPT; ++k) pb[k] = fl[k] ? xb[k] : pb[k];
+            stv<PPT>(P + o, pb);
+          }
+          const float gd = sg[j + 1], lo = slb[j + 1], hi = sub[j + 1];
+#pragma unroll
+          for (int k = 0; k < PPT; ++k) {
+            vb[k] = velocity(xb[k], vb[k], pb[k], gd, w, c1, c2, u01(r[k].c), u01(r[k].d));
+            xb[k] = clamp_lb_ub(__fadd_rn(xb[k], vb[k]), lo, hi);
+            acc[k].add(op, j + 1, xb[k]);
+          }
+          stv<PPT>(X + o, xb);
+          stv<PPT>(V + o, vb);
+        }
 #pragma unroll
         for (int k = 0; k < PPT; ++k) {
-          va[k] = velocity(xa[k], va[k], pa[k], gd, w, c1, c2, u01(r[k].a), u01(r[k].b));
-          xa[k] = clamp_lb_ub(__fadd_rn(xa[k], va[k]), lo, hi);
-          acc[k].add(op, j, xa[k]);
+          xa[k] = nxa[k]; va[k] = nva[k]; pa[k] = npa[k];
+          xb[k] = nxb[k]; vb[k] = nvb[k]; pb[k] = npb[k];
         }
-        stv<PPT>(X + o, xa);
-        stv<PPT>(V + o, va);
       }
-      if (j + 1 < D) {  // dim j + 1
-        const int64_t o = (int64_t)(j + 1) * npad + i0;
-        if (anyfl) {
-#pragma unroll
-          for (int k = 0; k < PPT; ++k) pb[k] = fl[k] ? xb[k] : pb[k];
-          stv<PPT>(P + o, pb);
-        }
-        const float gd = sg[j + 1], lo = slb[j + 1], hi = sub[j + 1];
-#pragma unroll
-        for (int k = 0; k < PPT; ++k) {
-          vb[k] = velocity(xb[k], vb[k], pb[k], gd, w, c1, c2, u01(r[k].c), u01(r[k].d));
-          xb[k] = clamp_lb_ub(__fadd_rn(xb[k], vb[k]), lo, hi);
-          acc[k].add(op, j + 1, xb[k]);
-        }
-        stv<PPT>(X + o, xb);
-        stv<PPT>(V + o, vb);
-      }
+      float pc[PPT], cc[PPT];
+      ldv<PPT>(pc, s.pcost + i0);
 #pragma unroll
       for (int k = 0; k < PPT; ++k) {
-        xa[k] = nxa[k]; va[k] = nva[k]; pa[k] = npa[k];
-        xb[k] = nxb[k]; vb[k] = nvb[k]; pb[k] = npb[k];
+        cc[k] = finalize<OBJ>(op, acc[k].s1, acc[k].s2);
+        const bool valid = i0 + k < n;
+        // if cost < best_cost: best = position (strict <, src/kernels.jl:21-24)
+        fl[k] = (valid && cc[k] < pc[k]) ? 1 : 0;
+        pc[k] = fl[k] ? cc[k] : pc[k];
+        if (valid) {
+          const unsigned long long key = argmin_key(pc[k], (uint32_t)(i0 + k));
+          best = key < best ? key : best;
+        }
       }
+      stv<PPT>(s.pcost + i0, pc);
+      stv<PPT>(s.cost + i0, cc);
+      stflags<PPT>(s.flag + i0, fl);
     }
-    float pc[PPT], cc[PPT];
-    ldv<PPT>(pc, s.pcost + i0);
-#pragma unroll
-    for (int k = 0; k < PPT; ++k) {
-      cc[k] = finalize<OBJ>(op, acc[k].s1, acc[k].s2);
-      const bool valid = i0 + k < n;
-      // if cost < best_cost: best = position (strict <, src/kernels.jl:21-24)
-      fl[k] = (valid && cc[k] < pc[k]) ? 1 : 0;
-      pc[k] = fl[k] ? cc[k] : pc[k];
-      if (valid) {
-        const unsigned long long key = argmin_key(pc[k], (uint32_t)(i0 + k));
-        best = key < best ? key : best;
-      }
-    }
-    stv<PPT>(s.pcost + i0, pc);
-    stv<PPT>(s.cost + i0, cc);
-    stflags<PPT>(s.flag + i0, fl);
+    __syncthreads();  // s_tile[slot ^ 1] written; s_tile[slot] free for the grab after next
   }
   if (publish_block_min(best, st)) {
     finish_iteration(s, from_position != 0, t + 1u, __fmul_rn(w, st->wdamp));
@@ -228,6 +240,7 @@ __global__ void k_materialize(SwarmDev s) {
 }
 
 __global__ void k_set_iter(IterState* st, uint32_t t, float w, float wdamp) {
+  st->tile_next = 0u;
   st->key = ~0ull;
   st->count = 0u;
   st->t = t;
@@ -305,7 +318,7 @@ static int occupancy_of(int ppt, size_t smem) {
 }
 
 int sync_grid(pps_swarm* s) {
-  // resident blocks across the GPU, at most one per 32-particle chunk
+  // resident blocks of the step kernel per SM (cached per objective, device, dim)
   static thread_local int cached_obj = -1, cached_blocks = 0, cached_dev = -1, cached_dim = -1;
   int per_sm = 0;
   if (cached_obj == s->objective && cached_dev == s->device && cached_dim == s->dv.dim) {
@@ -326,31 +339,27 @@ int sync_grid(pps_swarm* s) {
     cached_dev = s->device;
     cached_dim = s->dv.dim;
   }
-  // tiles of kSyncThreads x PPT particles, the same number per block
+  // every resident block, at most one per tile; blocks take tiles dynamically
   const int64_t resident = (int64_t)per_sm * s->sm_count;
   const int64_t tile = (int64_t)kSyncThreads * sync_ppt();
   const int64_t ntiles = (s->dv.npad + tile - 1) / tile;
-  int64_t passes = (ntiles + resident - 1) / resident;
-  if (passes < 1) passes = 1;
-  int64_t grid = (ntiles + passes - 1) / passes;
+  int64_t grid = resident < ntiles ? resident : ntiles;
   if (grid < 1) grid = 1;
-  s->sync_passes = (int)passes;
   return (int)grid;
 }
 
 int launch_sync_step(pps_swarm* s, float c1, float c2) {
   const int grid = sync_grid(s);
-  const int passes = s->sync_passes;
   const size_t smem = 3 * sizeof(float) * (size_t)s->dv.dim;
   const int from_pos = (s->flags & PPS_FLAG_GBEST_FROM_POSITION) ? 1 : 0;
   const int ppt = sync_ppt();
 #define L_STEP(O)                                                                                       \
   if (ppt == 4)                                                                                         \
-    k_sync_step<O, 4><<<grid, kSyncThreads, smem, s->stream>>>(s->dv, s->op, s->seed, c1, c2, from_pos, passes); \
+    k_sync_step<O, 4><<<grid, kSyncThreads, smem, s->stream>>>(s->dv, s->op, s->seed, c1, c2, from_pos); \
   else if (ppt == 2)                                                                                    \
-    k_sync_step<O, 2><<<grid, kSyncThreads, smem, s->stream>>>(s->dv, s->op, s->seed, c1, c2, from_pos, passes); \
+    k_sync_step<O, 2><<<grid, kSyncThreads, smem, s->stream>>>(s->dv, s->op, s->seed, c1, c2, from_pos); \
   else                                                                                                  \
-    k_sync_step<O, 1><<<grid, kSyncThreads, smem, s->stream>>>(s->dv, s->op, s->seed, c1, c2, from_pos, passes)
+    k_sync_step<O, 1><<<grid, kSyncThreads, smem, s->stream>>>(s->dv, s->op, s->seed, c1, c2, from_pos)
   PPS_DISPATCH_SEPARABLE(s->objective, L_STEP)
 #undef L_STEP
   PPS_CUDA(cudaGetLastError());
