@@ -363,7 +363,8 @@ def run_served(pps, args, with_mlp=True) -> dict:
     """The served mixed stream through the continuous-batching server: a
     closed-loop saturation run, a Poisson(2000/s) open-loop run, p50/p99 time
     to solution, against the same requests solved one at a time (plain)."""
-    cfg = dict(memory_budget=24 << 30, max_launches=16, max_pack=128, threads=256, ppt=2, tick_us=200.0)
+    cfg = dict(memory_budget=24 << 30, max_launches=32, max_pack=128, threads=256, ppt=2, tick_us=200.0,
+               single_min_n=2048)
     mix = "Rosenbrock, Rastrigin, Ackley, Lotka-Volterra fit" + (", MLP fit (577 parameters, 1024 samples)"
                                                                  if with_mlp else "")
     out = {"workload": f"mixed stream: objective U{{{mix}}}, dim U{{2..64}}, particles U{{256..16384}}, "

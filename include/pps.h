@@ -224,6 +224,11 @@ typedef struct pps_serve_config {
   int32_t ppt;            /* particles per thread (0: 1) */
   double tick_us;         /* while launches are in flight, the oldest queued request
                              waits at most this long for a fuller pack */
+  int32_t single_min_n;   /* requests with at least this many particles run as a swarm
+                             of their own with the multi-block step kernels, like a
+                             plain solve, instead of in a batched launch (0: 2048,
+                             negative: only MLP fits, which always do) */
+  int32_t reserved;
 } pps_serve_config;
 typedef struct pps_serve_stats {
   uint64_t submitted, completed, launches;

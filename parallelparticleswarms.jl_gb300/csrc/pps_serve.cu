@@ -2,12 +2,14 @@
 //
 // The reference has no serving layer: each solve() owns the device for its
 // duration.  This server admits optimization problems as they arrive and
-// solves them in the batched kernel (one CTA or cluster per swarm,
-// pps_batch.cu); MLP-fit requests, whose loss runs on the tensor cores with
-// one CTA per SM and tile (pps_mlp.cu), run instead as a swarm of their own on
-// a launch slot (state carved from the same arena, iterations replayed as a
-// CUDA graph, the result written to the request's mailbox by a last kernel),
-// concurrently with the batched launches on the other slots:
+// solves small swarms in the batched kernel (one CTA or cluster per swarm,
+// all iterations in one launch, pps_batch.cu).  Large swarms (at least
+// `single_min_n` particles) and MLP fits, whose loss runs on the tensor cores
+// with one CTA per SM and tile (pps_mlp.cu), run instead as a swarm of their
+// own on a launch slot with the multi-block step kernels of a plain solve
+// (state carved from the same arena, iterations replayed as a CUDA graph, the
+// result written to the request's mailbox by a last kernel), concurrently
+// with the batched launches on the other slots:
 //
 //   submit()  validates the problem, stamps the arrival time and queues it.
 //   worker    one host thread that, in a loop,
@@ -384,6 +386,7 @@ int pps_serve_start(const pps_serve_config* cfg_in, pps_server** out) {
   if (cfg.threads == 0) cfg.threads = 256;
   if (cfg.ppt == 0) cfg.ppt = 1;
   if (cfg.tick_us < 0) cfg.tick_us = 0;
+  if (cfg.single_min_n == 0) cfg.single_min_n = 2048;
   if (cfg.max_launches > 64 || cfg.max_pack > kMaxPack)
     return set_error(PPS_EINVAL, "max_launches <= 64 and max_pack <= %d", kMaxPack);
   if (!(cfg.threads == 128 || cfg.threads == 256 || cfg.threads == 512) ||
@@ -429,9 +432,14 @@ int pps_serve_submit(pps_server* s, const pps_problem* prob, int64_t n, uint64_t
   if (!s || !ticket) return set_error(PPS_EINVAL, "NULL argument");
   Request* r = new (std::nothrow) Request();
   if (!r) return set_error(PPS_ENOMEM, "host allocation failed");
-  if (prob && prob->objective == kMlp) {
-    // solved as a swarm of its own (the tensor-core kernel wants whole SMs)
+  // MLP fits (the tensor-core kernel wants whole SMs) and large swarms run as
+  // a swarm of their own with the multi-block step kernels; the rest are
+  // packed into batched launches
+  const bool single = prob && (prob->objective == kMlp || (s->cfg.single_min_n > 0 && n >= s->cfg.single_min_n));
+  if (single) {
     int rc = swarm_check(prob, n);
+    if (!rc && prob->dim > kBatchMaxDim)
+      rc = set_error(PPS_EINVAL, "served problems have at most %d dims (got %d)", kBatchMaxDim, prob->dim);
     if (!rc && maxiters < 0) rc = set_error(PPS_EINVAL, "maxiters must be >= 0");
     if (!rc && !(std::isfinite(w) && std::isfinite(wdamp) && std::isfinite(c1) && std::isfinite(c2)))
       rc = set_error(PPS_EINVAL, "coefficients must be finite");
@@ -447,13 +455,14 @@ int pps_serve_submit(pps_server* s, const pps_problem* prob, int64_t n, uint64_t
       r->host[D + d] = prob->ub ? prob->ub[d] : INFINITY;
       r->host[2 * D + d] = prob->u0 ? prob->u0[d] : 0.0f;
     }
-    memcpy(r->host.data() + 3 * D, prob->data, sizeof(float) * (size_t)prob->ndata);
+    if (prob->data && prob->ndata > 0) memcpy(r->host.data() + 3 * D, prob->data, sizeof(float) * (size_t)prob->ndata);
     for (int k = 0; k < prob->nparams; ++k) r->params[k] = prob->params[k];
     r->prob = *prob;
     r->prob.lb = r->host.data();
     r->prob.ub = r->host.data() + D;
     r->prob.u0 = r->host.data() + 2 * D;
-    r->prob.data = r->host.data() + 3 * D;
+    r->prob.data = (prob->data && prob->ndata > 0) ? r->host.data() + 3 * D : nullptr;
+    r->prob.ndata = (prob->data && prob->ndata > 0) ? prob->ndata : 0;
     r->prob.params = r->params;
     r->n = n;
     r->seed = seed;

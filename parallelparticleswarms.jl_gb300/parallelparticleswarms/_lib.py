@@ -85,6 +85,8 @@ class ServeConfig(ctypes.Structure):
         ("threads", ctypes.c_int32),
         ("ppt", ctypes.c_int32),
         ("tick_us", ctypes.c_double),
+        ("single_min_n", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
     ]
 
 

@@ -81,6 +81,20 @@ def test_mlp_fits_served_beside_batched_requests(pps):
         assert i == ai and np.float32(c) == np.float32(ac) and np.array_equal(u, au)
 
 
+def test_large_requests_run_as_swarms_of_their_own(pps):
+    """Requests at or above single_min_n particles take the multi-block step
+    kernels of a plain solve on a launch slot, the others the batched kernel;
+    both kinds of result equal the problem solved alone."""
+    reqs = _stream(pps, 16, seed=9, objectives=NO_MLP)
+    assert any(n >= 128 for _, n, _, _ in reqs) and any(n < 128 for _, n, _, _ in reqs)
+    with pps.Server(memory_budget=1 << 30, max_launches=6, max_pack=16, tick_us=50.0, single_min_n=128) as srv:
+        tickets = [srv.submit(p, n, maxiters=it, seed=s) for (p, n, it, s) in reqs]
+        results = [srv.wait(t) for t in tickets]
+    for (prob, n, iters, s), (u, c, i, lat) in zip(reqs, results):
+        au, ac, ai = _alone(pps, prob, n, iters, s)
+        assert i == ai and np.float32(c) == np.float32(ac) and np.array_equal(u, au)
+
+
 def test_poll_and_errors(pps):
     reqs = _stream(pps, 1, seed=5, objectives=NO_MLP)
     prob, n, iters, s = reqs[0]
