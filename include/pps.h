@@ -58,6 +58,8 @@ typedef enum pps_objective {
   PPS_OBJ_LV_FIT = 4,     /* SSE of an RK4 Lotka-Volterra solve vs observations (data) */
   PPS_OBJ_FHN_FIT = 5,    /* SSE of an RK4 FitzHugh-Nagumo solve vs observations (data) */
   PPS_OBJ_MLP = 6,        /* MSE of a 2-layer tanh MLP on a sample set (data) */
+  PPS_OBJ_SHIFTED_SPHERE = 7, /* sum (x_i - p_i)^2, p_i = 0 past nparams: the objective of the
+                                 reference's constraint test (test/constraints.jl:7) */
   /* the closed-form objectives of the reference's L-BFGS tests (test/lbfgs.jl:20-26) */
   PPS_OBJ_BEALE = 16,
   PPS_OBJ_BOOTH = 17,
@@ -77,6 +79,14 @@ typedef struct pps_problem {
   int32_t nparams;
   const float* data;     /* objective data (observations / samples), may be NULL */
   int64_t ndata;         /* floats in data */
+  /* Constraints g_k(x) <= 0 (OptimizationFunction(f; cons) with lcons = -Inf, ucons = 0),
+   * handled by the reference's penalty calc_penalty (src/utils.jl:320-372, h = sqrt,
+   * theta_default, gamma_default) in init and the sync / queue-lock steps.  A C ABI takes
+   * no Julia closure, so each constraint has the registered form
+   *   g_k(x) = c_k + sum_i a_ki x_i + b_ki x_i^2,
+   * cons = ncons rows of (c_k, a_k[dim], b_k[dim]) floats, 0 <= ncons <= 4. */
+  int32_t ncons;
+  const float* cons;
 } pps_problem;
 
 typedef struct pps_swarm pps_swarm;

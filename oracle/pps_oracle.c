@@ -215,6 +215,12 @@ static void slice_sums(const orc_problem* prob, const float* x, int64_t stride, 
       }
       break;
     }
+    case ORC_OBJ_SHIFTED_SPHERE:
+      for (int d = d0; d < d1; ++d) {
+        float t = x[d * stride] - prm(prob, d, 0.0f);
+        a1 = a1 + t * t;
+      }
+      break;
     case ORC_OBJ_ACKLEY: {
       float k = prm(prob, 2, 1.0f);
       for (int d = d0; d < d1; ++d) {
@@ -235,6 +241,35 @@ static void slice_sums(const orc_problem* prob, const float* x, int64_t stride, 
 }
 
 static inline float sq(float a) { return a * a; }
+
+/* theta_default / gamma_default (src/utils.jl:320-338).  The reference
+ * compares a Float32 with the Float64 literals 0.001 and 0.1; no binary32
+ * lies in [0.001, 0.001f) or in (0.1, 0.1f), so q < 0.001 is q < 0.001f and
+ * q <= 0.1 is q < 0.1f. */
+static inline float theta_default(float q) {
+  return q < 0.001f ? 10.0f : (q < 0.1f ? 20.0f : (q <= 1.0f ? 100.0f : 300.0f));
+}
+
+float orc_penalty(const orc_problem* prob, const float* x, int64_t stride, float iter) {
+  const int D = prob->dim;
+  float q[4];
+  for (int k = 0; k < prob->ncons; ++k) {
+    const float* row = prob->cons + (int64_t)k * (1 + 2 * D);
+    float g = row[0];
+    for (int d = 0; d < D; ++d) {
+      const float xi = x[d * stride];
+      g = g + ((row[1 + d] * xi) + (row[1 + D + d] * (xi * xi)));
+    }
+    q[k] = (g < 0.0f) ? 0.0f : g; /* max.(cons, 0), NaN kept */
+  }
+  float pen = 0.0f; /* sum(thetaq) */
+  for (int k = 0; k < prob->ncons; ++k) pen = pen + theta_default(q[k]);
+  for (int k = 0; k < prob->ncons; ++k) {
+    const float pw = (q[k] < 1.0f) ? q[k] : q[k] * q[k]; /* q^gamma_default(q) */
+    pen = pen + theta_default(q[k]) * pw;
+  }
+  return sqrtf(iter) * pen; /* h = sqrt */
+}
 
 /* closed-form objectives of test/lbfgs.jl:20-26 from (x1, x2) */
 static float closed_form(const orc_problem* prob, float x1, float x2) {
@@ -457,6 +492,7 @@ void orc_init(const orc_problem* prob, orc_swarm* s, uint64_t seed, int32_t samp
       }
     }
     float c = orc_objective(prob, s->x + i, n, 1);
+    if (prob->ncons > 0) c = c + orc_penalty(prob, s->x + i, n, 1.0f);
     s->cost[i] = c;
     s->pcost[i] = c;
   }
@@ -531,6 +567,8 @@ static void sync_worker(void* a_, int tid, int nth) {
     update_dims(a->prob, s->x + i, s->v + i, s->pbest + i, s->g, n, (uint32_t)i, a->t, a->seed,
                 a->w, a->c1, a->c2);
     float c = orc_objective(a->prob, s->x + i, n, 1);
+    /* the sync step passes the 1-based particle index as iter (src/kernels.jl:151) */
+    if (a->prob->ncons > 0) c = c + orc_penalty(a->prob, s->x + i, n, (float)(i + 2));
     s->cost[i] = c;
     if (c < s->pcost[i]) {
       s->pcost[i] = c;

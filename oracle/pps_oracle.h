@@ -59,6 +59,7 @@ enum {
   ORC_OBJ_LV_FIT = 4,   /* SSE of an RK4 Lotka-Volterra solve vs data */
   ORC_OBJ_FHN_FIT = 5,  /* SSE of an RK4 FitzHugh-Nagumo solve vs data */
   ORC_OBJ_MLP = 6,      /* MLP regression loss (16 -> 32 tanh -> 1, MSE) */
+  ORC_OBJ_SHIFTED_SPHERE = 7, /* sum (x_i - p_i)^2, p_i = 0 past nparams (test/constraints.jl:7) */
   /* closed-form objectives of the reference's L-BFGS tests (test/lbfgs.jl:20-26) */
   ORC_OBJ_BEALE = 16,
   ORC_OBJ_BOOTH = 17,
@@ -81,6 +82,10 @@ typedef struct orc_problem {
   const struct orc_ode_fit* ode;  /* ORC_OBJ_LV_FIT / ORC_OBJ_FHN_FIT only */
   const float* mlp_data;          /* ORC_OBJ_MLP: S x 16 samples then S targets */
   int32_t mlp_samples;
+  /* constraints g_k(x) <= 0, k < ncons <= 4, each c_k + sum_i a_ki x_i + b_ki x_i^2:
+   * cons = ncons rows of (c_k, a_k[dim], b_k[dim]) */
+  int32_t ncons;
+  const float* cons;
 } orc_problem;
 
 /* structure-of-arrays swarm state: x[d*n + i] */
@@ -110,6 +115,12 @@ uint64_t orc_argmin_key(float cost, uint32_t idx);
  * even length, each summed in order, the slice sums combined by a balanced
  * pairwise tree (lanes a power of two, 1 = plain sequential sum). */
 float orc_objective(const orc_problem* prob, const float* x, int64_t stride, int32_t lanes);
+/* calc_penalty (src/utils.jl:320-372) for the registered constraint form at x
+ * (stride `stride`), with h = sqrt and the weight's argument `iter`: 1 at init
+ * (src/utils.jl:72-74), particle index + 1 (1-based) in the sync and
+ * queue-lock steps (src/kernels.jl:77,151 pass the index as `iter`,
+ * handle_constraints adds 1, :28-31).  0 without constraints. */
+float orc_penalty(const orc_problem* prob, const float* x, int64_t stride, float iter);
 /* analytic gradient (Rosenbrock, Rastrigin, Ackley, sphere), sequential sums */
 float orc_objective_grad(const orc_problem* prob, const float* x, float* grad);
 

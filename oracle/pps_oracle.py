@@ -35,7 +35,8 @@ class OdeFit(ctypes.Structure):
 class Problem(ctypes.Structure):
     _fields_ = [("objective", ctypes.c_int32), ("dim", ctypes.c_int32), ("lb", _fp), ("ub", _fp),
                 ("u0", _fp), ("params", ctypes.c_float * 8), ("nparams", ctypes.c_int32),
-                ("ode", ctypes.POINTER(OdeFit)), ("mlp_data", _fp), ("mlp_samples", ctypes.c_int32)]
+                ("ode", ctypes.POINTER(OdeFit)), ("mlp_data", _fp), ("mlp_samples", ctypes.c_int32),
+                ("ncons", ctypes.c_int32), ("cons", _fp)]
 
 
 class SwarmC(ctypes.Structure):
@@ -70,6 +71,8 @@ def load() -> ctypes.CDLL:
             getattr(L, name).argtypes = [ctypes.c_float]
         L.orc_objective.restype = ctypes.c_float
         L.orc_objective.argtypes = [ctypes.POINTER(Problem), _fp, ctypes.c_int64, ctypes.c_int32]
+        L.orc_penalty.restype = ctypes.c_float
+        L.orc_penalty.argtypes = [ctypes.POINTER(Problem), _fp, ctypes.c_int64, ctypes.c_float]
         L.orc_objective_grad.restype = ctypes.c_float
         L.orc_objective_grad.argtypes = [ctypes.POINTER(Problem), _fp, _fp]
         L.orc_init.argtypes = [ctypes.POINTER(Problem), ctypes.POINTER(SwarmC), ctypes.c_uint64, ctypes.c_int32]
@@ -130,7 +133,8 @@ def default_threads() -> int:
 class OracleProblem:
     """orc_problem over numpy buffers (objective ids are include/pps.h's)."""
 
-    def __init__(self, objective: int, dim: int, lb=None, ub=None, u0=None, params=(), ode=None, mlp_data=None):
+    def __init__(self, objective: int, dim: int, lb=None, ub=None, u0=None, params=(), ode=None, mlp_data=None,
+                 cons=None):
         self.dim = int(dim)
         self.lb = np.ascontiguousarray(np.full(dim, -np.inf, np.float32) if lb is None else np.asarray(lb, np.float32))
         self.ub = np.ascontiguousarray(np.full(dim, np.inf, np.float32) if ub is None else np.asarray(ub, np.float32))
@@ -146,6 +150,11 @@ class OracleProblem:
         self.ode = ode
         if ode is not None:
             self.c.ode = ctypes.pointer(ode.c)
+        self.cons = None
+        if cons is not None:  # (ncons, 1 + 2 dim): c_k, a_k, b_k of g_k(x) = c_k + a_k . x + b_k . x^2 <= 0
+            self.cons = np.ascontiguousarray(np.asarray(cons, np.float32).reshape(-1, 1 + 2 * self.dim))
+            self.c.ncons = self.cons.shape[0]
+            self.c.cons = fp(self.cons)
         self.mlp_data = None
         if mlp_data is not None:  # S x 16 samples followed by S targets
             self.mlp_data = np.ascontiguousarray(np.asarray(mlp_data, np.float32).reshape(-1))
@@ -155,6 +164,10 @@ class OracleProblem:
     def objective(self, x, lanes: int = 1) -> float:
         x = np.ascontiguousarray(np.asarray(x, np.float32))
         return float(load().orc_objective(ctypes.byref(self.c), fp(x), 1, lanes))
+
+    def penalty(self, x, iter: float) -> float:
+        x = np.ascontiguousarray(np.asarray(x, np.float32))
+        return float(load().orc_penalty(ctypes.byref(self.c), fp(x), 1, float(iter)))
 
     def objective_grad(self, x):
         x = np.ascontiguousarray(np.asarray(x, np.float32))

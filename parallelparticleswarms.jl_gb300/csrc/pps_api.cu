@@ -49,6 +49,7 @@ static bool supported_objective(int obj) {
     case kLvFit:
     case kFhnFit:
     case kMlp:
+    case kShiftedSphere:
       return true;
     default:
       return false;
@@ -73,6 +74,15 @@ static int check_problem(const pps_problem* prob) {
   if (prob->objective == kMlp) {
     const int rc = mlp_check(prob);
     if (rc) return rc;
+  }
+  if (prob->ncons < 0 || prob->ncons > kMaxCons)
+    return set_error(PPS_EINVAL, "ncons must be in [0, %d] (got %d)", kMaxCons, prob->ncons);
+  if (prob->ncons > 0) {
+    if (!prob->cons) return set_error(PPS_EINVAL, "cons is NULL");
+    if (is_ode(prob->objective) || prob->objective == kMlp)
+      return set_error(PPS_ENOTSUP, "constraints apply to the registered closed-form objectives only");
+    for (int64_t k = 0; k < (int64_t)prob->ncons * (1 + 2 * (int64_t)prob->dim); ++k)
+      if (!std::isfinite(prob->cons[k])) return set_error(PPS_EINVAL, "constraint coefficients must be finite");
   }
   for (int d = 0; d < prob->dim; ++d) {
     const float lo = prob->lb ? prob->lb[d] : -INFINITY;
@@ -123,7 +133,7 @@ namespace pps {
 
 // One device block per swarm, carved into 256-byte-aligned arrays.
 struct SwarmLayout {
-  size_t oX, oV, oP, oPc, oC, oF, oG, oLb, oUb, oU0, oSt, oData, oMlpA, bytes;
+  size_t oX, oV, oP, oPc, oC, oF, oG, oLb, oUb, oU0, oSt, oData, oMlpA, oCons, bytes;
   int64_t npad;
   int mlp_samples;
 };
@@ -152,6 +162,7 @@ static SwarmLayout swarm_layout(const pps_problem* prob, int64_t n) {
   L.oData = take(sizeof(float) * (prob->data ? (size_t)prob->ndata : 0));
   L.mlp_samples = prob->objective == kMlp ? (int)(prob->ndata / 17) : 0;
   L.oMlpA = take(L.mlp_samples ? mlp_a_bytes(L.mlp_samples) : 0);
+  L.oCons = take(sizeof(float) * (size_t)(prob->ncons > 0 ? prob->ncons : 0) * (1 + 2 * (size_t)D));
   L.bytes = off;
   return L;
 }
@@ -191,6 +202,8 @@ static int swarm_setup(pps_swarm* s, const pps_problem* prob, int64_t n, uint64_
   s->dv.n = n;
   s->dv.npad = L.npad;
   s->dv.dim = D;
+  s->dv.ncons = prob->ncons > 0 ? prob->ncons : 0;
+  s->dv.cons = s->dv.ncons ? reinterpret_cast<const float*>(b + L.oCons) : nullptr;
   s->op = make_params(prob);
   s->objective = prob->objective;
   s->seed = seed;
@@ -211,6 +224,9 @@ static int swarm_setup(pps_swarm* s, const pps_problem* prob, int64_t n, uint64_
   if (prob->data && prob->ndata > 0)
     PPS_CUDA(cudaMemcpyAsync(s->data_dev, prob->data, sizeof(float) * (size_t)prob->ndata, cudaMemcpyHostToDevice,
                              s->stream));
+  if (s->dv.ncons)
+    PPS_CUDA(cudaMemcpyAsync(b + L.oCons, prob->cons, sizeof(float) * (size_t)s->dv.ncons * (1 + 2 * (size_t)D),
+                             cudaMemcpyHostToDevice, s->stream));
   if (L.mlp_samples) {
     std::vector<uint8_t> packed(mlp_a_bytes(L.mlp_samples));
     mlp_pack_a(prob->data, L.mlp_samples, packed.data());
@@ -490,6 +506,8 @@ int pps_async_run(pps_swarm* s, int32_t maxiters, float w, float wdamp, float c1
     return set_error(PPS_ENOTSUP, "ODE fits run synchronously (parameter_estim_ode!); use pps_sync_run");
   if (s->objective == kMlp)
     return set_error(PPS_ENOTSUP, "the MLP objective runs synchronously (tensor-core evaluation); use pps_sync_run");
+  if (s->dv.ncons > 0)
+    return set_error(PPS_ENOTSUP, "constrained problems run with pps_sync_run / pps_queue_run");
   if ((rc = launch_set_iter(s, s->t, w, wdamp))) return rc;
   PPS_CUDA(cudaEventRecord(s->ev0, s->stream));
   int lanes = 0;

@@ -225,6 +225,7 @@ int launch_async(pps_swarm* s, int iters, float c1, float c2, int* lanes_out) {
     case kHimmelblau: return launch_async_obj<kHimmelblau>(s, iters, c1, c2, lanes, slice);
     case kQuadratic: return launch_async_obj<kQuadratic>(s, iters, c1, c2, lanes, slice);
     case kBoundaryQuadratic: return launch_async_obj<kBoundaryQuadratic>(s, iters, c1, c2, lanes, slice);
+    case kShiftedSphere: return launch_async_obj<kShiftedSphere>(s, iters, c1, c2, lanes, slice);
     default: return set_error(PPS_ENOTSUP, "objective %d has no async kernel", s->objective);
   }
 }

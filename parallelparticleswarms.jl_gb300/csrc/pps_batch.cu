@@ -541,6 +541,8 @@ int batch_describe(const pps_problem* prob, int64_t n, uint64_t seed, int32_t ma
     return set_error(PPS_ENOTSUP, "objective %d is not supported in batches", obj);
   if (prob->dim < 1 || prob->dim > kBatchMaxDim)
     return set_error(PPS_EINVAL, "batched swarms have 1 <= dim <= %d (got %d)", kBatchMaxDim, prob->dim);
+  if (prob->ncons != 0)
+    return set_error(PPS_ENOTSUP, "constrained problems are solved as swarms of their own, not in batches");
   if (n < 1 || n > kBatchMaxParticles)
     return set_error(PPS_EINVAL, "batched swarms have 1 <= n <= %lld (got %lld)", (long long)kBatchMaxParticles,
                      (long long)n);

@@ -34,6 +34,7 @@ enum Objective : int {
   kLvFit = 4,
   kFhnFit = 5,
   kMlp = 6,
+  kShiftedSphere = 7,
   kBeale = 16,
   kBooth = 17,
   kHimmelblau = 18,
@@ -131,6 +132,57 @@ __device__ __forceinline__ float exp_f(float x) {
   return __fmul_rn(p, __int_as_float((ki + 127) << 23));
 }
 
+// ---------------------------------------------------------------- constraints
+// calc_penalty (src/utils.jl:320-372) for the registered constraint form
+// g_k(x) = c_k + sum_i a_ki x_i + b_ki x_i^2 (rows of `cons`: c_k, a_k[dim],
+// b_k[dim]).  ConsAcc streams the dims like Acc; penalty() turns the k
+// constraint values into h(iter) (sum theta(q) + sum theta(q) q^gamma(q)),
+// q = max.(g, 0), h = sqrt, theta_default / gamma_default (:320-338).  The
+// reference compares a Float32 with the Float64 literals 0.001 and 0.1; no
+// binary32 lies in [0.001, 0.001f) or in (0.1, 0.1f), so q < 0.001 is
+// q < 0.001f and q <= 0.1 is q < 0.1f.
+constexpr int kMaxCons = 4;
+
+struct ConsAcc {
+  float g[kMaxCons];
+  __device__ __forceinline__ void start(const float* __restrict__ cons, int ncons, int dim) {
+#pragma unroll
+    for (int k = 0; k < kMaxCons; ++k) g[k] = (k < ncons) ? cons[(size_t)k * (1 + 2 * dim)] : 0.0f;
+  }
+  __device__ __forceinline__ void add(const float* __restrict__ cons, int ncons, int dim, int d, float x) {
+    const float x2 = __fmul_rn(x, x);
+#pragma unroll
+    for (int k = 0; k < kMaxCons; ++k) {
+      if (k < ncons) {
+        const float* row = cons + (size_t)k * (1 + 2 * dim);
+        g[k] = __fadd_rn(g[k], __fadd_rn(__fmul_rn(__ldg(row + 1 + d), x), __fmul_rn(__ldg(row + 1 + dim + d), x2)));
+      }
+    }
+  }
+};
+
+__device__ __forceinline__ float theta_default(float q) {
+  return q < 0.001f ? 10.0f : (q < 0.1f ? 20.0f : (q <= 1.0f ? 100.0f : 300.0f));
+}
+
+__device__ __forceinline__ float penalty(const ConsAcc& a, int ncons, float iter) {
+  float q[kMaxCons];
+#pragma unroll
+  for (int k = 0; k < kMaxCons; ++k) q[k] = (a.g[k] < 0.0f) ? 0.0f : a.g[k];  // max.(g, 0), NaN kept
+  float pen = 0.0f;
+#pragma unroll
+  for (int k = 0; k < kMaxCons; ++k)
+    if (k < ncons) pen = __fadd_rn(pen, theta_default(q[k]));
+#pragma unroll
+  for (int k = 0; k < kMaxCons; ++k) {
+    if (k < ncons) {
+      const float pw = (q[k] < 1.0f) ? q[k] : __fmul_rn(q[k], q[k]);  // q^gamma_default(q)
+      pen = __fadd_rn(pen, __fmul_rn(theta_default(q[k]), pw));
+    }
+  }
+  return __fmul_rn(__fsqrt_rn(iter), pen);
+}
+
 // orderable image of a cost (NaN above +inf) packed with the particle index:
 // the minimum key is the lowest cost, lowest index on ties.
 __device__ __forceinline__ unsigned long long argmin_key(float c, uint32_t idx) {
@@ -193,6 +245,9 @@ struct Acc {
     } else if constexpr (OBJ == kAckley) {
       s1 = __fadd_rn(s1, __fmul_rn(x, x));
       s2 = __fadd_rn(s2, cos2pi(__fmul_rn(prm(o, 2, 1.0f), x)));
+    } else if constexpr (OBJ == kShiftedSphere) {
+      const float t = __fsub_rn(x, prm(o, d, 0.0f));  // test/constraints.jl:7
+      s1 = __fadd_rn(s1, __fmul_rn(t, t));
     } else if constexpr (OBJ == kMlp) {
       // evaluated by the tensor-core kernel after the position update
     } else {

@@ -52,6 +52,8 @@ struct SwarmDev {
   int64_t n;
   int64_t npad;
   int dim;
+  int ncons;          // constraints of the penalty path (0: none)
+  const float* cons;  // ncons rows of (c_k, a_k[dim], b_k[dim])
 };
 
 struct ObjData {

@@ -131,7 +131,7 @@ extern "C" int pps_sync_run_noalloc(int32_t objective, const float* params, int3
   }
   switch (objective) {
     case kSphere: case kRosenbrock: case kRastrigin: case kAckley: case kBeale: case kBooth:
-    case kHimmelblau: case kQuadratic: case kBoundaryQuadratic:
+    case kHimmelblau: case kQuadratic: case kBoundaryQuadratic: case kShiftedSphere:
       break;
     default:
       return set_error(PPS_ENOTSUP, "objective %d is not supported by pps_sync_run_noalloc", objective);

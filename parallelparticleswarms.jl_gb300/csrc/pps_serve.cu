@@ -435,7 +435,8 @@ int pps_serve_submit(pps_server* s, const pps_problem* prob, int64_t n, uint64_t
   // MLP fits (the tensor-core kernel wants whole SMs) and large swarms run as
   // a swarm of their own with the multi-block step kernels; the rest are
   // packed into batched launches
-  const bool single = prob && (prob->objective == kMlp || (s->cfg.single_min_n > 0 && n >= s->cfg.single_min_n));
+  const bool single = prob && (prob->objective == kMlp || prob->ncons > 0 ||
+                               (s->cfg.single_min_n > 0 && n >= s->cfg.single_min_n));
   if (single) {
     int rc = swarm_check(prob, n);
     if (!rc && prob->dim > kBatchMaxDim)

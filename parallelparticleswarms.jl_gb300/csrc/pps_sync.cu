@@ -29,7 +29,9 @@ namespace pps {
 constexpr int kSyncThreads = 256;
 
 // ------------------------------------------------------------------ init
-template <int OBJ>
+// CONS: the penalty of the constrained path is added to the cost
+// (src/utils.jl:72-74: calc_penalty with iter = 1 at init)
+template <int OBJ, bool CONS = false>
 __global__ void __launch_bounds__(kSyncThreads) k_init(SwarmDev s, ObjParams op, uint64_t seed,
                                                         int sampler, const float* __restrict__ u0) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -39,6 +41,8 @@ __global__ void __launch_bounds__(kSyncThreads) k_init(SwarmDev s, ObjParams op,
   if (i < s.npad) {
     const bool valid = i < s.n;
     Acc<OBJ> acc;
+    ConsAcc ca;
+    if constexpr (CONS) ca.start(s.cons, s.ncons, D);
     for (int j = 0; j < D; j += 4) {
       const Rand4 r = philox4x32_10((uint32_t)i, (uint32_t)(j >> 2), 0u, kTagInit, k0, k1);
       const uint32_t rr[4] = {r.a, r.b, r.c, r.d};
@@ -62,10 +66,14 @@ __global__ void __launch_bounds__(kSyncThreads) k_init(SwarmDev s, ObjParams op,
         s.V[o] = 0.0f;
         s.P[o] = x;
         acc.add(op, d, x);
+        if constexpr (CONS) ca.add(s.cons, s.ncons, D, d, x);
       }
     }
     if constexpr (OBJ != kMlp) {
-      const float c = valid ? finalize<OBJ>(op, acc.s1, acc.s2) : __int_as_float(0x7f800000);
+      float c = valid ? finalize<OBJ>(op, acc.s1, acc.s2) : __int_as_float(0x7f800000);
+      if constexpr (CONS) {
+        if (valid) c = __fadd_rn(c, penalty(ca, s.ncons, 1.0f));
+      }
       s.cost[i] = c;
       s.pcost[i] = c;
       s.flag[i] = 0;
@@ -90,7 +98,10 @@ __global__ void __launch_bounds__(kSyncThreads) k_init(SwarmDev s, ObjParams op,
 // while the current tile runs: blocks on busier SMs or farther from the
 // memory take fewer tiles, and all finish within about one tile of each
 // other.  A particle's arithmetic does not depend on which block takes it.
-template <int OBJ, int PPT>
+// CONS: the constrained path (PPT = 1 only): the cost adds calc_penalty with
+// iter = the 1-based particle index, as the reference's sync and queue-lock
+// kernels pass it (src/kernels.jl:77,151; handle_constraints adds 1, :28-31).
+template <int OBJ, int PPT, bool CONS = false>
 __global__ void __launch_bounds__(kSyncThreads, (PPT == 4 ? 2 : (PPT == 2 ? 3 : 4)))
     k_sync_step(SwarmDev s, ObjParams op, uint64_t seed, float c1, float c2, int from_position) {
   extern __shared__ float sm[];
@@ -135,6 +146,11 @@ __global__ void __launch_bounds__(kSyncThreads, (PPT == 4 ? 2 : (PPT == 2 ? 3 : 
 #pragma unroll
       for (int k = 0; k < PPT; ++k) anyfl |= (fl[k] != 0);
       Acc<OBJ> acc[PPT];
+      ConsAcc ca[PPT];
+      if constexpr (CONS) {
+#pragma unroll
+        for (int k = 0; k < PPT; ++k) ca[k].start(s.cons, s.ncons, D);
+      }
       // current pair (dims j, j+1) and the prefetched next pair
       float xa[PPT], va[PPT], pa[PPT], xb[PPT], vb[PPT], pb[PPT];
       ldv<PPT>(xa, X + i0);
@@ -175,6 +191,7 @@ __global__ void __launch_bounds__(kSyncThreads, (PPT == 4 ? 2 : (PPT == 2 ? 3 : 
             va[k] = velocity(xa[k], va[k], pa[k], gd, w, c1, c2, u01(r[k].a), u01(r[k].b));
             xa[k] = clamp_lb_ub(__fadd_rn(xa[k], va[k]), lo, hi);
             acc[k].add(op, j, xa[k]);
+            if constexpr (CONS) ca[k].add(s.cons, s.ncons, D, j, xa[k]);
           }
           stv<PPT>(X + o, xa);
           stv<PPT>(V + o, va);
@@ -192,6 +209,7 @@ __global__ void __launch_bounds__(kSyncThreads, (PPT == 4 ? 2 : (PPT == 2 ? 3 : 
             vb[k] = velocity(xb[k], vb[k], pb[k], gd, w, c1, c2, u01(r[k].c), u01(r[k].d));
             xb[k] = clamp_lb_ub(__fadd_rn(xb[k], vb[k]), lo, hi);
             acc[k].add(op, j + 1, xb[k]);
+            if constexpr (CONS) ca[k].add(s.cons, s.ncons, D, j + 1, xb[k]);
           }
           stv<PPT>(X + o, xb);
           stv<PPT>(V + o, vb);
@@ -207,6 +225,7 @@ __global__ void __launch_bounds__(kSyncThreads, (PPT == 4 ? 2 : (PPT == 2 ? 3 : 
 #pragma unroll
       for (int k = 0; k < PPT; ++k) {
         cc[k] = finalize<OBJ>(op, acc[k].s1, acc[k].s2);
+        if constexpr (CONS) cc[k] = __fadd_rn(cc[k], penalty(ca[k], s.ncons, __uint2float_rn((uint32_t)(i0 + k + 2))));
         const bool valid = i0 + k < n;
         // if cost < best_cost: best = position (strict <, src/kernels.jl:21-24)
         fl[k] = (valid && cc[k] < pc[k]) ? 1 : 0;
@@ -265,6 +284,7 @@ __global__ void k_eval(ObjParams op, const float* __restrict__ x, int64_t npts, 
     case kSphere: MACRO(kSphere); break;   \
     case kRosenbrock: MACRO(kRosenbrock); break; \
     case kRastrigin: MACRO(kRastrigin); break;   \
+    case kShiftedSphere: MACRO(kShiftedSphere); break; \
     case kAckley: MACRO(kAckley); break;   \
     case kBeale: MACRO(kBeale); break;     \
     case kBooth: MACRO(kBooth); break;     \
@@ -277,11 +297,16 @@ __global__ void k_eval(ObjParams op, const float* __restrict__ x, int64_t npts, 
 int launch_init(pps_swarm* s, int sampler, const float* u0_dev) {
   const int64_t blocks = (s->dv.npad + kSyncThreads - 1) / kSyncThreads;
 #define L_INIT(O) k_init<O><<<(unsigned)blocks, kSyncThreads, 0, s->stream>>>(s->dv, s->op, s->seed, sampler, u0_dev)
+#define L_INIT_CONS(O) \
+  k_init<O, true><<<(unsigned)blocks, kSyncThreads, 0, s->stream>>>(s->dv, s->op, s->seed, sampler, u0_dev)
   if (s->objective == kMlp) {
     L_INIT(kMlp);
+  } else if (s->dv.ncons > 0) {
+    PPS_DISPATCH_SEPARABLE(s->objective, L_INIT_CONS)
   } else {
     PPS_DISPATCH_SEPARABLE(s->objective, L_INIT)
   }
+#undef L_INIT_CONS
 #undef L_INIT
   PPS_CUDA(cudaGetLastError());
   return PPS_OK;
@@ -360,7 +385,18 @@ int launch_sync_step(pps_swarm* s, float c1, float c2) {
     k_sync_step<O, 2><<<grid, kSyncThreads, smem, s->stream>>>(s->dv, s->op, s->seed, c1, c2, from_pos); \
   else                                                                                                  \
     k_sync_step<O, 1><<<grid, kSyncThreads, smem, s->stream>>>(s->dv, s->op, s->seed, c1, c2, from_pos)
-  PPS_DISPATCH_SEPARABLE(s->objective, L_STEP)
+  if (s->dv.ncons > 0) {
+    // constrained path: one particle per thread; tiles of 256 particles,
+    // handed out dynamically, so any grid up to 4 blocks per SM is right
+    const int64_t ntiles = (s->dv.npad + kSyncThreads - 1) / kSyncThreads;
+    const int64_t cgrid = ntiles < 4 * (int64_t)s->sm_count ? ntiles : 4 * (int64_t)s->sm_count;
+#define L_STEP_CONS(O) \
+  k_sync_step<O, 1, true><<<(unsigned)cgrid, kSyncThreads, smem, s->stream>>>(s->dv, s->op, s->seed, c1, c2, from_pos)
+    PPS_DISPATCH_SEPARABLE(s->objective, L_STEP_CONS)
+#undef L_STEP_CONS
+  } else {
+    PPS_DISPATCH_SEPARABLE(s->objective, L_STEP)
+  }
 #undef L_STEP
   PPS_CUDA(cudaGetLastError());
   return PPS_OK;

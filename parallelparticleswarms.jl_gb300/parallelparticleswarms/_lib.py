@@ -50,6 +50,8 @@ class Problem(ctypes.Structure):
         ("nparams", ctypes.c_int32),
         ("data", c_float_p),
         ("ndata", ctypes.c_int64),
+        ("ncons", ctypes.c_int32),
+        ("cons", c_float_p),
     ]
 
 

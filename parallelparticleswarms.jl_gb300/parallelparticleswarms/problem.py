@@ -35,6 +35,8 @@ ackley = Objective("ackley", 3, (20.0, 0.2, 1.0))
 lotka_volterra_fit = Objective("lotka_volterra_fit", 4)
 fitzhugh_nagumo_fit = Objective("fitzhugh_nagumo_fit", 5)
 mlp_regression = Objective("mlp_regression", 6)
+# sum (x_i - p_i)^2: the objective of the reference's constraint test (test/constraints.jl:7)
+shifted_sphere = Objective("shifted_sphere", 7)
 # closed-form objectives of test/lbfgs.jl:20-26
 beale = Objective("beale", 16, (), 2)
 booth = Objective("booth", 17, (), 2)
@@ -43,8 +45,22 @@ quadratic = Objective("quadratic", 19, (1.0,), 2)
 boundary_quadratic = Objective("boundary_quadratic", 20, (), 1)
 
 REGISTRY = {o.name: o for o in (sphere, rosenbrock, rastrigin, ackley, lotka_volterra_fit,
-                               fitzhugh_nagumo_fit, mlp_regression, beale, booth, himmelblau,
+                               fitzhugh_nagumo_fit, mlp_regression, shifted_sphere, beale, booth, himmelblau,
                                quadratic, boundary_quadratic)}
+
+
+def quadratic_constraint(dim: int, c: float = 0.0, a=None, b=None) -> np.ndarray:
+    """One constraint g(x) = c + sum_i a_i x_i + b_i x_i^2 <= 0 as a row (c, a, b)
+    of an OptimizationProblem's ``cons``.  This is the registered form of the
+    reference's ``OptimizationFunction(f; cons)`` with ``ucons = 0``: the
+    engine takes no Python or Julia callable."""
+    row = np.zeros(1 + 2 * dim, np.float32)
+    row[0] = c
+    if a is not None:
+        row[1:1 + dim] = np.asarray(a, np.float32).reshape(dim)
+    if b is not None:
+        row[1 + dim:] = np.asarray(b, np.float32).reshape(dim)
+    return row
 
 
 def _f32(a, n=None):
@@ -62,6 +78,9 @@ class OptimizationProblem:
 
     ``lb``/``ub`` of ``None`` mean unbounded (src/utils.jl:310-318).  ``data``
     carries an objective's observations (ODE fits) or sample set (MLP).
+    ``cons`` holds up to 4 constraints g_k(x) <= 0 as rows (c_k, a_k, b_k) of
+    g_k(x) = c_k + a_k . x + b_k . x^2 (see ``quadratic_constraint``); they
+    enter the cost through the reference's penalty (src/utils.jl:320-372).
     """
 
     f: Objective
@@ -70,6 +89,7 @@ class OptimizationProblem:
     lb: np.ndarray | None = None
     ub: np.ndarray | None = None
     data: np.ndarray | None = None
+    cons: np.ndarray | None = None
     _keep: list = field(default_factory=list, repr=False)
 
     def __post_init__(self):
@@ -86,9 +106,14 @@ class OptimizationProblem:
         self.lb = _f32(self.lb, self.dim) if self.lb is not None else None
         self.ub = _f32(self.ub, self.dim) if self.ub is not None else None
         self.data = _f32(self.data)
+        if self.cons is not None:
+            c = np.ascontiguousarray(np.asarray(self.cons, dtype=np.float32))
+            if c.size % (1 + 2 * self.dim):
+                raise _lib.ArgumentError(_lib.EINVAL, f"cons rows have 1 + 2 dim = {1 + 2 * self.dim} values")
+            self.cons = c.reshape(-1, 1 + 2 * self.dim)
 
     def remake(self, **kw) -> "OptimizationProblem":
-        args = dict(f=self.f, u0=self.u0, p=self.p, lb=self.lb, ub=self.ub, data=self.data)
+        args = dict(f=self.f, u0=self.u0, p=self.p, lb=self.lb, ub=self.ub, data=self.data, cons=self.cons)
         args.update(kw)
         return OptimizationProblem(**args)
 
@@ -104,6 +129,8 @@ class OptimizationProblem:
         pr.nparams = 0 if self.p is None else int(self.p.size)
         pr.data = _lib.fptr(self.data)
         pr.ndata = 0 if self.data is None else int(self.data.size)
+        pr.ncons = 0 if self.cons is None else int(self.cons.shape[0])
+        pr.cons = _lib.fptr(self.cons)
         return pr
 
 
