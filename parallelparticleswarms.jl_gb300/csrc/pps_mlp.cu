@@ -302,12 +302,24 @@ __global__ void __launch_bounds__(kMlpThreads, 1) k_mlp_eval(SwarmDev s, MlpArgs
   __shared__ uint64_t full_bar[2], empty_bar[2];
   __shared__ uint32_t tmem_base;
   __shared__ volatile int abort_flag;
+  __shared__ int64_t s_next[2];  // the tile after the next one, fetched a tile ahead
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int q = warp & 3;    // TMEM lane quarter: samples 32 q .. 32 q + 31 of each block
   const int pg = warp >> 2;  // particles 2 pg, 2 pg + 1 of the tile
   const int64_t n = s.n;
   const int64_t ntiles = (n + kMlpTileParticles - 1) / kMlpTileParticles;
   int64_t tile = blockIdx.x;
+  // Tiles after the first: in a swarm (MODE 0, 1) taken from the iteration
+  // state's counter, so CTAs on slower SMs take fewer; for points in turn.
+  int64_t static_next = blockIdx.x;
+  auto grab = [&]() -> int64_t {
+    if constexpr (MODE == 2) {
+      static_next += gridDim.x;
+      return static_next;
+    } else {
+      return (int64_t)gridDim.x + (int64_t)atomicAdd(&s.st->tile_next, 1u);
+    }
+  };
   uint32_t t = 0;
   float w = 0.0f;
   if constexpr (MOVE) {
@@ -355,6 +367,7 @@ __global__ void __launch_bounds__(kMlpThreads, 1) k_mlp_eval(SwarmDev s, MlpArgs
     mbar_init(smem_u32(&empty_bar[1]), kMlpWarps);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     abort_flag = 0;
+    s_next[0] = grab();
   }
   fence_async_smem();  // operands written by the generic proxy, read by the tensor core
   tc_before_sync();
@@ -382,10 +395,14 @@ __global__ void __launch_bounds__(kMlpThreads, 1) k_mlp_eval(SwarmDev s, MlpArgs
     issued = g + 1;
   };
 
-  for (; tile < ntiles; tile += gridDim.x, tb ^= 1) {
+  for (int k = 0; tile < ntiles; ++k, tb ^= 1) {
     const int64_t i0 = tile * kMlpTileParticles;
-    const int64_t next = tile + gridDim.x;
+    const int64_t next = s_next[k & 1];  // read by every thread before the end-of-tile barrier
+    if (tid == 0) s_next[(k + 1) & 1] = grab();  // read at the top of the tile after next
     if (tid == 0) issue(0);
+    // MODE 1: the personal-best costs the tile compares against, loaded early
+    float pc_old = 0.0f;
+    if (MODE == 1 && tid < kMlpTileParticles && i0 + tid < n) pc_old = s.pcost[i0 + tid];
     const float* w2base = sW2 + (size_t)tb * kMlpTileParticles * kMlpW2Stride + (2 * pg) * kMlpW2Stride;
     uint8_t* nB = sB + (size_t)(tb ^ 1) * kMlpBBytes;
     uint8_t* nBb = sBb + (size_t)(tb ^ 1) * kMlpBBytes;
@@ -477,7 +494,7 @@ __global__ void __launch_bounds__(kMlpThreads, 1) k_mlp_eval(SwarmDev s, MlpArgs
           float pc = c;
           uint8_t fl = 0;
           if (MODE == 1) {
-            pc = s.pcost[pi];
+            pc = pc_old;
             fl = (c < pc) ? 1 : 0;  // strict <, src/kernels.jl:21-24
             pc = fl ? c : pc;
           }
@@ -489,6 +506,7 @@ __global__ void __launch_bounds__(kMlpThreads, 1) k_mlp_eval(SwarmDev s, MlpArgs
         }
       }
     }
+    tile = next;
   }
   if (abort_flag && tid == 0) {
     atomicOr(a.status, 2u);
