@@ -20,10 +20,13 @@
 // sequence of the CPU restatement, so results are bit-identical to it.
 //
 // GB300 design: one thread per particle; vectors of the particle's dimension
-// live in registers (compile-time bound MAXD), the L-BFGS history (2 m D
-// floats) and the Broyden matrix (D^2) in thread-local memory, which stays
-// L1/L2 resident.  The argmin over the per-particle results (the reference's
-// host findmin) runs on the device with the 64-bit (cost, index) key.
+// live in registers (compile-time bound MAXD).  Up to 16 dims the L-BFGS
+// history (2 m D + 2 m floats per particle) lives in shared memory, particle
+// fastest (element (slot, d) of thread t at (slot D + d) blockDim + t, so a
+// warp's accesses hit 32 banks), with blocks of 32-128 threads sized to fit;
+// longer histories and the Broyden matrix (D^2) stay in thread-local memory.  The
+// argmin over the per-particle results (the reference's host findmin) runs on
+// the device with the 64-bit (cost, index) key.
 #include <cmath>
 
 #include "pps_internal.h"
@@ -48,17 +51,47 @@ __device__ __forceinline__ float dotv(const float (&a)[MAXD], const float (&b)[M
   return s;
 }
 
-template <int OBJ, int MAXD>
+// the history of one thread: in shared memory (SMEM) or thread-local arrays
+template <int MAXD, bool SMEM>
+struct LbfgsHistory;
+template <int MAXD>
+struct LbfgsHistory<MAXD, true> {
+  float* base;
+  int D, m, nt, t;
+  __device__ __forceinline__ LbfgsHistory(float* sm, int D_, int m_) : base(sm), D(D_), m(m_) {
+    nt = blockDim.x;
+    t = threadIdx.x;
+  }
+  __device__ __forceinline__ float& S(int slot, int d) { return base[((size_t)slot * D + d) * nt + t]; }
+  __device__ __forceinline__ float& Y(int slot, int d) { return base[((size_t)(m + slot) * D + d) * nt + t]; }
+  __device__ __forceinline__ float& rho(int slot) { return base[((size_t)2 * m * D + slot) * nt + t]; }
+  __device__ __forceinline__ float& alpha(int slot) { return base[((size_t)2 * m * D + m + slot) * nt + t]; }
+};
+template <int MAXD>
+struct LbfgsHistory<MAXD, false> {
+  float s_[kMaxHistory][MAXD], y_[kMaxHistory][MAXD], rho_[kMaxHistory], alpha_[kMaxHistory];
+  __device__ __forceinline__ LbfgsHistory(float*, int, int) {}
+  __device__ __forceinline__ float& S(int slot, int d) { return s_[slot][d]; }
+  __device__ __forceinline__ float& Y(int slot, int d) { return y_[slot][d]; }
+  __device__ __forceinline__ float& rho(int slot) { return rho_[slot]; }
+  __device__ __forceinline__ float& alpha(int slot) { return alpha_[slot]; }
+};
+
+// floats of shared memory one thread's L-BFGS history takes
+__host__ __device__ constexpr size_t lbfgs_hist_floats(int m, int D) { return (size_t)2 * m * D + 2 * (size_t)m; }
+
+template <int OBJ, int MAXD, bool SMEM>
 __global__ void __launch_bounds__(128) k_lbfgs(const float* __restrict__ X0, int64_t ld, int64_t n, ObjParams op,
                                                const float* __restrict__ lbp, const float* __restrict__ ubp,
                                                LocalOpts o, float* __restrict__ xout, float* __restrict__ fout,
                                                float* __restrict__ itout) {
+  extern __shared__ float hist_sm[];
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int D = op.dim;
   const int m = o.history;
   float lb[MAXD], ub[MAXD], x[MAXD], g[MAXD], pg[MAXD], q[MAXD], dir[MAXD], xn[MAXD], gn[MAXD];
-  float S[kMaxHistory][MAXD], Y[kMaxHistory][MAXD], rho[kMaxHistory], alpha[kMaxHistory];
+  LbfgsHistory<MAXD, SMEM> H(hist_sm, D, m);
   PPS_FOR_D(d) {
     lb[d] = lbp[d];
     ub[d] = ubp[d];
@@ -79,26 +112,26 @@ __global__ void __launch_bounds__(128) k_lbfgs(const float* __restrict__ X0, int
     for (int j = 0; j < hist; ++j) {  // newest pair first
       const int slot = (head - 1 - j + m) % m;
       float sq_ = 0.0f;
-      PPS_FOR_D(d) sq_ = __fadd_rn(sq_, __fmul_rn(S[slot][d], q[d]));
-      const float a = __fmul_rn(rho[slot], sq_);
-      alpha[slot] = a;
-      PPS_FOR_D(d) q[d] = __fsub_rn(q[d], __fmul_rn(a, Y[slot][d]));
+      PPS_FOR_D(d) sq_ = __fadd_rn(sq_, __fmul_rn(H.S(slot, d), q[d]));
+      const float a = __fmul_rn(H.rho(slot), sq_);
+      H.alpha(slot) = a;
+      PPS_FOR_D(d) q[d] = __fsub_rn(q[d], __fmul_rn(a, H.Y(slot, d)));
     }
     float gamma = 1.0f;
     if (hist > 0) {
       const int nw = (head - 1 + m) % m;
       float sy = 0.0f, yy = 0.0f;
-      PPS_FOR_D(d) sy = __fadd_rn(sy, __fmul_rn(S[nw][d], Y[nw][d]));
-      PPS_FOR_D(d) yy = __fadd_rn(yy, __fmul_rn(Y[nw][d], Y[nw][d]));
+      PPS_FOR_D(d) sy = __fadd_rn(sy, __fmul_rn(H.S(nw, d), H.Y(nw, d)));
+      PPS_FOR_D(d) yy = __fadd_rn(yy, __fmul_rn(H.Y(nw, d), H.Y(nw, d)));
       gamma = __fdiv_rn(sy, yy);
     }
     PPS_FOR_D(d) q[d] = __fmul_rn(gamma, q[d]);
     for (int j = hist - 1; j >= 0; --j) {  // oldest pair first
       const int slot = (head - 1 - j + m) % m;
       float yq = 0.0f;
-      PPS_FOR_D(d) yq = __fadd_rn(yq, __fmul_rn(Y[slot][d], q[d]));
-      const float b = __fmul_rn(rho[slot], yq);
-      PPS_FOR_D(d) q[d] = __fadd_rn(q[d], __fmul_rn(S[slot][d], __fsub_rn(alpha[slot], b)));
+      PPS_FOR_D(d) yq = __fadd_rn(yq, __fmul_rn(H.Y(slot, d), q[d]));
+      const float b = __fmul_rn(H.rho(slot), yq);
+      PPS_FOR_D(d) q[d] = __fadd_rn(q[d], __fmul_rn(H.S(slot, d), __fsub_rn(H.alpha(slot), b)));
     }
     PPS_FOR_D(d) {
       const float dd = -q[d];
@@ -138,10 +171,10 @@ __global__ void __launch_bounds__(128) k_lbfgs(const float* __restrict__ X0, int
     }
     if (sy > 1e-12f) {
       PPS_FOR_D(d) {
-        S[head][d] = sv[d];
-        Y[head][d] = yv[d];
+        H.S(head, d) = sv[d];
+        H.Y(head, d) = yv[d];
       }
-      rho[head] = __fdiv_rn(1.0f, sy);
+      H.rho(head) = __fdiv_rn(1.0f, sy);
       head = (head + 1) % m;
       if (hist < m) ++hist;
     }
@@ -333,37 +366,55 @@ static LocalBufs local_bufs(pps_swarm* s) {
   return lb;
 }
 
+// L-BFGS: up to 16 dims the history lives in shared memory (blocks of 32-128
+// threads, at most 96 KB: two or more blocks per SM; 16 slots x 16 dims fit
+// 32 threads); above 16 dims in thread-local memory
 template <int OBJ, int MAXD>
-static void launch_local_lbfgs(pps_swarm* s, const float* x0, const LocalOpts& o, const LocalBufs& b) {
+static int launch_local_lbfgs(pps_swarm* s, const float* x0, const LocalOpts& o, const LocalBufs& b) {
   const int64_t n = s->dv.n;
-  const unsigned blocks = (unsigned)((n + 127) / 128);
-  k_lbfgs<OBJ, MAXD><<<blocks, 128, 0, s->stream>>>(x0, s->dv.npad, n, s->op, s->dv.lb, s->dv.ub, o, b.x, b.f, b.it);
+  if constexpr (MAXD <= 16) {
+    const size_t per_thread = sizeof(float) * lbfgs_hist_floats(o.history, s->dv.dim);
+    int nt = 128;
+    while (nt > 32 && per_thread * nt > (96u << 10)) nt /= 2;
+    const size_t smem = per_thread * nt;
+    PPS_CUDA(cudaFuncSetAttribute(k_lbfgs<OBJ, MAXD, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const unsigned blocks = (unsigned)((n + nt - 1) / nt);
+    k_lbfgs<OBJ, MAXD, true><<<blocks, nt, smem, s->stream>>>(x0, s->dv.npad, n, s->op, s->dv.lb, s->dv.ub, o, b.x,
+                                                               b.f, b.it);
+  } else {
+    const unsigned blocks = (unsigned)((n + 127) / 128);
+    k_lbfgs<OBJ, MAXD, false><<<blocks, 128, 0, s->stream>>>(x0, s->dv.npad, n, s->op, s->dv.lb, s->dv.ub, o, b.x,
+                                                              b.f, b.it);
+  }
+  return PPS_OK;
 }
 
 template <int OBJ, int MAXD>
-static void launch_local_t(pps_swarm* s, int kind, const float* x0, const LocalOpts& o, const LocalBufs& b) {
+static int launch_local_t(pps_swarm* s, int kind, const float* x0, const LocalOpts& o, const LocalBufs& b) {
+  if (kind == 0) return launch_local_lbfgs<OBJ, MAXD>(s, x0, o, b);
   const int64_t n = s->dv.n;
   const unsigned blocks = (unsigned)((n + 127) / 128);
-  if (kind == 0)
-    k_lbfgs<OBJ, MAXD><<<blocks, 128, 0, s->stream>>>(x0, s->dv.npad, n, s->op, s->dv.lb, s->dv.ub, o, b.x, b.f, b.it);
-  else
-    k_broyden<OBJ, MAXD><<<blocks, 128, 0, s->stream>>>(x0, s->dv.npad, n, s->op, s->dv.lb, s->dv.ub, o, b.x, b.f, b.it);
+  k_broyden<OBJ, MAXD><<<blocks, 128, 0, s->stream>>>(x0, s->dv.npad, n, s->op, s->dv.lb, s->dv.ub, o, b.x, b.f, b.it);
+  return PPS_OK;
 }
 
 template <int OBJ>
 static int launch_local_obj(pps_swarm* s, int kind, const float* x0, const LocalOpts& o, const LocalBufs& b) {
   const int D = s->dv.dim;
   if (kind == 1 && D > 16) return set_error(PPS_ENOTSUP, "the Broyden local stage supports dim <= 16 (got %d)", D);
+  int rc;
   if constexpr (OBJ >= kBeale) {  // closed forms are defined for dim <= 2
-    launch_local_t<OBJ, 2>(s, kind, x0, o, b);
+    rc = launch_local_t<OBJ, 2>(s, kind, x0, o, b);
   } else {
-    if (D <= 2) launch_local_t<OBJ, 2>(s, kind, x0, o, b);
-    else if (D <= 4) launch_local_t<OBJ, 4>(s, kind, x0, o, b);
-    else if (D <= 8) launch_local_t<OBJ, 8>(s, kind, x0, o, b);
-    else if (D <= 16) launch_local_t<OBJ, 16>(s, kind, x0, o, b);
-    else if (D <= 32) launch_local_lbfgs<OBJ, 32>(s, x0, o, b);
-    else launch_local_lbfgs<OBJ, 64>(s, x0, o, b);
+    if (D <= 2) rc = launch_local_t<OBJ, 2>(s, kind, x0, o, b);
+    else if (D <= 4) rc = launch_local_t<OBJ, 4>(s, kind, x0, o, b);
+    else if (D <= 8) rc = launch_local_t<OBJ, 8>(s, kind, x0, o, b);
+    else if (D <= 10 && kind == 0) rc = launch_local_lbfgs<OBJ, 10>(s, x0, o, b);
+    else if (D <= 16) rc = launch_local_t<OBJ, 16>(s, kind, x0, o, b);
+    else if (D <= 32) rc = launch_local_lbfgs<OBJ, 32>(s, x0, o, b);
+    else rc = launch_local_lbfgs<OBJ, 64>(s, x0, o, b);
   }
+  if (rc) return rc;
   PPS_CUDA(cudaGetLastError());
   return PPS_OK;
 }
