@@ -218,6 +218,9 @@ def run_hybrid(pps) -> dict:
             sw.init()
             pso_ms = sw.sync_run(200)
             _, pso_cost, _ = sw.gbest()
+            # the first call loads the kernel's module; the local stage leaves
+            # the swarm unchanged, so the second call is the timed one
+            sw.local_stage("lbfgs", history=10, maxiters=100, armijo_c1=1e-4, gtol=1e-5)
             u, f, idx, local_ms = sw.local_stage("lbfgs", history=10, maxiters=100, armijo_c1=1e-4, gtol=1e-5)
             iters = sw.get(7)
         out[name] = {"pso_ms": pso_ms, "pso_particle_iters_per_s": n * 200 / (pso_ms / 1e3),
