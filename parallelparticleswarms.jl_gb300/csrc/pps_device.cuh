@@ -67,6 +67,41 @@ __device__ __forceinline__ Rand4 philox4x32_10(uint32_t c0, uint32_t c1, uint32_
   return Rand4{c0, c1, c2, c3};
 }
 
+// The round keys of a Philox4x32-10 key (k0 + r W0, k1 + r W1, r = 0..9),
+// computed once on the host: a kernel that takes them by value reads them
+// from its parameter bank instead of stepping the key schedule in every call.
+struct PhiloxKeys {
+  uint32_t k[20];
+};
+inline PhiloxKeys philox_round_keys(uint64_t seed) {
+  PhiloxKeys K;
+  uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+  for (int r = 0; r < 10; ++r) {
+    K.k[2 * r] = k0;
+    K.k[2 * r + 1] = k1;
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+  return K;
+}
+__device__ __forceinline__ Rand4 philox4x32_10(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3,
+                                               const PhiloxKeys& K) {
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    const uint64_t p0 = (uint64_t)0xD2511F53u * (uint64_t)c0;
+    const uint64_t p1 = (uint64_t)0xCD9E8D57u * (uint64_t)c2;
+    const uint32_t n0 = (uint32_t)(p1 >> 32) ^ c1 ^ K.k[2 * r];
+    const uint32_t n1 = (uint32_t)p1;
+    const uint32_t n2 = (uint32_t)(p0 >> 32) ^ c3 ^ K.k[2 * r + 1];
+    const uint32_t n3 = (uint32_t)p0;
+    c0 = n0;
+    c1 = n1;
+    c2 = n2;
+    c3 = n3;
+  }
+  return Rand4{c0, c1, c2, c3};
+}
+
 __device__ __forceinline__ float u01(uint32_t bits) {
   return __fmul_rn(__uint2float_rn(bits >> 8), 0x1p-24f);
 }

@@ -103,7 +103,7 @@ __global__ void __launch_bounds__(kSyncThreads) k_init(SwarmDev s, ObjParams op,
 // kernels pass it (src/kernels.jl:77,151; handle_constraints adds 1, :28-31).
 template <int OBJ, int PPT, bool CONS = false>
 __global__ void __launch_bounds__(kSyncThreads, (PPT == 4 ? 2 : (PPT == 2 ? 3 : 4)))
-    k_sync_step(SwarmDev s, ObjParams op, uint64_t seed, float c1, float c2, int from_position) {
+    k_sync_step(SwarmDev s, ObjParams op, PhiloxKeys keys, float c1, float c2, int from_position) {
   extern __shared__ float sm[];
   const int D = s.dim;
   float* sg = sm;
@@ -118,7 +118,6 @@ __global__ void __launch_bounds__(kSyncThreads, (PPT == 4 ? 2 : (PPT == 2 ? 3 : 
     sub[d] = s.ub[d];
   }
   __syncthreads();
-  const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
   const int64_t npad = s.npad;
   const int64_t ngroups = npad / PPT;  // groups of PPT particles
   const uint32_t ntiles = (uint32_t)((ngroups + blockDim.x - 1) / blockDim.x);
@@ -177,7 +176,7 @@ __global__ void __launch_bounds__(kSyncThreads, (PPT == 4 ? 2 : (PPT == 2 ? 3 : 
         }
         Rand4 r[PPT];
 #pragma unroll
-        for (int k = 0; k < PPT; ++k) r[k] = philox4x32_10((uint32_t)(i0 + k), (uint32_t)(j >> 1), t, kTagStep, k0, k1);
+        for (int k = 0; k < PPT; ++k) r[k] = philox4x32_10((uint32_t)(i0 + k), (uint32_t)(j >> 1), t, kTagStep, keys);
         {  // dim j
           const int64_t o = (int64_t)j * npad + i0;
           if (anyfl) {
@@ -375,23 +374,24 @@ int sync_grid(pps_swarm* s) {
 
 int launch_sync_step(pps_swarm* s, float c1, float c2) {
   const int grid = sync_grid(s);
+  const PhiloxKeys keys = philox_round_keys(s->seed);
   const size_t smem = 3 * sizeof(float) * (size_t)s->dv.dim;
   const int from_pos = (s->flags & PPS_FLAG_GBEST_FROM_POSITION) ? 1 : 0;
   const int ppt = sync_ppt();
 #define L_STEP(O)                                                                                       \
   if (ppt == 4)                                                                                         \
-    k_sync_step<O, 4><<<grid, kSyncThreads, smem, s->stream>>>(s->dv, s->op, s->seed, c1, c2, from_pos); \
+    k_sync_step<O, 4><<<grid, kSyncThreads, smem, s->stream>>>(s->dv, s->op, keys, c1, c2, from_pos); \
   else if (ppt == 2)                                                                                    \
-    k_sync_step<O, 2><<<grid, kSyncThreads, smem, s->stream>>>(s->dv, s->op, s->seed, c1, c2, from_pos); \
+    k_sync_step<O, 2><<<grid, kSyncThreads, smem, s->stream>>>(s->dv, s->op, keys, c1, c2, from_pos); \
   else                                                                                                  \
-    k_sync_step<O, 1><<<grid, kSyncThreads, smem, s->stream>>>(s->dv, s->op, s->seed, c1, c2, from_pos)
+    k_sync_step<O, 1><<<grid, kSyncThreads, smem, s->stream>>>(s->dv, s->op, keys, c1, c2, from_pos)
   if (s->dv.ncons > 0) {
     // constrained path: one particle per thread; tiles of 256 particles,
     // handed out dynamically, so any grid up to 4 blocks per SM is right
     const int64_t ntiles = (s->dv.npad + kSyncThreads - 1) / kSyncThreads;
     const int64_t cgrid = ntiles < 4 * (int64_t)s->sm_count ? ntiles : 4 * (int64_t)s->sm_count;
 #define L_STEP_CONS(O) \
-  k_sync_step<O, 1, true><<<(unsigned)cgrid, kSyncThreads, smem, s->stream>>>(s->dv, s->op, s->seed, c1, c2, from_pos)
+  k_sync_step<O, 1, true><<<(unsigned)cgrid, kSyncThreads, smem, s->stream>>>(s->dv, s->op, keys, c1, c2, from_pos)
     PPS_DISPATCH_SEPARABLE(s->objective, L_STEP_CONS)
 #undef L_STEP_CONS
   } else {
