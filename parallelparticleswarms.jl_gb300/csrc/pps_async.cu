@@ -36,7 +36,7 @@ __device__ __forceinline__ unsigned long long warp_min_u64_a(unsigned long long 
 }
 
 template <int OBJ, int S>
-__global__ void __launch_bounds__(kAsyncThreads) k_async(SwarmDev s, ObjParams op, uint64_t seed,
+__global__ void __launch_bounds__(kAsyncThreads) k_async(SwarmDev s, ObjParams op, PhiloxKeys keys,
                                                           int iters, float c1, float c2, int lanes,
                                                           int slice) {
   extern __shared__ float sm[];
@@ -64,8 +64,6 @@ __global__ void __launch_bounds__(kAsyncThreads) k_async(SwarmDev s, ObjParams o
   const int d0 = lane * slice;
   int cnt = D - d0;
   cnt = cnt < 0 ? 0 : (cnt > slice ? slice : cnt);
-  const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
-
   float x[S], v[S], p[S];
   const bool pending = s.flag[il] != 0;
 #pragma unroll
@@ -88,7 +86,7 @@ __global__ void __launch_bounds__(kAsyncThreads) k_async(SwarmDev s, ObjParams o
 #pragma unroll
     for (int k = 0; k < S; k += 2) {
       if (k < cnt) {
-        const Rand4 r = philox4x32_10((uint32_t)il, (uint32_t)((d0 + k) >> 1), t, kTagStep, k0, k1);
+        const Rand4 r = philox4x32_10((uint32_t)il, (uint32_t)((d0 + k) >> 1), t, kTagStep, keys);
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
           const int kk = k + h;
@@ -199,13 +197,13 @@ static int launch_async_obj(pps_swarm* s, int iters, float c1, float c2, int lan
   const int64_t blocks = (threads + kAsyncThreads - 1) / kAsyncThreads;
   const size_t smem = 3 * sizeof(float) * (size_t)s->dv.dim;
   if (slice <= 4)
-    k_async<OBJ, 4><<<(unsigned)blocks, kAsyncThreads, smem, s->stream>>>(s->dv, s->op, s->seed, iters, c1, c2, lanes, slice);
+    k_async<OBJ, 4><<<(unsigned)blocks, kAsyncThreads, smem, s->stream>>>(s->dv, s->op, philox_round_keys(s->seed), iters, c1, c2, lanes, slice);
   else if (slice <= 8)
-    k_async<OBJ, 8><<<(unsigned)blocks, kAsyncThreads, smem, s->stream>>>(s->dv, s->op, s->seed, iters, c1, c2, lanes, slice);
+    k_async<OBJ, 8><<<(unsigned)blocks, kAsyncThreads, smem, s->stream>>>(s->dv, s->op, philox_round_keys(s->seed), iters, c1, c2, lanes, slice);
   else if (slice <= 16)
-    k_async<OBJ, 16><<<(unsigned)blocks, kAsyncThreads, smem, s->stream>>>(s->dv, s->op, s->seed, iters, c1, c2, lanes, slice);
+    k_async<OBJ, 16><<<(unsigned)blocks, kAsyncThreads, smem, s->stream>>>(s->dv, s->op, philox_round_keys(s->seed), iters, c1, c2, lanes, slice);
   else
-    k_async<OBJ, 32><<<(unsigned)blocks, kAsyncThreads, smem, s->stream>>>(s->dv, s->op, s->seed, iters, c1, c2, lanes, slice);
+    k_async<OBJ, 32><<<(unsigned)blocks, kAsyncThreads, smem, s->stream>>>(s->dv, s->op, philox_round_keys(s->seed), iters, c1, c2, lanes, slice);
   PPS_CUDA(cudaGetLastError());
   return PPS_OK;
 }
