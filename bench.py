@@ -65,13 +65,6 @@ UNIT = "particle-iters/s"
 WORKLOAD = "sync PSO, 2^20 particles x 100-D Rastrigin, Float32, bounds [-5.12,5.12], 1000 iterations"
 
 
-def dist_env():
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return rank, world, local
-
-
 class ClockSampler:
     """nvidia-smi samples of SM clock and throttle reasons during a region."""
 
@@ -450,7 +443,9 @@ def main():
                     help="arrival window of the open-loop served run of the full mix")
     ap.add_argument("--ode-fits", type=int, default=512, help="fits of each model in the batched ODE run")
     args = ap.parse_args()
-    rank, world, local = dist_env()
+    from parallelparticleswarms import multi
+
+    rank, world, local = multi.rank_env()
 
     if args.impl == "reference":
         return run_reference(args, rank, world)
@@ -470,7 +465,7 @@ def main():
     _lib.check(_lib.load().pps_set_device(local))
     prob = make_problem(pps)
     iters = args.iters
-    seed0 = 1000 * rank
+    seed0 = multi.swarm_seed(0, rank)
 
     if args.only in ("hybrid", "ode", "serve", "mlp"):
         fn = {"hybrid": lambda: run_hybrid(pps), "ode": lambda: run_ode_batch(pps, args.ode_fits),
@@ -504,17 +499,10 @@ def main():
             sw.init()  # fresh swarm; init is outside the timed loop as in src/solve.jl:15-26
             step_ms.append(sw.sync_run(iters))  # CUDA events on the swarm's stream
     barrier()
-    total_ms = sum(step_ms)
-    if dist:
-        import torch
-
-        t = torch.tensor([total_ms], device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = multi.max_over_ranks(sum(step_ms), dist, f"cuda:{local}")
     _, gcost, _ = sw.gbest()
     sw.close()
-    units = N_PARTICLES * iters * args.steps * world
-    value = units / (total_ms / 1000.0)
+    value = multi.job_throughput(N_PARTICLES * iters * args.steps, world, total_ms)
     launch_ms = total_ms / (args.steps * iters)
     algo_bytes = N_PARTICLES * BYTES_PER_PARTICLE_ITER
     achieved = algo_bytes / (launch_ms / 1000.0) / 1e9
@@ -544,7 +532,7 @@ def main():
             sol = pps.solve(prob, alg, maxiters=iters, seed=seed0 + k)
             _ = sol.objective
         barrier()
-        e2e_s = time.perf_counter() - t0
+        e2e_s = multi.max_over_ranks(time.perf_counter() - t0, dist, f"cuda:{local}")
         h2d = 4 * (3 * DIM + 1)  # lb, ub, u0, p
         d2h = 4 * DIM + 8 + 4 + 4 * N_PARTICLES * DIM  # u, gbest cost+index, objective, original positions
         e2e = {"value": N_PARTICLES * iters * e2e_steps * world / e2e_s, "unit": UNIT,
