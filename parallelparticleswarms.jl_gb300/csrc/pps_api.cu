@@ -11,6 +11,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <limits>
+#include <mutex>
 #include <new>
 #include <vector>
 
@@ -548,6 +549,90 @@ static int field_ptr(pps_swarm* s, int32_t field, float** dev, int* rows) {
   }
 }
 
+}  // extern "C"
+
+namespace pps {
+
+// Device -> pageable host copies of swarm state (hundreds of MB for the
+// particle positions of a large swarm) go through two pinned staging
+// buffers of kStageBytes, allocated once per device: the copy engine fills
+// one while the host copies the other out, instead of the driver's slower
+// staging of a pageable destination.
+constexpr size_t kStageBytes = (size_t)32 << 20;
+
+struct HostStage {
+  std::mutex mu;
+  char* buf[2] = {nullptr, nullptr};
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  bool ready = false;
+};
+
+static HostStage& host_stage(int device) {
+  static HostStage stages[64];
+  return stages[device & 63];
+}
+
+// rows x row_bytes from dev (pitch src_pitch bytes) to the contiguous host
+// array out, on stream
+static int copy_rows_to_host(pps_swarm* s, char* out, const char* dev, size_t src_pitch, size_t row_bytes,
+                             size_t rows) {
+  const size_t total = row_bytes * rows;
+  if (total < ((size_t)4 << 20) || s->device < 0 || s->device >= 64) {
+    PPS_CUDA(cudaMemcpy2DAsync(out, row_bytes, dev, src_pitch, row_bytes, rows, cudaMemcpyDeviceToHost, s->stream));
+    PPS_CUDA(cudaStreamSynchronize(s->stream));
+    return PPS_OK;
+  }
+  HostStage& hs = host_stage(s->device);
+  std::lock_guard<std::mutex> lock(hs.mu);
+  if (!hs.ready) {
+    for (int k = 0; k < 2; ++k) {
+      PPS_CUDA(cudaMallocHost(&hs.buf[k], kStageBytes));
+      PPS_CUDA(cudaEventCreateWithFlags(&hs.ev[k], cudaEventDisableTiming));
+    }
+    hs.ready = true;
+  }
+  // pieces: whole rows when a row fits a buffer, else segments of one row
+  struct Piece {
+    size_t src_off, dst_off, rows, bytes;  // bytes per row of the piece
+  };
+  std::vector<Piece> pieces;
+  if (row_bytes <= kStageBytes) {
+    const size_t per = kStageBytes / row_bytes;
+    for (size_t r = 0; r < rows; r += per) {
+      const size_t nr = (rows - r) < per ? (rows - r) : per;
+      pieces.push_back({r * src_pitch, r * row_bytes, nr, row_bytes});
+    }
+  } else {
+    for (size_t r = 0; r < rows; ++r)
+      for (size_t c = 0; c < row_bytes; c += kStageBytes) {
+        const size_t nb = (row_bytes - c) < kStageBytes ? (row_bytes - c) : kStageBytes;
+        pieces.push_back({r * src_pitch + c, r * row_bytes + c, 1, nb});
+      }
+  }
+  for (size_t k = 0; k <= pieces.size(); ++k) {
+    if (k < pieces.size()) {  // copy engine: piece k into buffer k % 2
+      const Piece& p = pieces[k];
+      PPS_CUDA(cudaMemcpy2DAsync(hs.buf[k & 1], p.bytes, dev + p.src_off, src_pitch, p.bytes, p.rows,
+                                 cudaMemcpyDeviceToHost, s->stream));
+      PPS_CUDA(cudaEventRecord(hs.ev[k & 1], s->stream));
+    }
+    if (k >= 1) {  // host: piece k - 1 out of its buffer while piece k is in flight
+      const Piece& p = pieces[k - 1];
+      PPS_CUDA(cudaEventSynchronize(hs.ev[(k - 1) & 1]));
+      if (p.rows == 1 || p.bytes == row_bytes) {
+        memcpy(out + p.dst_off, hs.buf[(k - 1) & 1], p.bytes * p.rows);
+      } else {
+        for (size_t r = 0; r < p.rows; ++r) memcpy(out + p.dst_off + r * row_bytes, hs.buf[(k - 1) & 1] + r * p.bytes, p.bytes);
+      }
+    }
+  }
+  return PPS_OK;
+}
+
+}  // namespace pps
+
+extern "C" {
+
 int pps_get_state(pps_swarm* s, int32_t field, float* out) {
   if (!s || !out) return set_error(PPS_EINVAL, "NULL argument");
   int rc = use_device(s);
@@ -556,10 +641,8 @@ int pps_get_state(pps_swarm* s, int32_t field, float* out) {
   int rows;
   if ((rc = field_ptr(s, field, &dev, &rows))) return rc;
   const size_t w = sizeof(float) * (size_t)s->dv.n;
-  PPS_CUDA(cudaMemcpy2DAsync(out, w, dev, sizeof(float) * (size_t)s->dv.npad, w, rows,
-                             cudaMemcpyDeviceToHost, s->stream));
-  PPS_CUDA(cudaStreamSynchronize(s->stream));
-  return PPS_OK;
+  return copy_rows_to_host(s, reinterpret_cast<char*>(out), reinterpret_cast<const char*>(dev),
+                           sizeof(float) * (size_t)s->dv.npad, w, (size_t)rows);
 }
 
 int pps_set_state(pps_swarm* s, int32_t field, const float* in) {

@@ -119,7 +119,9 @@ def _pso_solve(cache: PSOCache, maxiters, w, wdamp, c1, c2) -> OptimizationSolut
     t1 = time.perf_counter()
     u, _, _ = sw.gbest()
     obj = float(evaluate(cache.prob, u))  # prob.f(gbest.position, prob.p), src/solve.jl:56
-    original = sw.positions().T.copy()
+    # sol.original: every particle's position, (n, dim), a view of the SoA copy
+    # (a transposed copy would be a strided 4 n dim byte shuffle on the host)
+    original = sw.positions().T
     return OptimizationSolution(u=u, objective=obj, original=original,
                                 stats=OptimizationStats(time=t1 - t0, device_ms=ms, iterations=int(maxiters)),
                                 alg=alg)
