@@ -31,6 +31,8 @@ Prints ONE JSON line (rank 0).  Extra measurements ride in the same line:
   mlp          the MLP fit (16,384 particles x 577 parameters, 1024 samples)
                by sync PSO: particle-iters/s and the tanh rate against the
                special-function pipe
+  configs      C1 (3-D Rosenbrock, 1000 particles, 500 iterations) on the GPU
+               and the oracle; C2 with Rosenbrock
 With --impl reference the oracle's CPU implementation is timed instead
 (the Julia reference cannot run here: no Julia toolchain).
 """
@@ -270,6 +272,51 @@ def run_ode_batch(pps, count_each=512) -> dict:
             "block_shape": shape}
 
 
+def run_configs(pps) -> dict:
+    """The other sync configurations of the workload: C1 (3-D Rosenbrock, p =
+    [1, 100], bounds [-1, 10], 1000 particles, 500 iterations: the reference's
+    CPU-backend case) on the GPU and on the oracle, and C2 with Rosenbrock
+    (2^20 x 100-D, bounds [-5.12, 5.12], 1000 iterations)."""
+    out = {}
+    c1 = pps.OptimizationProblem(pps.rosenbrock, np.zeros(3, np.float32), [1.0, 100.0],
+                                 lb=np.full(3, -1.0, np.float32), ub=np.full(3, 10.0, np.float32))
+    with pps.Swarm(c1, 1000, seed=0) as sw:
+        sw.init()
+        sw.sync_run(500)  # warm
+        ms = []
+        for k in range(5):
+            sw.init()
+            ms.append(sw.sync_run(500))
+        _, cost, _ = sw.gbest()
+    gpu_ms = statistics.median(ms)
+    try:
+        sys.path.insert(0, str(ROOT / "oracle"))
+        import pps_oracle as orc
+        op = orc.OracleProblem(1, 3, np.full(3, -1.0, np.float32), np.full(3, 10.0, np.float32), params=[1.0, 100.0])
+        cms = []
+        for k in range(5):
+            ref = orc.OracleSwarm(op, 1000, 0).init()
+            t0 = time.perf_counter()
+            ref.sync_run(500)
+            cms.append((time.perf_counter() - t0) * 1e3)
+        cpu = {"ms": statistics.median(cms), "cores": os.cpu_count(), "same_gbest_cost": bool(ref.gcost == cost)}
+    except Exception as e:  # the oracle is optional on a machine without its build
+        cpu = {"unavailable": str(e)}
+    out["c1_rosenbrock_3d_1000x500"] = {"gpu_ms": gpu_ms, "particle_iters_per_s": 1000 * 500 / (gpu_ms / 1e3),
+                                        "gbest_cost": cost, "cpu_oracle": cpu}
+    c2 = pps.OptimizationProblem(pps.rosenbrock, np.zeros(DIM, np.float32), [1.0, 100.0],
+                                 lb=np.full(DIM, LO, np.float32), ub=np.full(DIM, HI, np.float32))
+    with pps.Swarm(c2, N_PARTICLES, seed=1) as sw:
+        sw.init()
+        sw.sync_run(50)  # warm
+        sw.init()
+        ms = sw.sync_run(ITERS)
+    launch_ms = ms / ITERS
+    out["c2_rosenbrock_2p20x100"] = {"device_ms": ms, "particle_iters_per_s": N_PARTICLES * ITERS / (ms / 1e3),
+                                     "hbm_gbs": N_PARTICLES * BYTES_PER_PARTICLE_ITER / (launch_ms / 1e3) / 1e9}
+    return out
+
+
 MLP_PARTICLES = 16384
 MLP_SAMPLES = 1024
 SFU_PER_CLK_PER_SM = 16  # tanh.approx results per clock per SM (special-function pipe)
@@ -430,7 +477,7 @@ def main():
     ap.add_argument("--no-async", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the hybrid, ODE-batch and served measurements")
     ap.add_argument("--mlp-iters", type=int, default=100, help="iterations of the MLP-fit measurement")
-    ap.add_argument("--only", choices=["sync", "async", "hybrid", "ode", "serve", "mlp"], default=None,
+    ap.add_argument("--only", choices=["sync", "async", "hybrid", "ode", "serve", "mlp", "configs"], default=None,
                     help="run one workload only (for profiling); prints its result")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU-baseline sample")
     ap.add_argument("--serve-requests", type=int, default=1500,
@@ -467,11 +514,11 @@ def main():
     iters = args.iters
     seed0 = multi.swarm_seed(0, rank)
 
-    if args.only in ("hybrid", "ode", "serve", "mlp"):
+    if args.only in ("hybrid", "ode", "serve", "mlp", "configs"):
         fn = {"hybrid": lambda: run_hybrid(pps), "ode": lambda: run_ode_batch(pps, args.ode_fits),
               "serve": lambda: {"served": run_served(pps, args, True),
                                 "served_without_mlp": run_served(pps, args, False)},
-              "mlp": lambda: run_mlp(pps, args.mlp_iters)}[args.only]
+              "mlp": lambda: run_mlp(pps, args.mlp_iters), "configs": lambda: run_configs(pps)}[args.only]
         if rank == 0:
             print(json.dumps({args.only: fn()}), flush=True)
         return 0
@@ -548,6 +595,7 @@ def main():
         extras["served"] = run_served(pps, args, True)
         extras["served_without_mlp"] = run_served(pps, args, False)
         extras["mlp"] = run_mlp(pps, args.mlp_iters)
+        extras["configs"] = run_configs(pps)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline and args.only is None:
