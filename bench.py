@@ -218,9 +218,12 @@ def run_hybrid(pps) -> dict:
             sw.local_stage("lbfgs", history=10, maxiters=100, armijo_c1=1e-4, gtol=1e-5)
             u, f, idx, local_ms = sw.local_stage("lbfgs", history=10, maxiters=100, armijo_c1=1e-4, gtol=1e-5)
             iters = sw.get(7)
+            sw.local_stage("bfgs", maxiters=100, gtol=1e-5)  # warm
+            _, fb, _, bfgs_ms = sw.local_stage("bfgs", maxiters=100, gtol=1e-5)
         out[name] = {"pso_ms": pso_ms, "pso_particle_iters_per_s": n * 200 / (pso_ms / 1e3),
                      "pso_best": pso_cost, "local_ms": local_ms, "local_particles_per_s": n / (local_ms / 1e3),
-                     "local_mean_iters": float(np.mean(iters)), "best": f, "solve_ms": pso_ms + local_ms}
+                     "local_mean_iters": float(np.mean(iters)), "best": f, "solve_ms": pso_ms + local_ms,
+                     "broyden_ms": bfgs_ms, "broyden_best": fb}
     return out
 
 
@@ -314,6 +317,53 @@ def run_configs(pps) -> dict:
     launch_ms = ms / ITERS
     out["c2_rosenbrock_2p20x100"] = {"device_ms": ms, "particle_iters_per_s": N_PARTICLES * ITERS / (ms / 1e3),
                                      "hbm_gbs": N_PARTICLES * BYTES_PER_PARTICLE_ITER / (launch_ms / 1e3) / 1e9}
+    # one large Lotka-Volterra fit solved alone (k_sync_step_ode: update, RK4,
+    # SSE, personal best and argmin fused, one launch per iteration)
+    fit, _ = pps.ode.synthetic_fit("lv", 3)
+    with pps.Swarm(fit, 16384, seed=3) as sw:
+        sw.init()
+        sw.sync_run(5)  # warm
+        sw.init()
+        ms = sw.sync_run(100)
+    steps = 1000 * 16384 * 100  # RK4 steps
+    out["ode_lv_16384x100_alone"] = {"device_ms": ms, "particle_iters_per_s": 16384 * 100 / (ms / 1e3),
+                                     "rk4_steps_per_s": steps / (ms / 1e3)}
+    # many small separable swarms in one batched launch against the same
+    # swarms solved one at a time
+    rng = np.random.default_rng(5)
+    swarms = []
+    for k in range(256):
+        name = ("rosenbrock", "rastrigin", "ackley")[k % 3]
+        D = int(rng.integers(2, 65))
+        lo = -5.12 if name == "rastrigin" else -5.0
+        obj = pps.REGISTRY[name]
+        prob = pps.OptimizationProblem(obj, np.zeros(D, np.float32), list(obj.default_params),
+                                       lb=np.full(D, lo, np.float32), ub=np.full(D, -lo, np.float32))
+        swarms.append((prob, int(rng.integers(256, 2049))))
+    with pps.Batch() as b:
+        for k, (prob, n) in enumerate(swarms):
+            b.add(prob, n, maxiters=500, seed=k)
+        b.run()  # autotune + warm
+        t0 = time.perf_counter()
+        bms = b.run()
+        bwall = time.perf_counter() - t0
+        res = [b.result(k) for k in range(len(swarms))]
+    same = True
+    t0 = time.perf_counter()
+    sample = list(range(0, len(swarms), 8))
+    for k in sample:
+        prob, n = swarms[k]
+        with pps.Swarm(prob, n, seed=k) as sw:
+            sw.init()
+            sw.sync_run(500)
+            u, c, i = sw.gbest()
+        same &= bool(np.array_equal(u, res[k][0]) and i == res[k][2])
+    plain = len(sample) / (time.perf_counter() - t0)
+    out["separable_batch_256"] = {"workload": "256 swarms (Rosenbrock / Rastrigin / Ackley, dim U{2..64}, "
+                                              "particles U{256..2048}), 500 iterations, one launch",
+                                  "batched_device_ms": bms, "batched_solves_per_s": len(swarms) / bwall,
+                                  "plain_solves_per_s": plain, "speedup_vs_plain": len(swarms) / bwall / plain,
+                                  "same_result_alone_and_batched": same}
     return out
 
 
