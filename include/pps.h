@@ -65,7 +65,9 @@ typedef enum pps_objective {
   PPS_OBJ_BOOTH = 17,
   PPS_OBJ_HIMMELBLAU = 18,
   PPS_OBJ_QUADRATIC = 19,         /* p1 (x1-1)^2 + (x2+2)^2 */
-  PPS_OBJ_BOUNDARY_QUADRATIC = 20 /* (x1+1)^2 */
+  PPS_OBJ_BOUNDARY_QUADRATIC = 20, /* (x1+1)^2 */
+  /* ids handed out by pps_objective_register, in registration order */
+  PPS_OBJ_USER_BASE = 256
 } pps_objective;
 
 /* An OptimizationProblem(f, u0, p; lb, ub) (SciMLBase) restated. */
@@ -272,6 +274,31 @@ PPS_API int pps_set_state(pps_swarm* s, int32_t field, const float* in);
 /* evaluate the problem's objective at npoints points (SoA dim x npoints) on
  * the device; used for sol.objective = f(u, p) (src/solve.jl:54-57) */
 PPS_API int pps_eval_objective(const pps_problem* prob, int64_t npoints, const float* x, float* f);
+
+/* ---- user objectives ---- */
+/* Registers an objective given as CUDA C source and returns its id (>=
+ * PPS_OBJ_USER_BASE) for pps_problem.objective.  Replaces the objective
+ * closure that the reference compiles into its kernels (cost =
+ * prob.f(x, p), src/kernels.jl:33).  The source defines
+ *
+ *   PPS_DEVICE float pps_objective(pps_point x, int dim, const float* p,
+ *                                  const float* data, long long ndata)
+ *
+ * with x[d] the point's coordinate d, p the problem's 8 parameters (zero past
+ * nparams) and data / ndata the problem's data buffer on the device.  It is
+ * compiled by NVRTC (loaded at run time) with --fmad=false for the current
+ * device, together with the library's init, synchronous-step and evaluation
+ * kernels; pps_exp, pps_cos2pi and pps_sin2pi are the library's exp(x),
+ * cos(2 pi x) and sin(2 pi x).  The same source registered again returns the
+ * same id.  Errors: PPS_EINVAL with the compiler log (pps_last_error) when
+ * the source does not compile, PPS_ENOTSUP without NVRTC.
+ * A user objective runs through pps_swarm_create / pps_swarm_init,
+ * pps_sync_run, pps_queue_run, pps_eval_objective and the server (as a swarm
+ * of its own), constraints included; pps_async_run, the HybridPSO local
+ * stage (no gradient), batches and pps_sync_run_noalloc return PPS_ENOTSUP.
+ * The library cannot bound the running time of the user's code: a function
+ * that does not return hangs the run. */
+PPS_API int pps_objective_register(const char* source, int32_t* objective);
 
 /* ---- caller-owned device buffers, no allocation ---- */
 /* A swarm whose device arrays belong to the caller.  All pointers are DEVICE

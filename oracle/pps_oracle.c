@@ -332,6 +332,12 @@ float orc_objective(const orc_problem* prob, const float* x, int64_t stride, int
     for (int d = 0; d < D && d < 8; ++d) p[d] = x[d * stride];
     return orc_ode_loss(prob->ode, p);
   }
+  if (prob->objective == ORC_OBJ_USER) {
+    /* cost = prob.f(x, p) (src/kernels.jl:33) with f given as C source */
+    float buf[4096];
+    for (int d = 0; d < D; ++d) buf[d] = x[d * stride];
+    return prob->user_fn(buf, D, prob->params, prob->user_data, (long long)prob->user_ndata);
+  }
   if (prob->objective == ORC_OBJ_MLP) {
     float p[577];
     for (int d = 0; d < 577; ++d) p[d] = x[d * stride];

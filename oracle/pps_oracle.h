@@ -66,7 +66,13 @@ enum {
   ORC_OBJ_HIMMELBLAU = 18,
   ORC_OBJ_QUADRATIC = 19,          /* p1 (x1-1)^2 + (x2+2)^2 */
   ORC_OBJ_BOUNDARY_QUADRATIC = 20, /* (x1+1)^2 */
+  /* a user objective (include/pps.h pps_objective_register): user_fn, the
+   * same source compiled as C (pps_point = const float*, PPS_DEVICE empty) */
+  ORC_OBJ_USER = 256,
 };
+
+/* f(x, dim, p, data, ndata) of a user objective, x contiguous */
+typedef float (*orc_user_fn)(const float* x, int dim, const float* p, const float* data, long long ndata);
 
 struct orc_ode_fit;
 
@@ -86,6 +92,10 @@ typedef struct orc_problem {
    * cons = ncons rows of (c_k, a_k[dim], b_k[dim]) */
   int32_t ncons;
   const float* cons;
+  /* ORC_OBJ_USER: the function and its data buffer */
+  orc_user_fn user_fn;
+  const float* user_data;
+  int64_t user_ndata;
 } orc_problem;
 
 /* structure-of-arrays swarm state: x[d*n + i] */

@@ -32,11 +32,16 @@ class OdeFit(ctypes.Structure):
                 ("nsaves", ctypes.c_int32), ("data", _fp), ("fixed", ctypes.c_float * 4)]
 
 
+USER_FN = ctypes.CFUNCTYPE(ctypes.c_float, _fp, ctypes.c_int, _fp, _fp, ctypes.c_longlong)
+OBJ_USER = 256
+
+
 class Problem(ctypes.Structure):
     _fields_ = [("objective", ctypes.c_int32), ("dim", ctypes.c_int32), ("lb", _fp), ("ub", _fp),
                 ("u0", _fp), ("params", ctypes.c_float * 8), ("nparams", ctypes.c_int32),
                 ("ode", ctypes.POINTER(OdeFit)), ("mlp_data", _fp), ("mlp_samples", ctypes.c_int32),
-                ("ncons", ctypes.c_int32), ("cons", _fp)]
+                ("ncons", ctypes.c_int32), ("cons", _fp),
+                ("user_fn", USER_FN), ("user_data", _fp), ("user_ndata", ctypes.c_int64)]
 
 
 class SwarmC(ctypes.Structure):
@@ -134,7 +139,7 @@ class OracleProblem:
     """orc_problem over numpy buffers (objective ids are include/pps.h's)."""
 
     def __init__(self, objective: int, dim: int, lb=None, ub=None, u0=None, params=(), ode=None, mlp_data=None,
-                 cons=None):
+                 cons=None, user=None, user_data=None):
         self.dim = int(dim)
         self.lb = np.ascontiguousarray(np.full(dim, -np.inf, np.float32) if lb is None else np.asarray(lb, np.float32))
         self.ub = np.ascontiguousarray(np.full(dim, np.inf, np.float32) if ub is None else np.asarray(ub, np.float32))
@@ -155,6 +160,15 @@ class OracleProblem:
             self.cons = np.ascontiguousarray(np.asarray(cons, np.float32).reshape(-1, 1 + 2 * self.dim))
             self.c.ncons = self.cons.shape[0]
             self.c.cons = fp(self.cons)
+        self.user = user  # UserObjective: objective is OBJ_USER, f is its C build
+        self.user_data = None
+        if user is not None:
+            self.c.objective = OBJ_USER
+            self.c.user_fn = user.fn
+            if user_data is not None:
+                self.user_data = np.ascontiguousarray(np.asarray(user_data, np.float32).reshape(-1))
+                self.c.user_data = fp(self.user_data)
+                self.c.user_ndata = self.user_data.size
         self.mlp_data = None
         if mlp_data is not None:  # S x 16 samples followed by S targets
             self.mlp_data = np.ascontiguousarray(np.asarray(mlp_data, np.float32).reshape(-1))
@@ -286,3 +300,49 @@ def mlp_loss(x, X, y) -> float:
     X = np.ascontiguousarray(np.asarray(X, np.float32))
     y = np.ascontiguousarray(np.asarray(y, np.float32))
     return float(load().orc_mlp_loss(fp(x), fp(X), fp(y), int(y.size)))
+
+
+# the prefix that makes the source of a user objective (the CUDA C of
+# pps_objective_register) a C translation unit: the same arithmetic, with the
+# oracle's exp / cos 2 pi x / sin 2 pi x for the library's own functions
+_USER_PREFIX = """#include <math.h>
+typedef const float* pps_point;
+#define PPS_DEVICE
+float orc_exp(float x);
+float orc_cos2pi(float x);
+float orc_sin2pi(float x);
+#define pps_exp orc_exp
+#define pps_cos2pi orc_cos2pi
+#define pps_sin2pi orc_sin2pi
+#line 1 "objective"
+"""
+
+
+class UserObjective:
+    """A user objective's source compiled as C by gcc (-ffp-contract=off) into
+    oracle/_build/user_<hash>.so, linked against the oracle for pps_exp etc."""
+
+    def __init__(self, source: str):
+        import hashlib
+        load()
+        h = hashlib.sha256(source.encode()).hexdigest()[:16]
+        so = HERE / "_build" / f"user_{h}.so"
+        if not so.exists():
+            c = HERE / "_build" / f"user_{h}.c"
+            c.write_text(_USER_PREFIX + source + "\n")
+            tmp = so.with_suffix(f".{os.getpid()}.tmp")
+            subprocess.run(["gcc", "-O2", "-fPIC", "-shared", "-std=gnu11", "-ffp-contract=off", "-fno-fast-math",
+                            "-o", str(tmp), str(c), str(LIB_PATH), f"-Wl,-rpath,{LIB_PATH.parent}", "-lm"],
+                           check=True, capture_output=True, text=True)
+            os.replace(tmp, so)
+        self.source = source
+        self.lib = ctypes.CDLL(str(so))
+        self.fn = USER_FN(ctypes.cast(self.lib.pps_objective, ctypes.c_void_p).value)
+
+    def __call__(self, x, params=(), data=None) -> float:
+        x = np.ascontiguousarray(np.asarray(x, np.float32))
+        p = np.zeros(8, np.float32)
+        p[:len(params)] = params
+        d = None if data is None else np.ascontiguousarray(np.asarray(data, np.float32).reshape(-1))
+        return float(self.fn(fp(x), x.size, fp(p), fp(d) if d is not None else ctypes.cast(None, _fp),
+                             0 if d is None else d.size))

@@ -19,7 +19,7 @@
 
 namespace pps {
 
-static thread_local char g_err[512] = "";
+static thread_local char g_err[4096] = "";
 
 int set_error(int code, const char* fmt, ...) {
   va_list ap;
@@ -53,7 +53,7 @@ static bool supported_objective(int obj) {
     case kShiftedSphere:
       return true;
     default:
-      return false;
+      return is_user(obj);
   }
 }
 
@@ -66,7 +66,7 @@ static int check_problem(const pps_problem* prob) {
   if (prob->nparams > 0 && !prob->params) return set_error(PPS_EINVAL, "params is NULL");
   if (!supported_objective(prob->objective))
     return set_error(PPS_ENOTSUP, "objective %d is not supported by this entry point", prob->objective);
-  if ((prob->objective >= kBeale) && prob->dim > 2)
+  if (prob->objective >= kBeale && prob->objective <= kBoundaryQuadratic && prob->dim > 2)
     return set_error(PPS_EINVAL, "objective %d is defined for dim <= 2", prob->objective);
   if (is_ode(prob->objective)) {
     const int rc = ode_check(prob);
@@ -76,6 +76,8 @@ static int check_problem(const pps_problem* prob) {
     const int rc = mlp_check(prob);
     if (rc) return rc;
   }
+  if (is_user(prob->objective) && prob->ndata != 0 && (prob->ndata < 0 || !prob->data))
+    return set_error(PPS_EINVAL, "data is NULL or ndata is negative");
   if (prob->ncons < 0 || prob->ncons > kMaxCons)
     return set_error(PPS_EINVAL, "ncons must be in [0, %d] (got %d)", kMaxCons, prob->ncons);
   if (prob->ncons > 0) {
@@ -423,7 +425,15 @@ static int run_steps(pps_swarm* s, int32_t maxiters, float c1, float c2, uint32_
   int rc;
   const uint32_t saved = s->flags;
   s->flags = run_flags;
-  if (!is_ode(s->objective)) sync_grid(s);  // resolve occupancy outside any capture
+  // resolve occupancy (and load a user objective's kernels) outside any capture
+  if (is_user(s->objective)) {
+    if ((rc = user_prepare(s))) {
+      s->flags = saved;
+      return rc;
+    }
+  } else if (!is_ode(s->objective)) {
+    sync_grid(s);
+  }
   if (maxiters >= kGraphChunk) {
     const bool stale = !s->graph || s->graph_len != kGraphChunk || s->graph_async_lanes != (int)run_flags ||
                        s->graph_c1 != c1 || s->graph_c2 != c2;
@@ -509,6 +519,8 @@ int pps_async_run(pps_swarm* s, int32_t maxiters, float w, float wdamp, float c1
     return set_error(PPS_ENOTSUP, "the MLP objective runs synchronously (tensor-core evaluation); use pps_sync_run");
   if (s->dv.ncons > 0)
     return set_error(PPS_ENOTSUP, "constrained problems run with pps_sync_run / pps_queue_run");
+  if (is_user(s->objective))
+    return set_error(PPS_ENOTSUP, "user objectives run with pps_sync_run / pps_queue_run");
   if ((rc = launch_set_iter(s, s->t, w, wdamp))) return rc;
   PPS_CUDA(cudaEventRecord(s->ev0, s->stream));
   int lanes = 0;
@@ -682,7 +694,7 @@ int pps_eval_objective(const pps_problem* prob, int64_t npoints, const float* x,
   ObjData od{};
   float* ddata = nullptr;
   rc = PPS_OK;
-  if (is_ode(prob->objective)) {
+  if (is_ode(prob->objective) || (is_user(prob->objective) && prob->ndata > 0)) {
     if ((e = cudaMallocAsync(&ddata, sizeof(float) * (size_t)prob->ndata, st)) != cudaSuccess) rc = cuda_error(e, "cudaMallocAsync");
     if (!rc && (e = cudaMemcpyAsync(ddata, prob->data, sizeof(float) * (size_t)prob->ndata, cudaMemcpyHostToDevice, st)) != cudaSuccess)
       rc = cuda_error(e, "cudaMemcpy");

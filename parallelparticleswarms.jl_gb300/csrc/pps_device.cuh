@@ -17,9 +17,17 @@
 // pi^k/k! rounded to binary32, and Cody-Waite reduction by ln 2 followed by
 // the Taylor series of exp.  Accuracy: <= 1.7 ulp (cos/sin), <= 0.9 ulp (exp).
 #pragma once
+#ifdef __CUDACC_RTC__
+// NVRTC (the kernels of a user objective) has no standard headers
+typedef unsigned char uint8_t;
+typedef unsigned int uint32_t;
+typedef unsigned long long uint64_t;
+typedef long long int64_t;
+#else
 #include <cstdint>
 
 #include <cuda_runtime.h>
+#endif
 
 namespace pps {
 
@@ -73,6 +81,7 @@ __device__ __forceinline__ Rand4 philox4x32_10(uint32_t c0, uint32_t c1, uint32_
 struct PhiloxKeys {
   uint32_t k[20];
 };
+#ifndef __CUDACC_RTC__
 inline PhiloxKeys philox_round_keys(uint64_t seed) {
   PhiloxKeys K;
   uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
@@ -84,6 +93,7 @@ inline PhiloxKeys philox_round_keys(uint64_t seed) {
   }
   return K;
 }
+#endif
 __device__ __forceinline__ Rand4 philox4x32_10(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3,
                                                const PhiloxKeys& K) {
 #pragma unroll

@@ -10,51 +10,9 @@
 
 #include "../../include/pps.h"
 #include "pps_device.cuh"
+#include "pps_state.cuh"
 
 namespace pps {
-
-// Device-resident iteration state of one swarm.  The last block of every
-// step launch publishes the new global best here and advances t and w, so
-// consecutive launches need no host round trip and capture into a CUDA graph
-// with identical parameters.
-struct IterState {
-  unsigned long long key;  // running argmin key of the current launch
-  unsigned int count;      // blocks finished in the current launch
-  unsigned int t;          // iteration counter of the next launch
-  float w;                 // inertia weight of the next launch
-  float wdamp;
-  float gcost;             // global best cost
-  unsigned int gidx;       // global best particle
-  unsigned int status;     // nonzero: a kernel detected a bad launch
-  unsigned int tile_next;  // step kernel: next tile to hand out (0 at launch start)
-  unsigned int pad[6];
-};
-
-// Swarm state in HBM (structure of arrays, particle index fastest):
-//   X, V, P   [dim][npad] float   position, velocity, personal best
-//   pcost     [npad] float        personal best cost
-//   cost      [npad] float        current cost
-//   flag      [npad] uint8        1: personal best improved in the last step
-//                                  and not yet copied (P lags X by one step)
-//   g         [dim] float         global best position
-//   lb, ub    [dim] float
-struct SwarmDev {
-  float* X;
-  float* V;
-  float* P;
-  float* pcost;
-  float* cost;
-  uint8_t* flag;
-  float* g;
-  float* lb;
-  float* ub;
-  IterState* st;
-  int64_t n;
-  int64_t npad;
-  int dim;
-  int ncons;          // constraints of the penalty path (0: none)
-  const float* cons;  // ncons rows of (c_k, a_k[dim], b_k[dim])
-};
 
 struct ObjData {
   const float* data;  // device copy of the objective's data (ODE obs, MLP set)
@@ -91,6 +49,7 @@ struct pps_swarm {
   int local_valid = 0;
   void* mlp_a_dev = nullptr;  // MLP objective: the samples as bf16 tensor-core tiles
   bool owns_memory = true;    // false: device block and stream belong to a server
+  int user_grid = 0;          // user objective: blocks of its step kernel (0: not resolved yet)
 };
 
 namespace pps {
@@ -141,6 +100,13 @@ int swarm_enqueue_init(pps_swarm* s);
 int swarm_enqueue_run(pps_swarm* s, int32_t maxiters, float w, float wdamp, float c1, float c2);
 // gbest (dim floats), its cost and index into mail, then done = 1, visible to the host
 int launch_publish_result(pps_swarm* s, float* mail, int* done);
+// user objectives compiled at run time (pps_user.cu)
+bool is_user(int objective);
+int user_prepare(pps_swarm* s);  // loads the kernels and sizes the grid; call outside stream capture
+int launch_user_init(pps_swarm* s, int sampler, const float* u0_dev);
+int launch_user_step(pps_swarm* s, float c1, float c2);
+int launch_user_eval(const ObjParams& op, const ObjData& od, int objective, const float* x, int64_t npts,
+                     int64_t stride, float* f, cudaStream_t stream);
 int launch_mlp_points(const float* data_dev, int64_t ndata, const uint8_t* a_dev, const float* x, int64_t npts,
                       int64_t stride, float* f, unsigned int* status, cudaStream_t stream);
 

@@ -6,7 +6,7 @@
 // gathers the winner's vector into the global-best buffer.  No block ever
 // waits for another.
 #pragma once
-#include "pps_internal.h"
+#include "pps_state.cuh"
 
 namespace pps {
 

@@ -294,6 +294,7 @@ __global__ void k_eval(ObjParams op, const float* __restrict__ x, int64_t npts, 
   }
 
 int launch_init(pps_swarm* s, int sampler, const float* u0_dev) {
+  if (is_user(s->objective)) return launch_user_init(s, sampler, u0_dev);
   const int64_t blocks = (s->dv.npad + kSyncThreads - 1) / kSyncThreads;
 #define L_INIT(O) k_init<O><<<(unsigned)blocks, kSyncThreads, 0, s->stream>>>(s->dv, s->op, s->seed, sampler, u0_dev)
 #define L_INIT_CONS(O) \
@@ -373,6 +374,7 @@ int sync_grid(pps_swarm* s) {
 }
 
 int launch_sync_step(pps_swarm* s, float c1, float c2) {
+  if (is_user(s->objective)) return launch_user_step(s, c1, c2);
   const int grid = sync_grid(s);
   const PhiloxKeys keys = philox_round_keys(s->seed);
   const size_t smem = 3 * sizeof(float) * (size_t)s->dv.dim;
@@ -432,7 +434,7 @@ int launch_materialize(pps_swarm* s) {
 
 int launch_eval(const ObjParams& op, const ObjData& od, int objective, const float* x, int64_t npts,
                 int64_t stride, float* f, cudaStream_t stream) {
-  (void)od;
+  if (is_user(objective)) return launch_user_eval(op, od, objective, x, npts, stride, f, stream);
   const int64_t blocks = (npts + 255) / 256;
 #define L_EVAL(O) k_eval<O><<<(unsigned)blocks, 256, 0, stream>>>(op, x, npts, stride, f)
   PPS_DISPATCH_SEPARABLE(objective, L_EVAL)

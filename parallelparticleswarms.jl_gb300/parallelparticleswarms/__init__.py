@@ -7,8 +7,8 @@ from ._lib import ArgumentError, PPSError
 from .algorithms import (BFGS, CUDA, GPUUniformSampler, GPUUnboundedSampler, HybridPSO, ParallelPSOKernel,
                          ParallelSyncPSOKernel, PSOAlgorithm, SimpleLBFGS)
 from .problem import (REGISTRY, Objective, OptimizationProblem, ackley, beale, booth, boundary_quadratic,
-                      evaluate, fitzhugh_nagumo_fit, himmelblau, lotka_volterra_fit, mlp_regression,
-                      quadratic, quadratic_constraint, rastrigin, rosenbrock, shifted_sphere, sphere)
+                      cuda_objective, evaluate, fitzhugh_nagumo_fit, himmelblau, lotka_volterra_fit,
+                      mlp_regression, quadratic, quadratic_constraint, rastrigin, rosenbrock, shifted_sphere, sphere)
 from .solve import (HybridPSOCache, OptimizationSolution, OptimizationStats, PSOCache, init, reinit_, solve,
                     solve_)
 from .swarm import Swarm
@@ -22,6 +22,6 @@ __all__ = [
     "PSOCache", "HybridPSOCache", "OptimizationSolution", "OptimizationStats", "Swarm", "PPSError",
     "ArgumentError", "evaluate", "Objective", "REGISTRY", "sphere", "rosenbrock", "rastrigin", "ackley",
     "lotka_volterra_fit", "fitzhugh_nagumo_fit", "mlp_regression", "beale", "booth", "himmelblau",
-    "quadratic", "boundary_quadratic", "shifted_sphere", "quadratic_constraint", "CUDA", "Batch", "Server", "ode",
-    "mlp",
+    "quadratic", "boundary_quadratic", "shifted_sphere", "quadratic_constraint", "cuda_objective", "CUDA",
+    "Batch", "Server", "ode", "mlp",
 ]

@@ -174,6 +174,7 @@ _SIGNATURES = {
                                         ctypes.POINTER(ctypes.c_int64), c_float_p]),
     "pps_hybrid_bfgs": (ctypes.c_int, [_P, ctypes.POINTER(LocalOpts), c_float_p, c_float_p,
                                        ctypes.POINTER(ctypes.c_int64), c_float_p]),
+    "pps_objective_register": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(ctypes.c_int32)]),
     "pps_sync_run_noalloc": (ctypes.c_int, [ctypes.c_int32, c_float_p, ctypes.c_int32, ctypes.POINTER(DeviceSwarm),
                                             ctypes.c_uint64, ctypes.c_uint32, ctypes.c_int32, ctypes.c_float,
                                             ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_uint32,

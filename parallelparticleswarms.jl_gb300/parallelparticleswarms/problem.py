@@ -5,7 +5,9 @@ an arbitrary Julia function ``f(x, p)`` that its kernels compile in
 (src/kernels.jl:33).  Through a C ABI the objective is chosen from the
 engine's registry; the objects below name the registry entries and carry
 their default parameters.  They are markers, not Python callables: objective
-values are always computed on the GPU (``evaluate`` below).
+values are always computed on the GPU (``evaluate`` below).  Any other
+objective is given as CUDA C source (``cuda_objective``), which the library
+compiles at run time into its own kernels.
 """
 from __future__ import annotations
 
@@ -23,6 +25,7 @@ class Objective:
     id: int
     default_params: tuple = ()
     max_dim: int | None = None
+    source: str | None = field(default=None, repr=False, compare=False)
 
     def __repr__(self) -> str:
         return f"<objective {self.name}>"
@@ -47,6 +50,26 @@ boundary_quadratic = Objective("boundary_quadratic", 20, (), 1)
 REGISTRY = {o.name: o for o in (sphere, rosenbrock, rastrigin, ackley, lotka_volterra_fit,
                                fitzhugh_nagumo_fit, mlp_regression, shifted_sphere, beale, booth, himmelblau,
                                quadratic, boundary_quadratic)}
+
+
+def cuda_objective(source: str, name: str = "user", default_params=()) -> Objective:
+    """An objective given as CUDA C source, the counterpart of the arbitrary
+    ``f(x, p)`` the reference compiles into its kernels (src/kernels.jl:33).
+
+    The source defines ``PPS_DEVICE float pps_objective(pps_point x, int dim,
+    const float* p, const float* data, long long ndata)``: ``x[d]`` is the
+    point's coordinate d, ``p`` the problem's parameters (8 floats, zero past
+    the given ones), ``data`` the problem's ``data`` on the device.  NVRTC
+    compiles it (``pps_objective_register``) with the library's init, step
+    and evaluation kernels; ``pps_exp``, ``pps_cos2pi`` and ``pps_sin2pi`` are
+    the library's exp(x), cos(2 pi x) and sin(2 pi x).  Compile errors raise
+    ArgumentError with the compiler's log.  Runs with ParallelSyncPSOKernel,
+    ParallelPSOKernel(global_update=True), ``evaluate`` and ``Server``;
+    the async kernel, HybridPSO and batches do not take it.
+    """
+    oid = ctypes.c_int32()
+    _lib.check(_lib.load().pps_objective_register(source.encode(), ctypes.byref(oid)))
+    return Objective(name, int(oid.value), tuple(float(v) for v in default_params), source=source)
 
 
 def quadratic_constraint(dim: int, c: float = 0.0, a=None, b=None) -> np.ndarray:
@@ -96,8 +119,8 @@ class OptimizationProblem:
         if isinstance(self.f, str):
             self.f = REGISTRY[self.f]
         if not isinstance(self.f, Objective):
-            raise _lib.ArgumentError(_lib.EINVAL, "f must be a registered objective (see problem.REGISTRY); "
-                                                  "the engine has no path for arbitrary Python callables")
+            raise _lib.ArgumentError(_lib.EINVAL, "f must be a registered objective (see problem.REGISTRY) or a "
+                                                  "cuda_objective; the engine has no path for Python callables")
         self.u0 = _f32(self.u0)
         self.dim = int(self.u0.size)
         if self.p is None:

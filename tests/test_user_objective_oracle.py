@@ -1,0 +1,76 @@
+"""User objectives on the CPU: the oracle's C build of a user source agrees
+bit for bit with the registered objectives it restates, a swarm over it runs
+the registered swarm's iterations, and the library compiles sources with
+NVRTC (no GPU needed) and reports compile errors with the compiler's log."""
+import numpy as np
+import pytest
+
+import user_sources as us
+
+
+def _points(D, n, lo, hi, seed):
+    return np.random.default_rng(seed).uniform(lo, hi, (n, D)).astype(np.float32)
+
+
+@pytest.mark.parametrize("src,obj,D,params", [
+    (us.ROSENBROCK, 1, 7, [1.0, 100.0]),
+    (us.RASTRIGIN, 2, 33, [10.0]),
+    (us.SHIFTED_SPHERE, 7, 5, [2.0, 1.0, -0.5]),
+])
+def test_user_source_matches_registered_objective(orc, src, obj, D, params):
+    user = orc.UserObjective(src)
+    reg = orc.OracleProblem(obj, D, params=params)
+    for x in _points(D, 500, -5.12, 5.12, seed=D):
+        want = np.float32(reg.objective(x))
+        got = np.float32(user(x, params))
+        assert got == want or (np.isnan(got) and np.isnan(want)), (x, got, want)
+
+
+def test_user_swarm_runs_the_registered_iterations(orc):
+    D, n = 3, 300
+    lb, ub = np.full(D, -1, np.float32), np.full(D, 10, np.float32)
+    user = orc.UserObjective(us.ROSENBROCK)
+    a = orc.OracleSwarm(orc.OracleProblem(1, D, lb, ub, params=[1.0, 100.0]), n, 4).init()
+    b = orc.OracleSwarm(orc.OracleProblem(0, D, lb, ub, params=[1.0, 100.0], user=user), n, 4).init()
+    a.sync_run(25)
+    b.sync_run(25)
+    for k in ("x", "v", "pbest", "pcost", "cost"):
+        assert np.array_equal(a.state()[k], b.state()[k]), k
+    assert a.gidx == b.gidx
+
+
+def test_user_data_objective_on_the_oracle(orc):
+    t = np.linspace(-1, 1, 40, dtype=np.float32)
+    y = (0.5 - 2.0 * t + 3.0 * t * t).astype(np.float32)
+    data = np.concatenate([t, y])
+    user = orc.UserObjective(us.POLYFIT)
+    assert user([0.5, -2.0, 3.0], data=data) < 1e-12
+    assert user([0.0, 0.0, 0.0], data=data) > 1.0
+
+
+def _register(pps, src):
+    try:
+        return pps.cuda_objective(src)
+    except pps.PPSError as e:
+        if e.code == 6:  # PPS_ENOTSUP: no NVRTC on this machine
+            pytest.skip(str(e))
+        raise
+
+
+def test_register_compiles_and_deduplicates():
+    pkg = pytest.importorskip("parallelparticleswarms")
+    a = _register(pkg, us.ROSENBROCK)
+    b = _register(pkg, us.ROSENBROCK)
+    c = _register(pkg, us.RASTRIGIN)
+    assert a.id == b.id >= 256 and c.id != a.id
+    assert a.source == us.ROSENBROCK
+
+
+def test_register_reports_compile_errors():
+    pkg = pytest.importorskip("parallelparticleswarms")
+    _register(pkg, us.SHIFTED_SPHERE)  # skips without NVRTC
+    with pytest.raises(pkg.ArgumentError) as e:
+        pkg.cuda_objective(us.HEAD + " { return undefined_name; }")
+    assert "objective(1)" in str(e.value) and "undefined_name" in str(e.value)
+    with pytest.raises(pkg.ArgumentError):
+        pkg.cuda_objective("")

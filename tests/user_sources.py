@@ -1,0 +1,74 @@
+"""Sources of user objectives shared by the CPU and GPU tests.
+
+Each is the CUDA C of pps_objective_register and, with the oracle's prefix,
+plain C for the CPU restatement.  ROSENBROCK and RASTRIGIN spell the
+registered objectives' operations in the same order (src/kernels.jl:33 with
+f from test/regression.jl:12-18 and the Rastrigin formula), so a swarm over
+them reproduces the registered swarm bit for bit."""
+
+HEAD = "PPS_DEVICE float pps_objective(pps_point x, int dim, const float* p, const float* data, long long ndata)"
+
+ROSENBROCK = HEAD + """ {
+  float s = 0.0f;
+  for (int i = 0; i + 1 < dim; ++i) {
+    const float t = x[i + 1] - x[i] * x[i];
+    const float u = p[0] - x[i];
+    s = s + (p[1] * (t * t) + u * u);
+  }
+  return s;
+}
+"""
+
+RASTRIGIN = HEAD + """ {
+  float s = 0.0f;
+  for (int i = 0; i < dim; ++i) s = s + (x[i] * x[i] - p[0] * pps_cos2pi(x[i]));
+  return p[0] * (float)dim + s;
+}
+"""
+
+SHIFTED_SPHERE = HEAD + """ {
+  float s = 0.0f;
+  for (int i = 0; i < dim; ++i) {
+    const float t = x[i] - (i < 8 ? p[i] : 0.0f);
+    s = s + t * t;
+  }
+  return s;
+}
+"""
+
+# mean squared residual of a quadratic model y = x0 + x1 t + x2 t^2 over the
+# samples data = (t_0..t_{m-1}, y_0..y_{m-1})
+POLYFIT = HEAD + """ {
+  const long long m = ndata / 2;
+  float s = 0.0f;
+  for (long long k = 0; k < m; ++k) {
+    const float t = data[k];
+    const float r = (x[0] + x[1] * t + x[2] * (t * t)) - data[m + k];
+    s = s + r * r;
+  }
+  return s / (float)m;
+}
+"""
+
+# Styblinski-Tang plus a square-root term: IEEE sqrt on both sides
+STYBLINSKI_SQRT = HEAD + """ {
+  float s = 0.0f;
+  for (int i = 0; i < dim; ++i) {
+    const float v = x[i];
+    const float v2 = v * v;
+    s = s + ((v2 * v2 - 16.0f * v2) + 5.0f * v);
+  }
+  return 0.5f * s + sqrtf(fabsf(x[0]));
+}
+"""
+
+# Griewank with the library's cos and a branch on the data
+GRIEWANK = HEAD + """ {
+  float s = 0.0f, q = 1.0f;
+  for (int i = 0; i < dim; ++i) {
+    s = s + x[i] * x[i];
+    q = q * pps_cos2pi(x[i] / (6.2831855f * sqrtf((float)(i + 1))));
+  }
+  return (s / 4000.0f - q) + 1.0f;
+}
+"""
