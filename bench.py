@@ -275,6 +275,41 @@ def run_ode_batch(pps, count_each=512) -> dict:
             "block_shape": shape}
 
 
+# the Rastrigin objective written as the CUDA C source of a user objective
+USER_RASTRIGIN = """PPS_DEVICE float pps_objective(pps_point x, int dim, const float* p, const float* data,
+                                long long ndata) {
+  float s = 0.0f;
+  for (int i = 0; i < dim; ++i) s = s + (x[i] * x[i] - p[0] * pps_cos2pi(x[i]));
+  return p[0] * (float)dim + s;
+}
+"""
+
+
+def run_user(pps, n: int = N_PARTICLES, iters: int = ITERS) -> dict:
+    """C2 Rastrigin (n x 100-D, bounds [-5.12, 5.12]) with f given as CUDA C
+    source: the NVRTC-compiled step kernel of a user objective against the
+    registered kernel, same seed, same result."""
+    lb, ub = np.full(DIM, LO, np.float32), np.full(DIM, HI, np.float32)
+    reg = pps.OptimizationProblem(pps.rastrigin, np.zeros(DIM, np.float32), [10.0], lb=lb, ub=ub)
+    usr = reg.remake(f=pps.cuda_objective(USER_RASTRIGIN, "rastrigin_source"))
+    res = {}
+    for key, prob in (("registered", reg), ("source", usr)):
+        with pps.Swarm(prob, n, seed=2) as sw:
+            sw.init()
+            sw.sync_run(10)  # warm (the first use loads the compiled library)
+            sw.init()
+            ms = sw.sync_run(iters)
+            res[key] = (ms, sw.gbest())
+    ms = res["source"][0]
+    return {"workload": f"{n} particles x {DIM}-D Rastrigin, {iters} sync iterations, f as CUDA C source "
+                        "(NVRTC, 2 particles per thread)",
+            "device_ms": ms, "particle_iters_per_s": n * iters / (ms / 1e3),
+            "hbm_gbs": n * BYTES_PER_PARTICLE_ITER / (ms / iters / 1e3) / 1e9,
+            "registered_device_ms": res["registered"][0], "vs_registered": res["registered"][0] / ms,
+            "same_result_as_registered": bool(np.array_equal(res["source"][1][0], res["registered"][1][0])
+                                              and res["source"][1][2] == res["registered"][1][2])}
+
+
 def run_configs(pps) -> dict:
     """The other sync configurations of the workload: C1 (3-D Rosenbrock, p =
     [1, 100], bounds [-1, 10], 1000 particles, 500 iterations: the reference's
@@ -534,7 +569,10 @@ def main():
     ap.add_argument("--no-async", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the hybrid, ODE-batch and served measurements")
     ap.add_argument("--mlp-iters", type=int, default=100, help="iterations of the MLP-fit measurement")
-    ap.add_argument("--only", choices=["sync", "async", "hybrid", "ode", "serve", "mlp", "configs"], default=None,
+    ap.add_argument("--user-n", type=int, default=N_PARTICLES,
+                    help="particles of the user-objective (CUDA C source) measurement")
+    ap.add_argument("--only", choices=["sync", "async", "hybrid", "ode", "serve", "mlp", "configs", "user"],
+                    default=None,
                     help="run one workload only (for profiling); prints its result")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU-baseline sample")
     ap.add_argument("--serve-requests", type=int, default=1500,
@@ -573,11 +611,12 @@ def main():
     iters = args.iters
     seed0 = multi.swarm_seed(0, rank)
 
-    if args.only in ("hybrid", "ode", "serve", "mlp", "configs"):
+    if args.only in ("hybrid", "ode", "serve", "mlp", "configs", "user"):
         fn = {"hybrid": lambda: run_hybrid(pps), "ode": lambda: run_ode_batch(pps, args.ode_fits),
               "serve": lambda: {"served": run_served(pps, args, True),
                                 "served_without_mlp": run_served(pps, args, False)},
-              "mlp": lambda: run_mlp(pps, args.mlp_iters), "configs": lambda: run_configs(pps)}[args.only]
+              "mlp": lambda: run_mlp(pps, args.mlp_iters), "configs": lambda: run_configs(pps),
+              "user": lambda: run_user(pps, args.user_n)}[args.only]
         if rank == 0:
             print(json.dumps({args.only: fn()}), flush=True)
         return 0
@@ -655,6 +694,7 @@ def main():
         extras["served_without_mlp"] = run_served(pps, args, False)
         extras["mlp"] = run_mlp(pps, args.mlp_iters)
         extras["configs"] = run_configs(pps)
+        extras["user_objective"] = run_user(pps, args.user_n)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline and args.only is None:

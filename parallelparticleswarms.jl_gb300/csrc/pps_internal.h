@@ -50,6 +50,7 @@ struct pps_swarm {
   void* mlp_a_dev = nullptr;  // MLP objective: the samples as bf16 tensor-core tiles
   bool owns_memory = true;    // false: device block and stream belong to a server
   int user_grid = 0;          // user objective: blocks of its step kernel (0: not resolved yet)
+  const void* user_step_kernel = nullptr;  // user objective: the step kernel variant in use
 };
 
 namespace pps {

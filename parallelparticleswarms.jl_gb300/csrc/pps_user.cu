@@ -93,7 +93,9 @@ struct UserObjective {
   std::mutex load_mu;
   std::atomic<bool> loaded{false};
   cudaLibrary_t lib = nullptr;
-  cudaKernel_t k_init = nullptr, k_step = nullptr, k_eval = nullptr;
+  cudaKernel_t k_init = nullptr, k_eval = nullptr;
+  cudaKernel_t k_step[3] = {};  // 1, 2, 4 particles per thread
+  cudaKernel_t k_step_cons = nullptr;
 };
 
 constexpr int kMaxUser = 4096;
@@ -134,8 +136,16 @@ int compile(const std::string& user, int arch, std::vector<char>* out) {
   // for); the plain target of any other device
   const std::string target =
       "--gpu-architecture=sm_" + std::to_string(arch) + (arch >= 90 ? "a" : "");
-  const char* opts[] = {target.c_str(), "-std=c++17", "--fmad=false", "-lineinfo", "-DPPS_RTC=1"};
-  r = api.compile(prog, (int)(sizeof(opts) / sizeof(opts[0])), opts);
+  // PPS_USER_MINBLOCKS=N overrides the resident blocks the step kernel is
+  // compiled for (register cap); the default is the header's
+  std::string minblocks;
+  if (const char* mb = getenv("PPS_USER_MINBLOCKS")) {
+    const int v = atoi(mb);
+    if (v >= 1 && v <= 8) minblocks = "-DPPS_USER_MINBLOCKS=" + std::to_string(v);
+  }
+  std::vector<const char*> opts = {target.c_str(), "-std=c++17", "--fmad=false", "-lineinfo"};
+  if (!minblocks.empty()) opts.push_back(minblocks.c_str());
+  r = api.compile(prog, (int)opts.size(), opts.data());
   if (r != NVRTC_SUCCESS) {
     size_t n = 0;
     std::string log;
@@ -165,7 +175,10 @@ int ensure_loaded(UserObjective* u) {
   if (u->loaded.load(std::memory_order_relaxed)) return PPS_OK;
   PPS_CUDA(cudaLibraryLoadData(&u->lib, u->cubin.data(), nullptr, nullptr, 0, nullptr, nullptr, 0));
   PPS_CUDA(cudaLibraryGetKernel(&u->k_init, u->lib, "pps_user_init"));
-  PPS_CUDA(cudaLibraryGetKernel(&u->k_step, u->lib, "pps_user_step"));
+  PPS_CUDA(cudaLibraryGetKernel(&u->k_step[0], u->lib, "pps_user_step1"));
+  PPS_CUDA(cudaLibraryGetKernel(&u->k_step[1], u->lib, "pps_user_step2"));
+  PPS_CUDA(cudaLibraryGetKernel(&u->k_step[2], u->lib, "pps_user_step4"));
+  PPS_CUDA(cudaLibraryGetKernel(&u->k_step_cons, u->lib, "pps_user_step_cons"));
   PPS_CUDA(cudaLibraryGetKernel(&u->k_eval, u->lib, "pps_user_eval"));
   u->loaded.store(true, std::memory_order_release);
   return PPS_OK;
@@ -183,6 +196,17 @@ UserObjective* loaded_or_error(int objective, int* rc) {
 
 constexpr int kUserThreads = 256;
 
+// particles per thread of the unconstrained step kernel; PPS_USER_PPT=1|2|4
+// overrides the default
+int user_step_ppt() {
+  static const int ppt = [] {
+    const char* e = getenv("PPS_USER_PPT");
+    const int v = e ? atoi(e) : 2;
+    return (v == 1 || v == 2 || v == 4) ? v : 2;
+  }();
+  return ppt;
+}
+
 }  // namespace
 
 bool is_user(int objective) { return lookup(objective) != nullptr; }
@@ -192,13 +216,20 @@ int user_prepare(pps_swarm* s) {
   UserObjective* u = loaded_or_error(s->objective, &rc);
   if (!u) return rc;
   if (s->user_grid > 0) return PPS_OK;
+  int ppt = 1;
+  const void* k = reinterpret_cast<const void*>(u->k_step_cons);
+  if (s->dv.ncons == 0) {
+    ppt = user_step_ppt();
+    k = reinterpret_cast<const void*>(u->k_step[ppt == 1 ? 0 : (ppt == 2 ? 1 : 2)]);
+  }
   const size_t smem = 3 * sizeof(float) * (size_t)s->dv.dim;
   int per_sm = 0;
-  PPS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, reinterpret_cast<const void*>(u->k_step),
-                                                         kUserThreads, smem));
+  PPS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kUserThreads, smem));
   if (per_sm < 1) return set_error(PPS_EINVAL, "the objective's step kernel cannot be resident (dim %d)", s->dv.dim);
-  const int64_t blocks = (s->dv.n + kUserThreads - 1) / kUserThreads;
+  const int64_t groups = (s->dv.n + ppt - 1) / ppt;
+  const int64_t blocks = (groups + kUserThreads - 1) / kUserThreads;
   const int64_t resident = (int64_t)per_sm * s->sm_count;
+  s->user_step_kernel = k;
   s->user_grid = (int)(blocks < resident ? blocks : resident);
   return PPS_OK;
 }
@@ -220,15 +251,13 @@ int launch_user_init(pps_swarm* s, int sampler, const float* u0_dev) {
 int launch_user_step(pps_swarm* s, float c1, float c2) {
   int rc;
   if ((rc = user_prepare(s))) return rc;
-  UserObjective* u = lookup(s->objective);
-  const size_t smem = 3 * sizeof(float) * (size_t)s->dv.dim;
   PhiloxKeys keys = philox_round_keys(s->seed);
   const float* data = s->od.data;
   long long ndata = (long long)s->od.ndata;
   int from_pos = (s->flags & PPS_FLAG_GBEST_FROM_POSITION) ? 1 : 0;
   void* args[] = {&s->dv, &s->op, &data, &ndata, &keys, &c1, &c2, &from_pos};
-  PPS_CUDA(cudaLaunchKernel(reinterpret_cast<const void*>(u->k_step), dim3((unsigned)s->user_grid),
-                            dim3(kUserThreads), args, smem, s->stream));
+  PPS_CUDA(cudaLaunchKernel(s->user_step_kernel, dim3((unsigned)s->user_grid), dim3(kUserThreads), args,
+                            3 * sizeof(float) * (size_t)s->dv.dim, s->stream));
   return PPS_OK;
 }
 

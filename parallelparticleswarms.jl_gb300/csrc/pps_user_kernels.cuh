@@ -16,6 +16,19 @@
 // problem carries constraints.
 #pragma once
 #include "pps_publish.cuh"
+#include "pps_vec.cuh"
+
+// resident blocks each kernel is compiled for (register cap 65536 / (256 x
+// blocks)): 4 leaves 64 registers a thread and 32 warps per SM for one or two
+// particles per thread, 2 leaves 128 for four.  PPS_USER_MINBLOCKS, when
+// defined, sets all of them.
+#ifdef PPS_USER_MINBLOCKS
+#define PPS_USER_MB4 PPS_USER_MINBLOCKS
+#define PPS_USER_MB2 PPS_USER_MINBLOCKS
+#else
+#define PPS_USER_MB4 4
+#define PPS_USER_MB2 2
+#endif
 
 namespace pps {
 
@@ -28,7 +41,7 @@ __device__ __forceinline__ void user_params(float* sp, const ObjParams& op) {
 
 }  // namespace pps
 
-extern "C" __global__ void __launch_bounds__(pps::kUserThreads)
+extern "C" __global__ void __launch_bounds__(pps::kUserThreads, PPS_USER_MB4)
     pps_user_init(pps::SwarmDev s, pps::ObjParams op, const float* data, long long ndata, unsigned long long seed,
                   int sampler, const float* u0) {
   using namespace pps;
@@ -81,12 +94,17 @@ extern "C" __global__ void __launch_bounds__(pps::kUserThreads)
   if (publish_block_min(key, s.st)) finish_iteration(s, false, 0u, s.st->w);
 }
 
-// One thread per particle, a grid of resident blocks striding over the
-// swarm.  Dims are walked in pairs, one Philox call per pair.
-extern "C" __global__ void __launch_bounds__(pps::kUserThreads)
-    pps_user_step(pps::SwarmDev s, pps::ObjParams op, const float* data, long long ndata, pps::PhiloxKeys keys,
-                  float c1, float c2, int from_position) {
-  using namespace pps;
+// Each thread owns PPT consecutive particles (float / float2 / float4 along
+// the particle axis, as the registered step kernel), the grid of resident
+// blocks strides over the groups.  Dims are walked in pairs, one Philox call
+// per particle and pair, the loads of the next pair issued before the current
+// pair is computed.  The objective then runs once per particle over the
+// column this thread has just written.
+namespace pps {
+
+template <int PPT, bool CONS>
+__device__ __forceinline__ void user_step(const SwarmDev& s, const ObjParams& op, const float* data, long long ndata,
+                                          const PhiloxKeys& keys, float c1, float c2, int from_position) {
   extern __shared__ float sm[];
   __shared__ float sp[8];
   const int D = s.dim;
@@ -104,48 +122,139 @@ extern "C" __global__ void __launch_bounds__(pps::kUserThreads)
   user_params(sp, op);
   __syncthreads();
   const int64_t npad = s.npad, n = s.n;
+  const int64_t ngroups = (n + PPT - 1) / PPT;  // the last group may hold padding
   float* X = s.X;  // not restrict: the objective reads back what this thread stores
   float* V = s.V;
   float* P = s.P;
   unsigned long long best = ~0ull;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const bool fl = s.flag[i] != 0;
-    ConsAcc ca;
-    if (s.ncons > 0) ca.start(s.cons, s.ncons, D);
-    for (int j = 0; j < D; j += 2) {
-      const Rand4 r = philox4x32_10((uint32_t)i, (uint32_t)(j >> 1), t, kTagStep, keys);
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < ngroups; q += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i0 = q * PPT;
+    uint8_t fl[PPT];
+    ldflags<PPT>(fl, s.flag + i0);
+    bool anyfl = false;
 #pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        const int d = j + h;
-        if (d >= D) break;
-        const int64_t o = (int64_t)d * npad + i;
-        float x = X[o], v = V[o], p = P[o];
-        if (fl) {  // the personal-best copy deferred from the last step
-          p = x;
-          P[o] = p;
+    for (int k = 0; k < PPT; ++k) anyfl |= (fl[k] != 0);
+    ConsAcc ca[PPT];
+    if constexpr (CONS) {
+#pragma unroll
+      for (int k = 0; k < PPT; ++k) ca[k].start(s.cons, s.ncons, D);
+    }
+    float xa[PPT], va[PPT], pa[PPT], xb[PPT], vb[PPT], pb[PPT];
+    ldv<PPT>(xa, X + i0);
+    ldv<PPT>(va, V + i0);
+    ldv<PPT>(pa, P + i0);
+    if (D > 1) {
+      ldv<PPT>(xb, X + npad + i0);
+      ldv<PPT>(vb, V + npad + i0);
+      ldv<PPT>(pb, P + npad + i0);
+    }
+    for (int j = 0; j < D; j += 2) {
+      float nxa[PPT], nva[PPT], npa[PPT], nxb[PPT], nvb[PPT], npb[PPT];
+      if (j + 2 < D) {
+        const int64_t o = (int64_t)(j + 2) * npad + i0;
+        ldv<PPT>(nxa, X + o);
+        ldv<PPT>(nva, V + o);
+        ldv<PPT>(npa, P + o);
+      }
+      if (j + 3 < D) {
+        const int64_t o = (int64_t)(j + 3) * npad + i0;
+        ldv<PPT>(nxb, X + o);
+        ldv<PPT>(nvb, V + o);
+        ldv<PPT>(npb, P + o);
+      }
+      Rand4 r[PPT];
+#pragma unroll
+      for (int k = 0; k < PPT; ++k) r[k] = philox4x32_10((uint32_t)(i0 + k), (uint32_t)(j >> 1), t, kTagStep, keys);
+      {  // dim j
+        const int64_t o = (int64_t)j * npad + i0;
+        if (anyfl) {  // the personal-best copies deferred from the last step
+#pragma unroll
+          for (int k = 0; k < PPT; ++k) pa[k] = fl[k] ? xa[k] : pa[k];
+          stv<PPT>(P + o, pa);
         }
-        v = velocity(x, v, p, sg[d], w, c1, c2, u01(h ? r.c : r.a), u01(h ? r.d : r.b));
-        x = clamp_lb_ub(__fadd_rn(x, v), slb[d], sub[d]);
-        X[o] = x;
-        V[o] = v;
-        if (s.ncons > 0) ca.add(s.cons, s.ncons, D, d, x);
+#pragma unroll
+        for (int k = 0; k < PPT; ++k) {
+          va[k] = velocity(xa[k], va[k], pa[k], sg[j], w, c1, c2, u01(r[k].a), u01(r[k].b));
+          xa[k] = clamp_lb_ub(__fadd_rn(xa[k], va[k]), slb[j], sub[j]);
+          if constexpr (CONS) ca[k].add(s.cons, s.ncons, D, j, xa[k]);
+        }
+        stv<PPT>(X + o, xa);
+        stv<PPT>(V + o, va);
+      }
+      if (j + 1 < D) {  // dim j + 1
+        const int64_t o = (int64_t)(j + 1) * npad + i0;
+        if (anyfl) {
+#pragma unroll
+          for (int k = 0; k < PPT; ++k) pb[k] = fl[k] ? xb[k] : pb[k];
+          stv<PPT>(P + o, pb);
+        }
+#pragma unroll
+        for (int k = 0; k < PPT; ++k) {
+          vb[k] = velocity(xb[k], vb[k], pb[k], sg[j + 1], w, c1, c2, u01(r[k].c), u01(r[k].d));
+          xb[k] = clamp_lb_ub(__fadd_rn(xb[k], vb[k]), slb[j + 1], sub[j + 1]);
+          if constexpr (CONS) ca[k].add(s.cons, s.ncons, D, j + 1, xb[k]);
+        }
+        stv<PPT>(X + o, xb);
+        stv<PPT>(V + o, vb);
+      }
+#pragma unroll
+      for (int k = 0; k < PPT; ++k) {
+        xa[k] = nxa[k]; va[k] = nva[k]; pa[k] = npa[k];
+        xb[k] = nxb[k]; vb[k] = nvb[k]; pb[k] = npb[k];
       }
     }
-    float c = pps_objective(pps_point{X + i, npad}, D, sp, data, ndata);
-    if (s.ncons > 0) c = __fadd_rn(c, penalty(ca, s.ncons, __uint2float_rn((uint32_t)(i + 2))));
-    float pc = s.pcost[i];
-    // if cost < best_cost: best = position (strict <, src/kernels.jl:21-24)
-    const bool imp = c < pc;
-    if (imp) {
-      pc = c;
-      s.pcost[i] = c;
+    float pc[PPT], cc[PPT];
+    ldv<PPT>(pc, s.pcost + i0);
+#pragma unroll
+    for (int k = 0; k < PPT; ++k) {
+      const bool valid = i0 + k < n;
+      float c = __int_as_float(0x7f800000);
+      if (valid) {
+        c = pps_objective(pps_point{X + i0 + k, npad}, D, sp, data, ndata);
+        if constexpr (CONS) c = __fadd_rn(c, penalty(ca[k], s.ncons, __uint2float_rn((uint32_t)(i0 + k + 2))));
+      }
+      cc[k] = c;
+      // if cost < best_cost: best = position (strict <, src/kernels.jl:21-24)
+      fl[k] = (valid && c < pc[k]) ? 1 : 0;
+      pc[k] = fl[k] ? c : pc[k];
+      if (valid) {
+        const unsigned long long key = argmin_key(pc[k], (uint32_t)(i0 + k));
+        best = key < best ? key : best;
+      }
     }
-    s.cost[i] = c;
-    s.flag[i] = imp ? 1 : 0;
-    const unsigned long long key = argmin_key(pc, (uint32_t)i);
-    best = key < best ? key : best;
+    stv<PPT>(s.pcost + i0, pc);
+    stv<PPT>(s.cost + i0, cc);
+    stflags<PPT>(s.flag + i0, fl);
   }
   if (publish_block_min(best, st)) finish_iteration(s, from_position != 0, t + 1u, __fmul_rn(w, st->wdamp));
+}
+
+}  // namespace pps
+
+extern "C" __global__ void __launch_bounds__(pps::kUserThreads, PPS_USER_MB4)
+    pps_user_step1(pps::SwarmDev s, pps::ObjParams op, const float* data, long long ndata, pps::PhiloxKeys keys,
+                   float c1, float c2, int from_position) {
+  pps::user_step<1, false>(s, op, data, ndata, keys, c1, c2, from_position);
+}
+
+extern "C" __global__ void __launch_bounds__(pps::kUserThreads, PPS_USER_MB4)
+    pps_user_step2(pps::SwarmDev s, pps::ObjParams op, const float* data, long long ndata, pps::PhiloxKeys keys,
+                   float c1, float c2, int from_position) {
+  pps::user_step<2, false>(s, op, data, ndata, keys, c1, c2, from_position);
+}
+
+// the constrained path: calc_penalty with iter = the 1-based particle index
+// (src/kernels.jl:77,151), one particle per thread
+extern "C" __global__ void __launch_bounds__(pps::kUserThreads, PPS_USER_MB4)
+    pps_user_step_cons(pps::SwarmDev s, pps::ObjParams op, const float* data, long long ndata,
+                       pps::PhiloxKeys keys, float c1, float c2, int from_position) {
+  pps::user_step<1, true>(s, op, data, ndata, keys, c1, c2, from_position);
+}
+
+extern "C" __global__ void __launch_bounds__(pps::kUserThreads, PPS_USER_MB2)
+    pps_user_step4(pps::SwarmDev s, pps::ObjParams op, const float* data, long long ndata, pps::PhiloxKeys keys,
+                   float c1, float c2, int from_position) {
+  pps::user_step<4, false>(s, op, data, ndata, keys, c1, c2, from_position);
 }
 
 // f[i] = objective at point i, coordinates x[d * stride + i]

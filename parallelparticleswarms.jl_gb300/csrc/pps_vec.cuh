@@ -1,9 +1,11 @@
 // pps_vec.cuh -- vector loads and stores of PPT consecutive particles
 // (float / float2 / float4 along the particle axis of the SoA state).
 #pragma once
+#ifndef __CUDACC_RTC__
 #include <cstdint>
 
 #include <cuda_runtime.h>
+#endif
 
 namespace pps {
 
