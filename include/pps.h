@@ -97,7 +97,11 @@ typedef struct pps_swarm pps_swarm;
 enum {
   PPS_SAMPLER_AUTO = 0,      /* unbounded if every bound is infinite, else uniform (src/init.jl:102-106) */
   PPS_SAMPLER_UNIFORM = 1,   /* x = U (ub - lb) + lb           (src/utils.jl:57-84) */
-  PPS_SAMPLER_UNBOUNDED = 2  /* x = u0 + U |u0| or U if u0 = 0 (src/utils.jl:23-55) */
+  PPS_SAMPLER_UNBOUNDED = 2, /* x = u0 + U |u0| or U if u0 = 0 (src/utils.jl:23-55) */
+  /* Latin hypercube (init(...; sampler = LatinHypercubeSample()), src/init.jl:15-34): in each dim
+   * the n strata are dealt to the particles by a random permutation (a keyed Feistel bijection of
+   * [0, n)), x = ((stratum + U) / n) (ub - lb) + lb; needs finite bounds */
+  PPS_SAMPLER_LHS = 3
 };
 
 /* swarm flags */

@@ -470,6 +470,48 @@ static inline void split_range(int64_t n, int tid, int nth, int64_t* b, int64_t*
 }
 
 /* ------------------------------------------------------------------------ */
+/* Latin hypercube strata: McKay, Beckman & Conover (1979) with the          */
+/* permutation of each dim as a Feistel bijection cycle-walked into [0, n)   */
+/* (Black & Rogaway, CT-RSA 2002); round keys = one Philox draw of (d, seed) */
+/* ------------------------------------------------------------------------ */
+#define ORC_TAG_LHS 0x4C485331u /* "LHS1" */
+
+static uint32_t lhs_round(uint32_t r, uint32_t key) {
+  uint32_t x = r ^ key;
+  x *= 0xD2511F53u;
+  x ^= x >> 15;
+  x *= 0xCD9E8D57u;
+  x ^= x >> 13;
+  return x;
+}
+
+static uint32_t lhs_feistel(uint32_t v, int h, const uint32_t key[4]) {
+  const uint32_t mask = (1u << h) - 1u;
+  uint32_t L = v >> h, R = v & mask;
+  for (int r = 0; r < 4; ++r) {
+    const uint32_t nl = R;
+    R = L ^ (lhs_round(R, key[r]) & mask);
+    L = nl;
+  }
+  return (L << h) | R;
+}
+
+uint32_t orc_lhs_stratum(uint32_t i, uint32_t n, uint32_t d, uint64_t seed) {
+  int bits = 0;
+  while (bits < 32 && (1ull << bits) < (uint64_t)n) ++bits;
+  const int h = bits < 2 ? 1 : (bits + 1) / 2;
+  uint32_t key[4];
+  philox_step(seed, d, 0u, 0u, ORC_TAG_LHS, key);
+  const uint64_t domain = 1ull << (2 * h);
+  uint32_t v = i;
+  for (uint64_t it = 0; it < domain; ++it) {
+    v = lhs_feistel(v, h, key);
+    if (v < n) return v;
+  }
+  return i;
+}
+
+/* ------------------------------------------------------------------------ */
 /* init (src/utils.jl:23-84, src/init.jl:38-54)                             */
 /* ------------------------------------------------------------------------ */
 void orc_init(const orc_problem* prob, orc_swarm* s, uint64_t seed, int32_t sampler) {
@@ -488,6 +530,10 @@ void orc_init(const orc_problem* prob, orc_swarm* s, uint64_t seed, int32_t samp
           float u0 = prob->u0[d];
           float a = fabsf(u0);
           xv = (a > 0.0f) ? (u0 + (u * a)) : u;
+        } else if (sampler == ORC_SAMPLER_LHS) {
+          /* x = ((stratum + U) / n) (ub - lb) + lb */
+          const float t = ((float)orc_lhs_stratum((uint32_t)i, (uint32_t)n, (uint32_t)d, seed) + u) / (float)n;
+          xv = (t * (prob->ub[d] - prob->lb[d])) + prob->lb[d];
         } else {
           /* uniform_itr: rand(T) * (ub[i] - lb[i]) + lb[i] */
           xv = (u * (prob->ub[d] - prob->lb[d])) + prob->lb[d];

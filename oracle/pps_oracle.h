@@ -135,7 +135,15 @@ float orc_penalty(const orc_problem* prob, const float* x, int64_t stride, float
 float orc_objective_grad(const orc_problem* prob, const float* x, float* grad);
 
 /* ---- swarm ---- */
-enum { ORC_SAMPLER_UNIFORM = 0, ORC_SAMPLER_UNBOUNDED = 1 };
+/* samplers: uniform_itr (src/utils.jl:1-5,57-84), the unbounded sampler
+ * (src/utils.jl:23-55), Latin hypercube (init(...; sampler =
+ * LatinHypercubeSample()), src/init.jl:15-34; QuasiMonteCarlo is not
+ * vendored, so this restates the published method: per dim a random
+ * permutation of the n strata, a uniform draw inside each stratum) */
+enum { ORC_SAMPLER_UNIFORM = 0, ORC_SAMPLER_UNBOUNDED = 1, ORC_SAMPLER_LHS = 2 };
+/* the Latin-hypercube stratum of particle i (< n) in dim d: a keyed bijection
+ * of [0, n) (4-round Feistel network on 2h bits, cycle-walked into [0, n)) */
+uint32_t orc_lhs_stratum(uint32_t i, uint32_t n, uint32_t d, uint64_t seed);
 enum { ORC_GBEST_FROM_PBEST = 0, ORC_GBEST_FROM_POSITION = 1 };
 
 void orc_init(const orc_problem* prob, orc_swarm* s, uint64_t seed, int32_t sampler);

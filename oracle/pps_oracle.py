@@ -19,7 +19,7 @@ LIB_PATH = HERE / "_build" / "libpps_oracle.so"
 
 TAG_INIT = 0x494E4954
 TAG_STEP = 0x50534F31
-SAMPLER_UNIFORM, SAMPLER_UNBOUNDED = 0, 1
+SAMPLER_UNIFORM, SAMPLER_UNBOUNDED, SAMPLER_LHS = 0, 1, 2
 GBEST_FROM_PBEST, GBEST_FROM_POSITION = 0, 1
 ODE_LV, ODE_FHN = 0, 1
 
@@ -94,6 +94,8 @@ def load() -> ctypes.CDLL:
         L.orc_async_lanes.argtypes = [ctypes.c_int32, ctypes.POINTER(ctypes.c_int32)]
         L.orc_argmin_key.restype = ctypes.c_uint64
         L.orc_argmin_key.argtypes = [ctypes.c_float, ctypes.c_uint32]
+        L.orc_lhs_stratum.restype = ctypes.c_uint32
+        L.orc_lhs_stratum.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint64]
         for name in ("orc_lbfgs", "orc_broyden"):
             getattr(L, name).argtypes = [ctypes.POINTER(Problem), ctypes.c_int64, _fp, ctypes.POINTER(LbfgsOpts),
                                          _fp, _fp, ctypes.POINTER(ctypes.c_int32), ctypes.c_int32]
@@ -107,6 +109,11 @@ def load() -> ctypes.CDLL:
         L.orc_bf16_round.argtypes = [ctypes.c_float]
         _lib = L
     return _lib
+
+
+def lhs_stratum(i: int, n: int, d: int, seed: int) -> int:
+    """The Latin-hypercube stratum of particle i (< n) in dim d."""
+    return int(load().orc_lhs_stratum(i, n, d, seed))
 
 
 def fp(a: np.ndarray):

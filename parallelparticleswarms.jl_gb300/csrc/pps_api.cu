@@ -358,12 +358,13 @@ int pps_swarm_init(pps_swarm* s, int32_t sampler) {
       if (!(std::isinf(s->host_lb[d]) && std::isinf(s->host_ub[d]))) all_inf = false;
     sampler = all_inf ? PPS_SAMPLER_UNBOUNDED : PPS_SAMPLER_UNIFORM;
   }
-  if (sampler != PPS_SAMPLER_UNIFORM && sampler != PPS_SAMPLER_UNBOUNDED)
+  if (sampler != PPS_SAMPLER_UNIFORM && sampler != PPS_SAMPLER_UNBOUNDED && sampler != PPS_SAMPLER_LHS)
     return set_error(PPS_EINVAL, "unknown sampler %d", sampler);
-  if (sampler == PPS_SAMPLER_UNIFORM) {
+  if (sampler == PPS_SAMPLER_UNIFORM || sampler == PPS_SAMPLER_LHS) {
     for (int d = 0; d < D; ++d)
       if (!std::isfinite(s->host_lb[d]) || !std::isfinite(s->host_ub[d]))
-        return set_error(PPS_EINVAL, "uniform sampler needs finite bounds (dim %d)", d);
+        return set_error(PPS_EINVAL, "%s sampler needs finite bounds (dim %d)",
+                         sampler == PPS_SAMPLER_LHS ? "Latin hypercube" : "uniform", d);
   }
   if ((rc = launch_set_iter(s, 0u, 0.7298f, 1.0f))) return rc;
   if ((rc = is_ode(s->objective) ? launch_init_ode(s, sampler, s->u0_dev) : launch_init(s, sampler, s->u0_dev)))

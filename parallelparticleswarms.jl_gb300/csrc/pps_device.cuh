@@ -33,6 +33,12 @@ namespace pps {
 
 constexpr uint32_t kTagInit = 0x494E4954u;  // "INIT"
 constexpr uint32_t kTagStep = 0x50534F31u;  // "PSO1"
+constexpr uint32_t kTagLhs = 0x4C485331u;   // "LHS1"
+
+// samplers (the values of include/pps.h's PPS_SAMPLER_*)
+constexpr int kSamplerUniform = 1;
+constexpr int kSamplerUnbounded = 2;
+constexpr int kSamplerLhs = 3;
 
 enum Objective : int {
   kSphere = 0,
@@ -114,6 +120,59 @@ __device__ __forceinline__ Rand4 philox4x32_10(uint32_t c0, uint32_t c1, uint32_
 
 __device__ __forceinline__ float u01(uint32_t bits) {
   return __fmul_rn(__uint2float_rn(bits >> 8), 0x1p-24f);
+}
+
+// ---------------------------------------------------------------- Latin hypercube
+// Latin hypercube sampling (McKay, Beckman & Conover, Technometrics 1979),
+// the reference's init(...; sampler = LatinHypercubeSample()) (QMC samples
+// read by the init kernel, src/init.jl:15-34, src/utils.jl:86-112): in each
+// dim the n strata [k/n, (k+1)/n) are dealt to the particles by a random
+// permutation and each particle draws uniformly inside its stratum.  The
+// permutation of dim d is computed per particle, with no sort: a 4-round
+// balanced Feistel network on 2h-bit values (2^(2h) >= n) whose round keys
+// are one Philox draw of (d, seed), restricted to [0, n) by cycle-walking
+// (Black & Rogaway, "Ciphers with arbitrary finite domains", CT-RSA 2002).
+// The walk from i < n returns below n within the cycle through i, so it ends
+// after at most 2^(2h) - n + 1 rounds (fewer than 4 expected).
+__device__ __forceinline__ uint32_t lhs_round(uint32_t r, uint32_t key) {
+  uint32_t x = r ^ key;
+  x *= 0xD2511F53u;
+  x ^= x >> 15;
+  x *= 0xCD9E8D57u;
+  x ^= x >> 13;
+  return x;
+}
+__device__ __forceinline__ uint32_t lhs_feistel(uint32_t v, int h, const Rand4& key) {
+  const uint32_t mask = (1u << h) - 1u;
+  uint32_t L = v >> h, R = v & mask;
+  const uint32_t k[4] = {key.a, key.b, key.c, key.d};
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const uint32_t nl = R;
+    R = L ^ (lhs_round(R, k[r]) & mask);
+    L = nl;
+  }
+  return (L << h) | R;
+}
+// the stratum of particle i (< n) in dim d
+__device__ __forceinline__ uint32_t lhs_stratum(uint32_t i, uint32_t n, uint32_t d, uint32_t k0, uint32_t k1) {
+  int bits = 0;
+  while (bits < 32 && (1ull << bits) < (unsigned long long)n) ++bits;
+  const int h = bits < 2 ? 1 : (bits + 1) / 2;
+  const Rand4 key = philox4x32_10(d, 0u, 0u, kTagLhs, k0, k1);
+  const unsigned long long domain = 1ull << (2 * h);
+  uint32_t v = i;
+  for (unsigned long long it = 0; it < domain; ++it) {
+    v = lhs_feistel(v, h, key);
+    if (v < n) return v;
+  }
+  return i;  // not reached (see above)
+}
+// x = ((stratum + u) / n) (ub - lb) + lb
+__device__ __forceinline__ float lhs_position(uint32_t i, uint32_t n, uint32_t d, float u, float lo, float hi,
+                                              uint32_t k0, uint32_t k1) {
+  const float t = __fdiv_rn(__fadd_rn(__uint2float_rn(lhs_stratum(i, n, d, k0, k1)), u), __uint2float_rn(n));
+  return __fadd_rn(__fmul_rn(t, __fsub_rn(hi, lo)), lo);
 }
 
 // ---------------------------------------------------------------- math

@@ -14,6 +14,10 @@
 
 namespace pps {
 
+static_assert(kSamplerUniform == PPS_SAMPLER_UNIFORM && kSamplerUnbounded == PPS_SAMPLER_UNBOUNDED &&
+                  kSamplerLhs == PPS_SAMPLER_LHS,
+              "device sampler ids follow include/pps.h");
+
 struct ObjData {
   const float* data;  // device copy of the objective's data (ODE obs, MLP set)
   int64_t ndata;

@@ -51,6 +51,8 @@ __global__ void __launch_bounds__(kOdeThreads) k_init_ode(SwarmDev s, ObjParams 
           const float z = u0 ? u0[d] : 0.0f;
           const float a = fabsf(z);
           xv = (a > 0.0f) ? __fadd_rn(z, __fmul_rn(u, a)) : u;
+        } else if (sampler == PPS_SAMPLER_LHS) {
+          xv = valid ? lhs_position((uint32_t)i, (uint32_t)s.n, (uint32_t)d, u, s.lb[d], s.ub[d], k0, k1) : 0.0f;
         } else {
           xv = __fadd_rn(__fmul_rn(u, __fsub_rn(s.ub[d], s.lb[d])), s.lb[d]);
         }

@@ -56,6 +56,8 @@ __global__ void __launch_bounds__(kSyncThreads) k_init(SwarmDev s, ObjParams op,
           const float z = u0 ? u0[d] : 0.0f;
           const float a = fabsf(z);
           x = (a > 0.0f) ? __fadd_rn(z, __fmul_rn(u, a)) : u;
+        } else if (sampler == PPS_SAMPLER_LHS) {
+          x = valid ? lhs_position((uint32_t)i, (uint32_t)s.n, (uint32_t)d, u, s.lb[d], s.ub[d], k0, k1) : 0.0f;
         } else {
           const float lo = s.lb[d], hi = s.ub[d];
           x = __fadd_rn(__fmul_rn(u, __fsub_rn(hi, lo)), lo);  // rand(T) * (ub - lb) + lb

@@ -33,7 +33,6 @@
 namespace pps {
 
 constexpr int kUserThreads = 256;
-constexpr int kUserSamplerUnbounded = 2;  // PPS_SAMPLER_UNBOUNDED
 
 __device__ __forceinline__ void user_params(float* sp, const ObjParams& op) {
   if (threadIdx.x < 8) sp[threadIdx.x] = (int)threadIdx.x < op.np ? op.p[threadIdx.x] : 0.0f;
@@ -65,10 +64,12 @@ extern "C" __global__ void __launch_bounds__(pps::kUserThreads, PPS_USER_MB4)
         if (d >= D) break;
         const float u = u01(rr[h]);
         float x;
-        if (sampler == kUserSamplerUnbounded) {
+        if (sampler == kSamplerUnbounded) {
           const float z = u0 ? u0[d] : 0.0f;
           const float a = fabsf(z);
           x = (a > 0.0f) ? __fadd_rn(z, __fmul_rn(u, a)) : u;
+        } else if (sampler == kSamplerLhs) {
+          x = valid ? lhs_position((uint32_t)i, (uint32_t)s.n, (uint32_t)d, u, s.lb[d], s.ub[d], k0, k1) : 0.0f;
         } else {
           const float lo = s.lb[d], hi = s.ub[d];
           x = __fadd_rn(__fmul_rn(u, __fsub_rn(hi, lo)), lo);  // rand(T) * (ub - lb) + lb

@@ -4,8 +4,8 @@ API over libpps_cuda.so (hand-written sm_103a kernels, C ABI in include/pps.h).
 Exports mirror src/ParallelParticleSwarms.jl:102-104.
 """
 from ._lib import ArgumentError, PPSError
-from .algorithms import (BFGS, CUDA, GPUUniformSampler, GPUUnboundedSampler, HybridPSO, ParallelPSOKernel,
-                         ParallelSyncPSOKernel, PSOAlgorithm, SimpleLBFGS)
+from .algorithms import (BFGS, CUDA, GPUUniformSampler, GPUUnboundedSampler, HybridPSO, LatinHypercubeSample,
+                         ParallelPSOKernel, ParallelSyncPSOKernel, PSOAlgorithm, SimpleLBFGS)
 from .problem import (REGISTRY, Objective, OptimizationProblem, ackley, beale, booth, boundary_quadratic,
                       cuda_objective, evaluate, fitzhugh_nagumo_fit, himmelblau, lotka_volterra_fit,
                       mlp_regression, quadratic, quadratic_constraint, rastrigin, rosenbrock, shifted_sphere, sphere)
@@ -19,6 +19,7 @@ from . import mlp, ode
 __all__ = [
     "ParallelPSOKernel", "ParallelSyncPSOKernel", "PSOAlgorithm", "HybridPSO", "SimpleLBFGS", "BFGS",
     "OptimizationProblem", "solve", "solve_", "init", "reinit_", "GPUUniformSampler", "GPUUnboundedSampler",
+    "LatinHypercubeSample",
     "PSOCache", "HybridPSOCache", "OptimizationSolution", "OptimizationStats", "Swarm", "PPSError",
     "ArgumentError", "evaluate", "Objective", "REGISTRY", "sphere", "rosenbrock", "rastrigin", "ackley",
     "lotka_volterra_fit", "fitzhugh_nagumo_fit", "mlp_regression", "beale", "booth", "himmelblau",

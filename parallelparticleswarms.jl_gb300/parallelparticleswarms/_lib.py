@@ -19,7 +19,7 @@ STATUS_NAMES = {0: "PPS_OK", 1: "PPS_EINVAL", 2: "PPS_ENOMEM", 3: "PPS_ECUDA", 4
                 5: "PPS_EBUSY", 6: "PPS_ENOTSUP", 7: "PPS_ENODEV"}
 
 # samplers, flags, fields
-SAMPLER_AUTO, SAMPLER_UNIFORM, SAMPLER_UNBOUNDED = 0, 1, 2
+SAMPLER_AUTO, SAMPLER_UNIFORM, SAMPLER_UNBOUNDED, SAMPLER_LHS = 0, 1, 2, 3
 FLAG_GBEST_FROM_POSITION = 1
 FIELD_POSITION, FIELD_VELOCITY, FIELD_PBEST, FIELD_PCOST, FIELD_COST = range(5)
 FIELD_LOCAL_X, FIELD_LOCAL_F, FIELD_LOCAL_ITERS = 5, 6, 7

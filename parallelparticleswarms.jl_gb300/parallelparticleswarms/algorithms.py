@@ -34,6 +34,14 @@ class GPUUnboundedSampler:
 
 
 @dataclass
+class LatinHypercubeSample:
+    """Latin hypercube init (``init(prob, alg; sampler = LatinHypercubeSample())``,
+    src/init.jl:15-34): in each dim the n strata of [lb, ub] are dealt to the
+    particles by a random permutation, each particle drawing uniformly inside
+    its stratum.  Computed on the device (no host sample matrix)."""
+
+
+@dataclass
 class ParallelSyncPSOKernel(PSOAlgorithm):
     """Synchronous PSO: global best recomputed after every iteration
     (src/algorithms.jl:115-121,199-204)."""

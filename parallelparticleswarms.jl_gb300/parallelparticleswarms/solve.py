@@ -10,7 +10,8 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from . import _lib
-from .algorithms import (BFGS, GPUUniformSampler, GPUUnboundedSampler, HybridPSO, ParallelPSOKernel,
+from .algorithms import (BFGS, GPUUniformSampler, GPUUnboundedSampler, HybridPSO, LatinHypercubeSample,
+                         ParallelPSOKernel,
                          ParallelSyncPSOKernel, SimpleLBFGS)
 from .problem import OptimizationProblem, evaluate
 from .swarm import C1_DEFAULT, C2_DEFAULT, W_DEFAULT, WDAMP_DEFAULT, Swarm
@@ -76,6 +77,8 @@ def _sampler_code(sampler) -> int:
         return _lib.SAMPLER_UNIFORM
     if isinstance(sampler, GPUUnboundedSampler):
         return _lib.SAMPLER_UNBOUNDED
+    if isinstance(sampler, LatinHypercubeSample):
+        return _lib.SAMPLER_LHS
     raise _lib.PPSError(_lib.ENOTSUP, f"sampler {type(sampler).__name__} is not supported on the device")
 
 
