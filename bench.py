@@ -363,6 +363,28 @@ def run_configs(pps) -> dict:
     steps = 1000 * 16384 * 100  # RK4 steps
     out["ode_lv_16384x100_alone"] = {"device_ms": ms, "particle_iters_per_s": 16384 * 100 / (ms / 1e3),
                                      "rk4_steps_per_s": steps / (ms / 1e3)}
+    # the reference's own ode_pso benchmarks: Tsit5 at dt = 0.1, saves every
+    # 0.01 on [0, 3] from its continuous extension, 10,000 particles, 100 iterations
+    for model in ("lv", "fhn"):
+        prob, truth = pps.ode.reference_benchmark_fit(model)
+        with pps.Swarm(prob, 10_000, seed=0) as sw:
+            sw.init()
+            sw.sync_run(5)  # warm
+            sw.init()
+            ms = sw.sync_run(100)
+            u, cost, _ = sw.gbest()
+        entry = {"device_ms": ms, "particle_iters_per_s": 10_000 * 100 / (ms / 1e3), "gbest_cost": cost,
+                 "max_rel_err_vs_truth": float(np.max(np.abs(u - truth) / truth))}
+        try:
+            ref = orc.OracleSwarm(orc.ode_fit_problem(prob), 2000, 0).init()
+            t0 = time.perf_counter()
+            ref.sync_run(10)
+            sec = time.perf_counter() - t0
+            entry["cpu_oracle"] = {"particle_iters_per_s": 2000 * 10 / sec, "cores": os.cpu_count(),
+                                   "sample": "2000 particles x 10 iterations"}
+        except Exception as e:  # the oracle is optional on a machine without its build
+            entry["cpu_oracle"] = {"unavailable": str(e)}
+        out[f"ode_{model}_tsit5_reference_benchmark"] = entry
     # many small separable swarms in one batched launch against the same
     # swarms solved one at a time
     rng = np.random.default_rng(5)

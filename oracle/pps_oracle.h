@@ -190,8 +190,11 @@ typedef struct orc_ode_fit {
   int32_t nsaves;
   const float* data;   /* nsaves x 2, row major */
   float fixed[4];      /* fixed model constants (FHN: l) */
+  int32_t method;      /* ORC_ODE_RK4 (saves every save_every steps) or ORC_ODE_TSIT5 */
+  float save_dt;       /* Tsit5: saves at m * save_dt from the continuous extension */
 } orc_ode_fit;
-/* RK4 integration + SSE against data (src/ode_pso.jl:47-52) */
+enum { ORC_ODE_RK4 = 0, ORC_ODE_TSIT5 = 1 };
+/* RK4 or Tsit5 integration + SSE against data (src/ode_pso.jl:47-52) */
 float orc_ode_loss(const orc_ode_fit* fit, const float* p);
 /* trajectory at the save points: out[nsaves*2] */
 void orc_ode_solve(const orc_ode_fit* fit, const float* p, float* out);

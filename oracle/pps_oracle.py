@@ -29,7 +29,8 @@ _fp = ctypes.POINTER(ctypes.c_float)
 class OdeFit(ctypes.Structure):
     _fields_ = [("model", ctypes.c_int32), ("nparams", ctypes.c_int32), ("u0", ctypes.c_float * 2),
                 ("dt", ctypes.c_float), ("nsteps", ctypes.c_int32), ("save_every", ctypes.c_int32),
-                ("nsaves", ctypes.c_int32), ("data", _fp), ("fixed", ctypes.c_float * 4)]
+                ("nsaves", ctypes.c_int32), ("data", _fp), ("fixed", ctypes.c_float * 4),
+                ("method", ctypes.c_int32), ("save_dt", ctypes.c_float)]
 
 
 USER_FN = ctypes.CFUNCTYPE(ctypes.c_float, _fp, ctypes.c_int, _fp, _fp, ctypes.c_longlong)
@@ -199,7 +200,7 @@ class OracleProblem:
 
 class OracleOdeFit:
     def __init__(self, model: int, nparams: int, u0, dt: float, nsteps: int, save_every: int, data,
-                 fixed=(0.0, 0.0, 0.0, 0.0)):
+                 fixed=(0.0, 0.0, 0.0, 0.0), method: int = 0, save_dt: float = 0.0):
         self.data = np.ascontiguousarray(np.asarray(data, np.float32).reshape(-1, 2))
         self.c = OdeFit()
         self.c.model, self.c.nparams = int(model), int(nparams)
@@ -209,6 +210,7 @@ class OracleOdeFit:
         self.c.data = fp(self.data)
         for k, v in enumerate(fixed):
             self.c.fixed[k] = float(v)
+        self.c.method, self.c.save_dt = int(method), float(save_dt)
 
     def loss(self, p) -> float:
         p = np.ascontiguousarray(np.asarray(p, np.float32))
@@ -353,3 +355,15 @@ class UserObjective:
         d = None if data is None else np.ascontiguousarray(np.asarray(data, np.float32).reshape(-1))
         return float(self.fn(fp(x), x.size, fp(p), fp(d) if d is not None else ctypes.cast(None, _fp),
                              0 if d is None else d.size))
+
+
+def ode_fit_problem(prob) -> OracleProblem:
+    """OracleProblem for an ODE-fit problem of the package (duck-typed: f.name,
+    dim, p = [u0_1, u0_2, dt, nsteps, save_every, l(, method, save_dt)], data,
+    lb, ub)."""
+    p = np.asarray(prob.p, np.float32)
+    model = ODE_LV if prob.f.name == "lotka_volterra_fit" else ODE_FHN
+    method, save_dt = (int(p[6]), float(p[7])) if p.size > 7 else (0, 0.0)
+    fit = OracleOdeFit(model, prob.dim, (p[0], p[1]), p[2], int(p[3]), int(p[4]), prob.data,
+                       fixed=(p[5], 0.0, 0.0, 0.0), method=method, save_dt=save_dt)
+    return OracleProblem(4 if model == ODE_LV else 5, prob.dim, prob.lb, prob.ub, ode=fit)

@@ -13,7 +13,8 @@
  *   Lotka-Volterra  benchmarks/Lotka_Volterra/lotka_volterra.jl:9-13
  *     du1 = p1*u1 - p2*u1*u2,  du2 = -p3*u2 + p4*u1*u2
  *   FitzHugh-Nagumo benchmarks/Fitzhugh_Nagumo/ode_estimation.jl:6-12
- *     dv = v - v^3/3 - w + l,  dw = tinv*(v + a - b*w)   (l held fixed)
+ *     dv = v - v^3/3 - w + l,  dw = tinv*(v + a - b*w)   (l held fixed, or
+ *     fitted as the 4th parameter as the reference's benchmark does)
  * evaluated in factored form, two roundings per term where the literal
  * form takes four (the RK4 arithmetic is this build's own: the reference
  * integrates with GPUTsit5):
@@ -32,7 +33,7 @@ static inline void rhs(const orc_ode_fit* f, const float* p, float u0, float u1,
     *d1 = u1 * fmaf(p[3], u0, -p[2]);
   } else {
     float v3 = (u0 * u0) * u0;
-    *d0 = (fmaf(v3, -0x1.555556p-2f, u0) - u1) + f->fixed[0];
+    *d0 = (fmaf(v3, -0x1.555556p-2f, u0) - u1) + (f->nparams > 3 ? p[3] : f->fixed[0]);
     *d1 = p[2] * fmaf(-p[1], u1, u0 + p[0]);
   }
 }
@@ -56,7 +57,115 @@ static inline void rk4_step(const orc_ode_fit* f, const float* p, float* u0, flo
   *u1 = fmaf(h6, sb, *u1);
 }
 
+/* ---- Tsit5: Tsitouras, Comput. Math. Appl. 62 (2011) 770-775 ----
+ * The 7-stage first-same-as-last 5(4) pair of the reference's GPUTsit5
+ * (src/ode_pso.jl:58, DiffEqGPU, not vendored), fixed step (adaptive = false,
+ * benchmarks/Lotka_Volterra/lotka_volterra.jl:122-127), saves from its
+ * 4th-order continuous extension b_i(theta) = delta_i1 theta + r_i2 theta^2 +
+ * r_i3 theta^3 + r_i4 theta^4.  tsit5_coefficients.py checks the tableau
+ * against the order-5 conditions and derives the extension from its own
+ * conditions.  Stage sums left to right with fmaf, as the CUDA kernel. */
+static const float A21 = 0.161f;
+static const float A31 = -0.008480655492356989f, A32 = 0.335480655492357f;
+static const float A41 = 2.897153057105493f, A42 = -6.359448489975075f, A43 = 4.3622954328695815f;
+static const float A51 = 5.325864828439257f, A52 = -11.748883564062828f, A53 = 7.4955393428898365f,
+                   A54 = -0.09249506636175525f;
+static const float A61 = 5.86145544294642f, A62 = -12.92096931784711f, A63 = 8.159367898576159f,
+                   A64 = -0.071584973281401f, A65 = -0.028269050394068383f;
+static const float B1 = 0.09646076681806523f, B2 = 0.01f, B3 = 0.4798896504144996f, B4 = 1.379008574103742f,
+                   B5 = -3.290069515436081f, B6 = 2.324710524099774f;
+static const float R[7][3] = {{-2.763706197274826f, 2.9132554618219126f, -1.0530884977290216f},
+                              {0.1317f, -0.2234f, 0.1017f},
+                              {3.9302962368947516f, -5.941033872131505f, 2.490627285651253f},
+                              {-12.411077166933676f, 30.33818863028232f, -16.548102889244902f},
+                              {37.50931341651104f, -88.1789048947664f, 47.37952196281928f},
+                              {-27.896526289197286f, 65.09189467479366f, -34.87065786149661f},
+                              {1.5f, -4.0f, 2.5f}};
+
+/* k[0] = f(u) on entry; k[0..6] the stages and (n0, n1) the new state on exit */
+static void tsit5_step(const orc_ode_fit* f, const float* p, float u0, float u1, float ka[7], float kb[7],
+                       float* n0, float* n1) {
+  const float dt = f->dt;
+  float sa, sb;
+  sa = A21 * ka[0];
+  sb = A21 * kb[0];
+  rhs(f, p, fmaf(dt, sa, u0), fmaf(dt, sb, u1), &ka[1], &kb[1]);
+  sa = fmaf(A32, ka[1], A31 * ka[0]);
+  sb = fmaf(A32, kb[1], A31 * kb[0]);
+  rhs(f, p, fmaf(dt, sa, u0), fmaf(dt, sb, u1), &ka[2], &kb[2]);
+  sa = fmaf(A43, ka[2], fmaf(A42, ka[1], A41 * ka[0]));
+  sb = fmaf(A43, kb[2], fmaf(A42, kb[1], A41 * kb[0]));
+  rhs(f, p, fmaf(dt, sa, u0), fmaf(dt, sb, u1), &ka[3], &kb[3]);
+  sa = fmaf(A54, ka[3], fmaf(A53, ka[2], fmaf(A52, ka[1], A51 * ka[0])));
+  sb = fmaf(A54, kb[3], fmaf(A53, kb[2], fmaf(A52, kb[1], A51 * kb[0])));
+  rhs(f, p, fmaf(dt, sa, u0), fmaf(dt, sb, u1), &ka[4], &kb[4]);
+  sa = fmaf(A65, ka[4], fmaf(A64, ka[3], fmaf(A63, ka[2], fmaf(A62, ka[1], A61 * ka[0]))));
+  sb = fmaf(A65, kb[4], fmaf(A64, kb[3], fmaf(A63, kb[2], fmaf(A62, kb[1], A61 * kb[0]))));
+  rhs(f, p, fmaf(dt, sa, u0), fmaf(dt, sb, u1), &ka[5], &kb[5]);
+  sa = fmaf(B6, ka[5], fmaf(B5, ka[4], fmaf(B4, ka[3], fmaf(B3, ka[2], fmaf(B2, ka[1], B1 * ka[0])))));
+  sb = fmaf(B6, kb[5], fmaf(B5, kb[4], fmaf(B4, kb[3], fmaf(B3, kb[2], fmaf(B2, kb[1], B1 * kb[0])))));
+  *n0 = fmaf(dt, sa, u0);
+  *n1 = fmaf(dt, sb, u1);
+  rhs(f, p, *n0, *n1, &ka[6], &kb[6]);
+}
+
+/* u + dt sum_i b_i(theta) k_i */
+static float tsit5_dense(float u, float dt, float th, const float k[7]) {
+  const float th2 = th * th;
+  const float w1 = th * fmaf(th, fmaf(th, fmaf(th, R[0][2], R[0][1]), R[0][0]), 1.0f);
+  float s = w1 * k[0];
+  for (int i = 1; i < 7; ++i) s = fmaf(th2 * fmaf(th, fmaf(th, R[i][2], R[i][1]), R[i][0]), k[i], s);
+  return fmaf(dt, s, u);
+}
+
+/* the Tsit5 solution at t_m = m save_dt, m < nsaves (out[0..1] = u0);
+ * with data: returns the SSE against it */
+static float tsit5_run(const orc_ode_fit* f, const float* p, float* out) {
+  const float dt = f->dt;
+  float u0 = f->u0[0], u1 = f->u0[1];
+  float acc = 0.0f;
+  if (out) {
+    out[0] = u0;
+    out[1] = u1;
+  } else {
+    const float e0 = f->data[0] - u0, e1 = f->data[1] - u1;
+    acc = (e0 * e0) + (e1 * e1);
+  }
+  float ka[7], kb[7];
+  rhs(f, p, u0, u1, &ka[0], &kb[0]);
+  int m = 1;
+  float tm = f->save_dt;
+  for (int n = 0; n < f->nsteps && m < f->nsaves; ++n) {
+    const float tn = (float)n * dt;
+    const float tn1 = (float)(n + 1) * dt;
+    float n0, n1;
+    tsit5_step(f, p, u0, u1, ka, kb, &n0, &n1);
+    while (m < f->nsaves && tm <= tn1) {
+      const float th = (tm - tn) / dt;
+      const float y0 = tsit5_dense(u0, dt, th, ka), y1 = tsit5_dense(u1, dt, th, kb);
+      if (out) {
+        out[2 * m] = y0;
+        out[2 * m + 1] = y1;
+      } else {
+        const float e0 = f->data[2 * m] - y0, e1 = f->data[2 * m + 1] - y1;
+        acc = acc + ((e0 * e0) + (e1 * e1));
+      }
+      ++m;
+      tm = (float)m * f->save_dt;
+    }
+    u0 = n0;
+    u1 = n1;
+    ka[0] = ka[6];
+    kb[0] = kb[6];
+  }
+  return acc;
+}
+
 void orc_ode_solve(const orc_ode_fit* f, const float* p, float* out) {
+  if (f->method == ORC_ODE_TSIT5) {
+    tsit5_run(f, p, out);
+    return;
+  }
   float u0 = f->u0[0], u1 = f->u0[1];
   out[0] = u0;
   out[1] = u1;
@@ -72,6 +181,7 @@ void orc_ode_solve(const orc_ode_fit* f, const float* p, float* out) {
 }
 
 float orc_ode_loss(const orc_ode_fit* f, const float* p) {
+  if (f->method == ORC_ODE_TSIT5) return tsit5_run(f, p, NULL);
   float u0 = f->u0[0], u1 = f->u0[1];
   float d0 = f->data[0] - u0, d1 = f->data[1] - u1;
   float acc = (d0 * d0) + (d1 * d1);

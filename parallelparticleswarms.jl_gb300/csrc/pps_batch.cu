@@ -554,6 +554,8 @@ int batch_describe(const pps_problem* prob, int64_t n, uint64_t seed, int32_t ma
   if (is_ode(obj)) {
     const int rc = ode_check(prob);
     if (rc) return rc;
+    if (prob->nparams > 6 && prob->params[6] != 0.0f)
+      return set_error(PPS_ENOTSUP, "batched ODE fits integrate with RK4; a Tsit5 fit runs as a swarm of its own");
   }
   const int D = prob->dim;
   bool all_inf = true;

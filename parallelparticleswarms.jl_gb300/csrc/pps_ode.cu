@@ -12,6 +12,8 @@
 // The reference clamps with max(position, lb) on whole SVectors
 // (src/ode_pso.jl:18-19), which compares lexicographically; this build
 // clamps each parameter (max.(x, lb), min.(x, ub)) as the other kernels do.
+#include <cmath>
+
 #include "pps_internal.h"
 #include "pps_ode.cuh"
 #include "pps_publish.cuh"
@@ -21,12 +23,13 @@ namespace pps {
 constexpr int kOdeThreads = 128;
 constexpr int kOdeMaxDim = 4;
 
-template <int MODEL>
+template <int MODEL, int METHOD>
 __device__ __forceinline__ float ode_eval(const float (&x)[kOdeMaxDim], const OdeCfg& c, const float* data) {
-  return ode_loss<MODEL>(x, c, data);
+  if constexpr (METHOD == kOdeTsit5) return tsit5_loss<MODEL>(x, c, data);
+  else return ode_loss<MODEL>(x, c, data);
 }
 
-template <int MODEL>
+template <int MODEL, int METHOD>
 __global__ void __launch_bounds__(kOdeThreads) k_init_ode(SwarmDev s, ObjParams op, OdeCfg cfg,
                                                           const float* __restrict__ data_g, uint64_t seed,
                                                           int sampler, const float* __restrict__ u0) {
@@ -63,7 +66,7 @@ __global__ void __launch_bounds__(kOdeThreads) k_init_ode(SwarmDev s, ObjParams 
         s.P[o] = x[d];
       }
     }
-    const float c = valid ? ode_eval<MODEL>(x, cfg, data) : __int_as_float(0x7f800000);
+    const float c = valid ? ode_eval<MODEL, METHOD>(x, cfg, data) : __int_as_float(0x7f800000);
     s.cost[i] = c;
     s.pcost[i] = c;
     s.flag[i] = 0;
@@ -72,7 +75,7 @@ __global__ void __launch_bounds__(kOdeThreads) k_init_ode(SwarmDev s, ObjParams 
   if (publish_block_min(key, s.st)) finish_iteration(s, false, 0u, s.st->w);
 }
 
-template <int MODEL>
+template <int MODEL, int METHOD>
 __global__ void __launch_bounds__(kOdeThreads) k_sync_step_ode(SwarmDev s, ObjParams op, OdeCfg cfg,
                                                                const float* __restrict__ data_g, uint64_t seed,
                                                                float c1, float c2, int from_position) {
@@ -118,7 +121,7 @@ __global__ void __launch_bounds__(kOdeThreads) k_sync_step_ode(SwarmDev s, ObjPa
         x[d] = xd;
       }
     }
-    const float c = ode_eval<MODEL>(x, cfg, data);
+    const float c = ode_eval<MODEL, METHOD>(x, cfg, data);
     float pc = s.pcost[i];
     const bool improved = valid && c < pc;
     pc = improved ? c : pc;
@@ -130,23 +133,45 @@ __global__ void __launch_bounds__(kOdeThreads) k_sync_step_ode(SwarmDev s, ObjPa
   if (publish_block_min(key, st)) finish_iteration(s, from_position != 0, t + 1u, __fmul_rn(w, st->wdamp));
 }
 
+// model x integrator
+#define PPS_DISPATCH_ODE(obj, method, MACRO)                              \
+  do {                                                                    \
+    const bool lv_ = (obj) == kLvFit;                                     \
+    if ((method) == kOdeTsit5) {                                          \
+      if (lv_) MACRO(kOdeLV, kOdeTsit5); else MACRO(kOdeFHN, kOdeTsit5);  \
+    } else {                                                              \
+      if (lv_) MACRO(kOdeLV, kOdeRk4); else MACRO(kOdeFHN, kOdeRk4);      \
+    }                                                                     \
+  } while (0)
+
 int ode_check(const pps_problem* prob) {
   if (prob->dim < 1 || prob->dim > kOdeMaxDim)
     return set_error(PPS_EINVAL, "ODE fits have at most %d parameters (got %d)", kOdeMaxDim, prob->dim);
   if (prob->objective == kLvFit && prob->dim != 4)
     return set_error(PPS_EINVAL, "the Lotka-Volterra fit has 4 parameters (got %d)", prob->dim);
-  if (prob->objective == kFhnFit && prob->dim != 3)
-    return set_error(PPS_EINVAL, "the FitzHugh-Nagumo fit has 3 parameters (got %d)", prob->dim);
+  if (prob->objective == kFhnFit && prob->dim != 3 && prob->dim != 4)
+    return set_error(PPS_EINVAL, "the FitzHugh-Nagumo fit has 3 parameters, or 4 with l (got %d)", prob->dim);
   if (prob->nparams < 5 || !prob->params)
     return set_error(PPS_EINVAL, "ODE fits take params = [u0_1, u0_2, dt, nsteps, save_every(, l)]");
-  if (prob->objective == kFhnFit && prob->nparams < 6)
-    return set_error(PPS_EINVAL, "the FitzHugh-Nagumo fit needs params[5] = l");
+  if (prob->objective == kFhnFit && prob->dim == 3 && prob->nparams < 6)
+    return set_error(PPS_EINVAL, "the FitzHugh-Nagumo fit of 3 parameters needs params[5] = l");
   const float nsteps = prob->params[3], every = prob->params[4];
   if (!(prob->params[2] > 0.0f) || !(nsteps >= 1.0f) || !(every >= 1.0f) || nsteps != (float)(int)nsteps ||
       every != (float)(int)every)
     return set_error(PPS_EINVAL, "ODE fit needs dt > 0 and integral nsteps, save_every >= 1");
   if (!prob->data || prob->ndata < 2 || (prob->ndata & 1) || prob->ndata / 2 > kOdeMaxSaves)
     return set_error(PPS_EINVAL, "ODE fit needs data of 2 * nsaves floats, 1 <= nsaves <= %d", kOdeMaxSaves);
+  const float method = prob->nparams > 6 ? prob->params[6] : 0.0f;
+  if (method != (float)kOdeRk4 && method != (float)kOdeTsit5)
+    return set_error(PPS_EINVAL, "ODE fit: params[6] (method) is 0 (RK4) or 1 (Tsit5)");
+  if (method == (float)kOdeTsit5) {
+    const float save_dt = prob->nparams > 7 ? prob->params[7] : 0.0f;
+    if (!(save_dt > 0.0f) || !std::isfinite(save_dt))
+      return set_error(PPS_EINVAL, "ODE fit with Tsit5 needs params[7] = save_dt > 0");
+    if ((double)(prob->ndata / 2 - 1) * save_dt > (double)nsteps * prob->params[2] * (1.0 + 1e-6))
+      return set_error(PPS_EINVAL, "ODE fit: (nsaves - 1) * save_dt exceeds nsteps * dt");
+    return PPS_OK;
+  }
   if ((prob->ndata / 2 - 1) * (int64_t)every > (int64_t)nsteps)
     return set_error(PPS_EINVAL, "ODE fit: (nsaves - 1) * save_every exceeds nsteps");
   return PPS_OK;
@@ -157,10 +182,10 @@ static OdeCfg cfg_of(pps_swarm* s) { return ode_cfg(s->op, s->od.ndata); }
 int launch_init_ode(pps_swarm* s, int sampler, const float* u0_dev) {
   const unsigned blocks = (unsigned)((s->dv.npad + kOdeThreads - 1) / kOdeThreads);
   const OdeCfg c = cfg_of(s);
-  if (s->objective == kLvFit)
-    k_init_ode<kOdeLV><<<blocks, kOdeThreads, 0, s->stream>>>(s->dv, s->op, c, s->od.data, s->seed, sampler, u0_dev);
-  else
-    k_init_ode<kOdeFHN><<<blocks, kOdeThreads, 0, s->stream>>>(s->dv, s->op, c, s->od.data, s->seed, sampler, u0_dev);
+#define L_INIT_ODE(M, I) \
+  k_init_ode<M, I><<<blocks, kOdeThreads, 0, s->stream>>>(s->dv, s->op, c, s->od.data, s->seed, sampler, u0_dev)
+  PPS_DISPATCH_ODE(s->objective, c.method, L_INIT_ODE);
+#undef L_INIT_ODE
   PPS_CUDA(cudaGetLastError());
   return PPS_OK;
 }
@@ -169,15 +194,16 @@ int launch_sync_step_ode(pps_swarm* s, float c1, float c2) {
   const unsigned blocks = (unsigned)((s->dv.npad + kOdeThreads - 1) / kOdeThreads);
   const OdeCfg c = cfg_of(s);
   const int from_pos = (s->flags & PPS_FLAG_GBEST_FROM_POSITION) ? 1 : 0;
-  if (s->objective == kLvFit)
-    k_sync_step_ode<kOdeLV><<<blocks, kOdeThreads, 0, s->stream>>>(s->dv, s->op, c, s->od.data, s->seed, c1, c2, from_pos);
-  else
-    k_sync_step_ode<kOdeFHN><<<blocks, kOdeThreads, 0, s->stream>>>(s->dv, s->op, c, s->od.data, s->seed, c1, c2, from_pos);
+#define L_STEP_ODE(M, I)                                                                                 \
+  k_sync_step_ode<M, I><<<blocks, kOdeThreads, 0, s->stream>>>(s->dv, s->op, c, s->od.data, s->seed, c1, c2, \
+                                                               from_pos)
+  PPS_DISPATCH_ODE(s->objective, c.method, L_STEP_ODE);
+#undef L_STEP_ODE
   PPS_CUDA(cudaGetLastError());
   return PPS_OK;
 }
 
-template <int MODEL>
+template <int MODEL, int METHOD>
 __global__ void k_eval_ode(ObjParams op, OdeCfg cfg, const float* __restrict__ data_g, const float* __restrict__ x,
                            int64_t npts, int64_t stride, float* __restrict__ f) {
   __shared__ float data[2 * kOdeMaxSaves];
@@ -189,17 +215,16 @@ __global__ void k_eval_ode(ObjParams op, OdeCfg cfg, const float* __restrict__ d
 #pragma unroll
   for (int d = 0; d < kOdeMaxDim; ++d)
     if (d < op.dim) p[d] = x[(int64_t)d * stride + i];
-  f[i] = ode_eval<MODEL>(p, cfg, data);
+  f[i] = ode_eval<MODEL, METHOD>(p, cfg, data);
 }
 
 int launch_eval_ode(const ObjParams& op, const ObjData& od, int objective, const float* x, int64_t npts,
                     int64_t stride, float* f, cudaStream_t stream) {
   const unsigned blocks = (unsigned)((npts + 127) / 128);
   const OdeCfg c = ode_cfg(op, od.ndata);
-  if (objective == kLvFit)
-    k_eval_ode<kOdeLV><<<blocks, 128, 0, stream>>>(op, c, od.data, x, npts, stride, f);
-  else
-    k_eval_ode<kOdeFHN><<<blocks, 128, 0, stream>>>(op, c, od.data, x, npts, stride, f);
+#define L_EVAL_ODE(M, I) k_eval_ode<M, I><<<blocks, 128, 0, stream>>>(op, c, od.data, x, npts, stride, f)
+  PPS_DISPATCH_ODE(objective, c.method, L_EVAL_ODE);
+#undef L_EVAL_ODE
   PPS_CUDA(cudaGetLastError());
   return PPS_OK;
 }

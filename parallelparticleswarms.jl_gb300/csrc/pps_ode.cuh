@@ -8,11 +8,17 @@
 // The workload integrates with the classical fixed-step RK4 instead; the
 // stage arithmetic below is exactly the CPU restatement's (fused multiply-adds
 // where it writes fmaf).
+// Integrators: the workload's classical fixed-step RK4 with saves every
+// save_every steps, or the reference's own method, Tsitouras' 5(4) pair
+// (GPUTsit5) at a fixed step, adaptive = false as the reference's benchmarks
+// run it (benchmarks/Lotka_Volterra/lotka_volterra.jl:122-127), with saves
+// at t_m = m save_dt taken from the method's 4th-order continuous extension.
 // Right-hand sides (the reference's benchmark models):
 //   Lotka-Volterra  benchmarks/Lotka_Volterra/lotka_volterra.jl:9-13
 //     du1 = p1 u1 - p2 u1 u2,  du2 = -p3 u2 + p4 u1 u2
 //   FitzHugh-Nagumo benchmarks/Fitzhugh_Nagumo/ode_estimation.jl:6-12
-//     dv = v - v^3/3 - w + l,  dw = tinv (v + a - b w),  p = (a, b, tinv), l fixed
+//     dv = v - v^3/3 - w + l,  dw = tinv (v + a - b w),  p = (a, b, tinv) with l
+//     fixed, or p = (a, b, tinv, l) as the reference's benchmark fits it
 // evaluated in factored form -- u1 fma(-p2, u2, p1), u2 fma(p4, u1, -p3),
 // (fma(v^3, -1/3, v) - w) + l, tinv fma(-b, w, v + a) -- two roundings per
 // term and no division, which halves the instructions of an RK4 step.
@@ -24,12 +30,19 @@ namespace pps {
 constexpr int kOdeLV = 0;
 constexpr int kOdeFHN = 1;
 constexpr int kOdeMaxSaves = 4096;
+constexpr int kOdeRk4 = 0;
+constexpr int kOdeTsit5 = 1;
 
 // Fit configuration, packed by the host from pps_problem.params:
-// params = [u0_1, u0_2, dt, nsteps, save_every, l (FHN)], data = nsaves x 2.
+// params = [u0_1, u0_2, dt, nsteps, save_every, l (FHN), method, save_dt],
+// data = nsaves x 2 (t = 0 included).  method 0 (default): RK4, a save every
+// save_every steps; 1: Tsit5, saves at m * save_dt.
 struct OdeCfg {
   float u0a, u0b, dt, l;
   int nsteps, save_every, nsaves;
+  int method;
+  float save_dt;
+  int dim;  // FHN: 3 fits (a, b, tinv) with l fixed, 4 fits l as well
 };
 
 __host__ __device__ inline OdeCfg ode_cfg(const ObjParams& op, int64_t ndata) {
@@ -41,8 +54,14 @@ __host__ __device__ inline OdeCfg ode_cfg(const ObjParams& op, int64_t ndata) {
   c.save_every = (int)op.p[4];
   c.l = op.p[5];
   c.nsaves = (int)(ndata / 2);
+  c.method = op.np > 6 ? (int)op.p[6] : kOdeRk4;
+  c.save_dt = op.np > 7 ? op.p[7] : 0.0f;
+  c.dim = op.dim;
   return c;
 }
+
+// FHN's l: fixed by the fit, or the particle's 4th parameter
+__device__ __forceinline__ float ode_l(const float* p, const OdeCfg& c) { return c.dim > 3 ? p[3] : c.l; }
 
 template <int MODEL>
 __device__ __forceinline__ void ode_rhs(const float* p, float l, float u0, float u1, float& d0, float& d1) {
@@ -79,13 +98,14 @@ __device__ __forceinline__ float ode_loss(const float* p, const OdeCfg& c, const
   const float dt = c.dt;
   const float h2 = __fmul_rn(dt, 0.5f);
   const float h6 = __fdiv_rn(dt, 6.0f);
+  const float l = ode_l(p, c);
   float u0 = c.u0a, u1 = c.u0b;
   float e0 = __fsub_rn(data[0], u0), e1 = __fsub_rn(data[1], u1);
   float acc = __fadd_rn(__fmul_rn(e0, e0), __fmul_rn(e1, e1));
   int m = 1;
   int next = c.save_every;
   for (int s = 1; s <= c.nsteps && m < c.nsaves; ++s) {
-    rk4_step<MODEL>(p, c.l, dt, h2, h6, u0, u1);
+    rk4_step<MODEL>(p, l, dt, h2, h6, u0, u1);
     if (s == next) {
       e0 = __fsub_rn(data[2 * m], u0);
       e1 = __fsub_rn(data[2 * m + 1], u1);
@@ -93,6 +113,120 @@ __device__ __forceinline__ float ode_loss(const float* p, const OdeCfg& c, const
       ++m;
       next += c.save_every;
     }
+  }
+  return acc;
+}
+
+// ---------------------------------------------------------------- Tsit5
+// Tsitouras, "Runge-Kutta pairs of order 5(4) satisfying only the first
+// column simplifying assumption", Comput. Math. Appl. 62 (2011) 770-775: the
+// 7-stage first-same-as-last pair (b = the 7th stage's row) and its
+// continuous extension b_i(theta) = delta_i1 theta + r_i2 theta^2 +
+// r_i3 theta^3 + r_i4 theta^4.  Decimal constants rounded to binary32 by the
+// compiler; the models are autonomous, so the nodes c_i are not needed.
+namespace ts5 {
+constexpr float a21 = 0.161f;
+constexpr float a31 = -0.008480655492356989f, a32 = 0.335480655492357f;
+constexpr float a41 = 2.897153057105493f, a42 = -6.359448489975075f, a43 = 4.3622954328695815f;
+constexpr float a51 = 5.325864828439257f, a52 = -11.748883564062828f, a53 = 7.4955393428898365f,
+                a54 = -0.09249506636175525f;
+constexpr float a61 = 5.86145544294642f, a62 = -12.92096931784711f, a63 = 8.159367898576159f,
+                a64 = -0.071584973281401f, a65 = -0.028269050394068383f;
+constexpr float b1 = 0.09646076681806523f, b2 = 0.01f, b3 = 0.4798896504144996f, b4 = 1.379008574103742f,
+                b5 = -3.290069515436081f, b6 = 2.324710524099774f;
+// continuous extension (r_i2, r_i3, r_i4); r_11 = 1
+constexpr float r12 = -2.763706197274826f, r13 = 2.9132554618219126f, r14 = -1.0530884977290216f;
+constexpr float r22 = 0.1317f, r23 = -0.2234f, r24 = 0.1017f;
+constexpr float r32 = 3.9302962368947516f, r33 = -5.941033872131505f, r34 = 2.490627285651253f;
+constexpr float r42 = -12.411077166933676f, r43 = 30.33818863028232f, r44 = -16.548102889244902f;
+constexpr float r52 = 37.50931341651104f, r53 = -88.1789048947664f, r54 = 47.37952196281928f;
+constexpr float r62 = -27.896526289197286f, r63 = 65.09189467479366f, r64 = -34.87065786149661f;
+constexpr float r72 = 1.5f, r73 = -4.0f, r74 = 2.5f;
+}  // namespace ts5
+
+// One step from u with k[0] = f(u) on entry; on exit k[0..6] are the seven
+// stages, (n0, n1) = u + dt sum_i b_i k_i and k[6] = f(n) (the next step's k[0]).
+// Stage sums are formed left to right with fused multiply-adds.
+template <int MODEL>
+__device__ __forceinline__ void tsit5_step(const float* p, float l, float dt, float u0, float u1, float (&ka)[7],
+                                           float (&kb)[7], float& n0, float& n1) {
+  using namespace ts5;
+  float sa, sb;
+  sa = __fmul_rn(a21, ka[0]);
+  sb = __fmul_rn(a21, kb[0]);
+  ode_rhs<MODEL>(p, l, __fmaf_rn(dt, sa, u0), __fmaf_rn(dt, sb, u1), ka[1], kb[1]);
+  sa = __fmaf_rn(a32, ka[1], __fmul_rn(a31, ka[0]));
+  sb = __fmaf_rn(a32, kb[1], __fmul_rn(a31, kb[0]));
+  ode_rhs<MODEL>(p, l, __fmaf_rn(dt, sa, u0), __fmaf_rn(dt, sb, u1), ka[2], kb[2]);
+  sa = __fmaf_rn(a43, ka[2], __fmaf_rn(a42, ka[1], __fmul_rn(a41, ka[0])));
+  sb = __fmaf_rn(a43, kb[2], __fmaf_rn(a42, kb[1], __fmul_rn(a41, kb[0])));
+  ode_rhs<MODEL>(p, l, __fmaf_rn(dt, sa, u0), __fmaf_rn(dt, sb, u1), ka[3], kb[3]);
+  sa = __fmaf_rn(a54, ka[3], __fmaf_rn(a53, ka[2], __fmaf_rn(a52, ka[1], __fmul_rn(a51, ka[0]))));
+  sb = __fmaf_rn(a54, kb[3], __fmaf_rn(a53, kb[2], __fmaf_rn(a52, kb[1], __fmul_rn(a51, kb[0]))));
+  ode_rhs<MODEL>(p, l, __fmaf_rn(dt, sa, u0), __fmaf_rn(dt, sb, u1), ka[4], kb[4]);
+  sa = __fmaf_rn(a65, ka[4],
+                 __fmaf_rn(a64, ka[3], __fmaf_rn(a63, ka[2], __fmaf_rn(a62, ka[1], __fmul_rn(a61, ka[0])))));
+  sb = __fmaf_rn(a65, kb[4],
+                 __fmaf_rn(a64, kb[3], __fmaf_rn(a63, kb[2], __fmaf_rn(a62, kb[1], __fmul_rn(a61, kb[0])))));
+  ode_rhs<MODEL>(p, l, __fmaf_rn(dt, sa, u0), __fmaf_rn(dt, sb, u1), ka[5], kb[5]);
+  sa = __fmaf_rn(b6, ka[5], __fmaf_rn(b5, ka[4], __fmaf_rn(b4, ka[3],
+                 __fmaf_rn(b3, ka[2], __fmaf_rn(b2, ka[1], __fmul_rn(b1, ka[0]))))));
+  sb = __fmaf_rn(b6, kb[5], __fmaf_rn(b5, kb[4], __fmaf_rn(b4, kb[3],
+                 __fmaf_rn(b3, kb[2], __fmaf_rn(b2, kb[1], __fmul_rn(b1, kb[0]))))));
+  n0 = __fmaf_rn(dt, sa, u0);
+  n1 = __fmaf_rn(dt, sb, u1);
+  ode_rhs<MODEL>(p, l, n0, n1, ka[6], kb[6]);
+}
+
+// b_i(theta) = theta^2 (r_i2 + theta (r_i3 + theta r_i4)), i >= 2, by Horner's rule
+__device__ __forceinline__ float tsit5_weight(float th, float th2, float r2, float r3, float r4) {
+  return __fmul_rn(th2, __fmaf_rn(th, __fmaf_rn(th, r4, r3), r2));
+}
+
+// u + dt sum_i b_i(theta) k_i
+__device__ __forceinline__ float tsit5_dense(float u, float dt, float th, const float (&k)[7]) {
+  using namespace ts5;
+  const float th2 = __fmul_rn(th, th);
+  const float w1 = __fmul_rn(th, __fmaf_rn(th, __fmaf_rn(th, __fmaf_rn(th, r14, r13), r12), 1.0f));
+  float s = __fmul_rn(w1, k[0]);
+  s = __fmaf_rn(tsit5_weight(th, th2, r22, r23, r24), k[1], s);
+  s = __fmaf_rn(tsit5_weight(th, th2, r32, r33, r34), k[2], s);
+  s = __fmaf_rn(tsit5_weight(th, th2, r42, r43, r44), k[3], s);
+  s = __fmaf_rn(tsit5_weight(th, th2, r52, r53, r54), k[4], s);
+  s = __fmaf_rn(tsit5_weight(th, th2, r62, r63, r64), k[5], s);
+  s = __fmaf_rn(tsit5_weight(th, th2, r72, r73, r74), k[6], s);
+  return __fmaf_rn(dt, s, u);
+}
+
+// SSE of the Tsit5 solution at t_m = m save_dt (m < nsaves) against data
+template <int MODEL>
+__device__ __forceinline__ float tsit5_loss(const float* p, const OdeCfg& c, const float* data) {
+  const float dt = c.dt;
+  float u0 = c.u0a, u1 = c.u0b;
+  float e0 = __fsub_rn(data[0], u0), e1 = __fsub_rn(data[1], u1);
+  float acc = __fadd_rn(__fmul_rn(e0, e0), __fmul_rn(e1, e1));
+  const float l = ode_l(p, c);
+  float ka[7], kb[7];
+  ode_rhs<MODEL>(p, l, u0, u1, ka[0], kb[0]);
+  int m = 1;
+  float tm = c.save_dt;
+  for (int n = 0; n < c.nsteps && m < c.nsaves; ++n) {
+    const float tn = __fmul_rn(__int2float_rn(n), dt);
+    const float tn1 = __fmul_rn(__int2float_rn(n + 1), dt);
+    float n0, n1;
+    tsit5_step<MODEL>(p, l, dt, u0, u1, ka, kb, n0, n1);
+    while (m < c.nsaves && tm <= tn1) {  // the saves inside (t_n, t_n+1]
+      const float th = __fdiv_rn(__fsub_rn(tm, tn), dt);
+      e0 = __fsub_rn(data[2 * m], tsit5_dense(u0, dt, th, ka));
+      e1 = __fsub_rn(data[2 * m + 1], tsit5_dense(u1, dt, th, kb));
+      acc = __fadd_rn(acc, __fadd_rn(__fmul_rn(e0, e0), __fmul_rn(e1, e1)));
+      ++m;
+      tm = __fmul_rn(__int2float_rn(m), c.save_dt);
+    }
+    u0 = n0;
+    u1 = n1;
+    ka[0] = ka[6];
+    kb[0] = kb[6];
   }
   return acc;
 }

@@ -433,9 +433,11 @@ int pps_serve_submit(pps_server* s, const pps_problem* prob, int64_t n, uint64_t
   Request* r = new (std::nothrow) Request();
   if (!r) return set_error(PPS_ENOMEM, "host allocation failed");
   // MLP fits (the tensor-core kernel wants whole SMs), constrained problems,
-  // user objectives and large swarms run as a swarm of their own with the
-  // multi-block step kernels; the rest are packed into batched launches
-  const bool single = prob && (prob->objective == kMlp || prob->ncons > 0 || is_user(prob->objective) ||
+  // user objectives, Tsit5 ODE fits and large swarms run as a swarm of their
+  // own with the multi-block step kernels; the rest are packed into batched
+  // launches
+  const bool tsit5 = prob && is_ode(prob->objective) && prob->nparams > 6 && prob->params && prob->params[6] != 0.0f;
+  const bool single = prob && (prob->objective == kMlp || prob->ncons > 0 || is_user(prob->objective) || tsit5 ||
                                (s->cfg.single_min_n > 0 && n >= s->cfg.single_min_n));
   if (single) {
     int rc = swarm_check(prob, n);

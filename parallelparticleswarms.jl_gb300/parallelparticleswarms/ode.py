@@ -1,10 +1,15 @@
 """ode_pso: estimate ODE parameters by PSO (src/ode_pso.jl).
 
 An ODE fit is an OptimizationProblem whose objective integrates the model
-with the particle's position as its parameters (fixed-step RK4 on the device)
-and returns the SSE against observations (_reduce_losses!, src/ode_pso.jl:47-52).
-The fit configuration travels in ``p`` = [u0_1, u0_2, dt, nsteps, save_every, l]
-and the observations in ``data`` (nsaves x 2, t = 0 included).
+with the particle's position as its parameters and returns the SSE against
+observations (_reduce_losses!, src/ode_pso.jl:47-52).  Two fixed-step
+integrators run on the device: the classical RK4 with a save every
+``save_every`` steps (the workload's), and Tsitouras' 5(4) pair, the
+reference's GPUTsit5 (src/ode_pso.jl:58) with adaptive = false as its
+benchmarks run it, saving at t_m = m * save_dt from the method's continuous
+extension.  The fit configuration travels in ``p`` = [u0_1, u0_2, dt, nsteps,
+save_every, l, method, save_dt] (method 0 = RK4, 1 = Tsit5) and the
+observations in ``data`` (nsaves x 2, t = 0 included).
 
 ``trajectory64`` / ``synthetic_fit`` build synthetic observations on the host
 (float64 RK4 plus Gaussian noise) for the workloads; they are input
@@ -44,19 +49,36 @@ def trajectory64(model: str, p, u0, dt: float, nsteps: int, save_every: int, l: 
     return np.array(out)
 
 
-def lv_problem(data, u0=(1.0, 1.0), dt=0.01, nsteps=1000, save_every=10, lb=0.0, ub=5.0) -> OptimizationProblem:
+METHODS = {"rk4": 0, "tsit5": 1}
+
+
+def _fit_params(u0, dt, nsteps, save_every, l, method, save_dt):
+    prm = [u0[0], u0[1], dt, nsteps, save_every, l]
+    if method == "tsit5":
+        if save_dt is None:
+            raise ValueError("a Tsit5 fit needs save_dt (the spacing of the observations)")
+        prm += [float(METHODS[method]), float(save_dt)]
+    elif method != "rk4":
+        raise ValueError(f"method must be one of {sorted(METHODS)}")
+    return prm
+
+
+def lv_problem(data, u0=(1.0, 1.0), dt=0.01, nsteps=1000, save_every=10, lb=0.0, ub=5.0, method="rk4",
+               save_dt=None) -> OptimizationProblem:
     """Lotka-Volterra fit: du1 = a u1 - b u1 u2, du2 = -c u2 + d u1 u2 (4 parameters)."""
     return OptimizationProblem(lotka_volterra_fit, np.zeros(4, np.float32),
-                               [u0[0], u0[1], dt, nsteps, save_every, 0.0],
+                               _fit_params(u0, dt, nsteps, save_every, 0.0, method, save_dt),
                                lb=np.full(4, lb, np.float32), ub=np.full(4, ub, np.float32), data=data)
 
 
 def fhn_problem(data, u0=(-1.0, 1.0), dt=0.01, nsteps=2000, save_every=10, l=FHN_L, lb=0.0,
-                ub=5.0) -> OptimizationProblem:
-    """FitzHugh-Nagumo fit of (a, b, tinv): dv = v - v^3/3 - w + l, dw = tinv (v + a - b w)."""
-    return OptimizationProblem(fitzhugh_nagumo_fit, np.zeros(3, np.float32),
-                               [u0[0], u0[1], dt, nsteps, save_every, l],
-                               lb=np.full(3, lb, np.float32), ub=np.full(3, ub, np.float32), data=data)
+                ub=5.0, method="rk4", save_dt=None, fit_l=False) -> OptimizationProblem:
+    """FitzHugh-Nagumo fit of (a, b, tinv), or of (a, b, tinv, l) with ``fit_l``:
+    dv = v - v^3/3 - w + l, dw = tinv (v + a - b w)."""
+    D = 4 if fit_l else 3
+    return OptimizationProblem(fitzhugh_nagumo_fit, np.zeros(D, np.float32),
+                               _fit_params(u0, dt, nsteps, save_every, l, method, save_dt),
+                               lb=np.full(D, lb, np.float32), ub=np.full(D, ub, np.float32), data=data)
 
 
 def synthetic_fit(model: str, seed: int, noise: float = 0.01, perturb: float = 0.2):
@@ -73,6 +95,44 @@ def synthetic_fit(model: str, seed: int, noise: float = 0.01, perturb: float = 0
     traj = trajectory64("fhn", truth, (-1.0, 1.0), 0.01, 2000, 10)
     data = (traj + rng.normal(0.0, noise, traj.shape)).astype(np.float32)
     return fhn_problem(data), truth
+
+
+def _dense64(model: str, p, u0, t_save, h: float = 1e-3, l: float = FHN_L) -> np.ndarray:
+    """float64 RK4 at step h, sampled at the times t_save (multiples of h)."""
+    p = np.asarray(p, dtype=np.float64)
+    u = np.array(u0, dtype=np.float64)
+    marks = np.rint(np.asarray(t_save) / h).astype(np.int64)
+    out, s = [], 0
+    for m in marks:
+        while s < m:
+            k1 = _rhs64(model, p, u, l)
+            k2 = _rhs64(model, p, u + 0.5 * h * k1, l)
+            k3 = _rhs64(model, p, u + 0.5 * h * k2, l)
+            k4 = _rhs64(model, p, u + h * k3, l)
+            u = u + h / 6 * (k1 + 2 * k2 + 2 * k3 + k4)
+            s += 1
+        out.append(u.copy())
+    return np.array(out)
+
+
+def reference_benchmark_fit(model: str):
+    """The reference's own ode_pso benchmarks (benchmarks/Lotka_Volterra/
+    lotka_volterra.jl, benchmarks/Fitzhugh_Nagumo/ode_estimation.jl):
+    observations at t = 0:0.01:3 (301 points) from an accurate solve of the
+    true model, Tsit5 at dt = 0.1 with saveat = those points (adaptive =
+    false), 10,000 particles, 100 iterations.  LV fits (1.5, 1, 3, 1) from
+    u0 = [1, 1] on [0, 10]^4; FHN fits (a, b, tinv, l) = (0.7, 0.8, 0.08, 0.5)
+    from u0 = [1, 1] on [0, 5]^4.  The observations come from a float64 RK4
+    at step 1e-3 (the reference solves with reltol 1e-9 / 1e-6)."""
+    t = np.arange(301) * 0.01
+    if model == "lv":
+        data = _dense64("lv", LV_TRUTH, (1.0, 1.0), t).astype(np.float32)
+        return lv_problem(data, u0=(1.0, 1.0), dt=0.1, nsteps=30, save_every=1, lb=0.0, ub=10.0, method="tsit5",
+                          save_dt=0.01), np.array(LV_TRUTH)
+    truth = (0.7, 0.8, 0.08, 0.5)
+    data = _dense64("fhn", truth[:3], (1.0, 1.0), t, l=truth[3]).astype(np.float32)
+    return fhn_problem(data, u0=(1.0, 1.0), dt=0.1, nsteps=30, save_every=1, l=0.0, lb=0.0, ub=5.0,
+                       method="tsit5", save_dt=0.01, fit_l=True), np.array(truth)
 
 
 def parameter_estim_ode(prob: OptimizationProblem, n: int, *, maxiters: int = 100, w: float = 0.7298,

@@ -6,12 +6,8 @@ import pytest
 
 
 def oracle_ode_problem(orc, prob):
-    """OracleProblem for an ODE-fit pps problem (p = [u0_1, u0_2, dt, nsteps, save_every, l])."""
-    p = prob.p
-    model = orc.ODE_LV if prob.f.name == "lotka_volterra_fit" else orc.ODE_FHN
-    fit = orc.OracleOdeFit(model, prob.dim, (p[0], p[1]), p[2], int(p[3]), int(p[4]), prob.data,
-                           fixed=(p[5], 0.0, 0.0, 0.0))
-    return orc.OracleProblem(4 if model == orc.ODE_LV else 5, prob.dim, prob.lb, prob.ub, ode=fit)
+    """OracleProblem for an ODE-fit pps problem."""
+    return orc.ode_fit_problem(prob)
 
 
 def test_rk4_matches_float64(orc):
