@@ -10,8 +10,11 @@ iterations.
 
 Prints ONE JSON line (rank 0).  Extra measurements ride in the same line:
   e2e          the same metric through the public solve() API with host
-               buffers: allocation, init, the loop, and the copy-back of the
-               solution and of every particle's position (sol.original)
+               buffers: allocation, init, the loop, the device snapshot of
+               every particle's position (sol.original, which the reference
+               also keeps on the device, src/solve.jl:51-56) and the copy-back
+               of the solution u and f(u); reading sol.original to the host
+               afterwards is timed separately (original_to_host_ms)
   roofline     the step kernel against the measured HBM copy bandwidth
   cpu_baseline the oracle (C restatement, all host cores) on a bounded sample
   async        ParallelPSOKernel(global_update=false) on the same workload
@@ -700,12 +703,16 @@ def main():
             _ = sol.objective
         barrier()
         e2e_s = multi.max_over_ranks(time.perf_counter() - t0, dist, f"cuda:{local}")
-        h2d = 4 * (3 * DIM + 1)  # lb, ub, u0, p
-        d2h = 4 * DIM + 8 + 4 + 4 * N_PARTICLES * DIM  # u, gbest cost+index, objective, original positions
+        t1 = time.perf_counter()
+        original = np.asarray(sol.original)  # every position to the host, once
+        original_ms = (time.perf_counter() - t1) * 1e3
+        h2d = 4 * (3 * DIM + 1) + 4 * DIM  # lb, ub, u0, p; the point u of f(u)
+        d2h = 4 * DIM + 4 + 8 + 4  # u, gbest cost and index, f(u)
         e2e = {"value": N_PARTICLES * iters * e2e_steps * world / e2e_s, "unit": UNIT,
                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "steps": e2e_steps,
+               "original_to_host_ms": original_ms, "original_shape": list(original.shape),
                "path": "parallelparticleswarms.solve -> libpps_cuda.so C ABI (pps_swarm_create/init/sync_run/"
-                       "get_gbest/get_state/eval_objective)"}
+                       "get_gbest/field_copy_create/eval_objective)"}
 
     # ---- CPU baseline (oracle on the host cores) --------------------------
     extras = {}

@@ -275,6 +275,14 @@ PPS_API int pps_get_gbest(pps_swarm* s, float* u, float* cost, int64_t* idx);
 /* copy a state field to / from host memory (SoA, particle fastest) */
 PPS_API int pps_get_state(pps_swarm* s, int32_t field, float* out);
 PPS_API int pps_set_state(pps_swarm* s, int32_t field, const float* in);
+/* A device snapshot of a state field: sol.original = get_pos.(particles), which the
+ * reference keeps on the device as a new array (src/solve.jl:51-56).  The swarm may be
+ * re-run or destroyed while the snapshot lives; read copies it to host memory in
+ * pps_get_state's layout (SoA, particle fastest). */
+typedef struct pps_field_copy pps_field_copy;
+PPS_API int pps_field_copy_create(pps_swarm* s, int32_t field, pps_field_copy** out);
+PPS_API int pps_field_copy_read(pps_field_copy* c, float* out);
+PPS_API int pps_field_copy_destroy(pps_field_copy* c);
 /* evaluate the problem's objective at npoints points (SoA dim x npoints) on
  * the device; used for sol.objective = f(u, p) (src/solve.jl:54-57) */
 PPS_API int pps_eval_objective(const pps_problem* prob, int64_t npoints, const float* x, float* f);

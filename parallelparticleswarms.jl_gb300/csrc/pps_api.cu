@@ -587,15 +587,15 @@ static HostStage& host_stage(int device) {
 
 // rows x row_bytes from dev (pitch src_pitch bytes) to the contiguous host
 // array out, on stream
-static int copy_rows_to_host(pps_swarm* s, char* out, const char* dev, size_t src_pitch, size_t row_bytes,
-                             size_t rows) {
+static int copy_rows_to_host(int device, cudaStream_t stream, char* out, const char* dev, size_t src_pitch,
+                             size_t row_bytes, size_t rows) {
   const size_t total = row_bytes * rows;
-  if (total < ((size_t)4 << 20) || s->device < 0 || s->device >= 64) {
-    PPS_CUDA(cudaMemcpy2DAsync(out, row_bytes, dev, src_pitch, row_bytes, rows, cudaMemcpyDeviceToHost, s->stream));
-    PPS_CUDA(cudaStreamSynchronize(s->stream));
+  if (total < ((size_t)4 << 20) || device < 0 || device >= 64) {
+    PPS_CUDA(cudaMemcpy2DAsync(out, row_bytes, dev, src_pitch, row_bytes, rows, cudaMemcpyDeviceToHost, stream));
+    PPS_CUDA(cudaStreamSynchronize(stream));
     return PPS_OK;
   }
-  HostStage& hs = host_stage(s->device);
+  HostStage& hs = host_stage(device);
   std::lock_guard<std::mutex> lock(hs.mu);
   if (!hs.ready) {
     for (int k = 0; k < 2; ++k) {
@@ -626,8 +626,8 @@ static int copy_rows_to_host(pps_swarm* s, char* out, const char* dev, size_t sr
     if (k < pieces.size()) {  // copy engine: piece k into buffer k % 2
       const Piece& p = pieces[k];
       PPS_CUDA(cudaMemcpy2DAsync(hs.buf[k & 1], p.bytes, dev + p.src_off, src_pitch, p.bytes, p.rows,
-                                 cudaMemcpyDeviceToHost, s->stream));
-      PPS_CUDA(cudaEventRecord(hs.ev[k & 1], s->stream));
+                                 cudaMemcpyDeviceToHost, stream));
+      PPS_CUDA(cudaEventRecord(hs.ev[k & 1], stream));
     }
     if (k >= 1) {  // host: piece k - 1 out of its buffer while piece k is in flight
       const Piece& p = pieces[k - 1];
@@ -654,7 +654,7 @@ int pps_get_state(pps_swarm* s, int32_t field, float* out) {
   int rows;
   if ((rc = field_ptr(s, field, &dev, &rows))) return rc;
   const size_t w = sizeof(float) * (size_t)s->dv.n;
-  return copy_rows_to_host(s, reinterpret_cast<char*>(out), reinterpret_cast<const char*>(dev),
+  return copy_rows_to_host(s->device, s->stream, reinterpret_cast<char*>(out), reinterpret_cast<const char*>(dev),
                            sizeof(float) * (size_t)s->dv.npad, w, (size_t)rows);
 }
 
@@ -670,6 +670,71 @@ int pps_set_state(pps_swarm* s, int32_t field, const float* in) {
   PPS_CUDA(cudaMemcpy2DAsync(dev, sizeof(float) * (size_t)s->dv.npad, in, w, w, rows,
                              cudaMemcpyHostToDevice, s->stream));
   PPS_CUDA(cudaStreamSynchronize(s->stream));
+  return PPS_OK;
+}
+
+// A device snapshot of a state field, as the reference's sol.original =
+// get_pos.(particles) is a new device array (src/solve.jl:51-56): the
+// swarm may be re-run or destroyed while the snapshot lives.
+struct pps_field_copy {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ready = nullptr;
+  float* dev = nullptr;
+  int rows = 0;
+  int64_t n = 0;
+};
+
+int pps_field_copy_create(pps_swarm* s, int32_t field, pps_field_copy** out) {
+  if (!s || !out) return set_error(PPS_EINVAL, "NULL argument");
+  int rc = use_device(s);
+  if (rc) return rc;
+  float* src;
+  int rows;
+  if ((rc = field_ptr(s, field, &src, &rows))) return rc;
+  pps_field_copy* c = new (std::nothrow) pps_field_copy();
+  if (!c) return set_error(PPS_ENOMEM, "host allocation failed");
+  c->device = s->device;
+  c->rows = rows;
+  c->n = s->dv.n;
+  const size_t w = sizeof(float) * (size_t)s->dv.n;
+  cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ready, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaMallocAsync(reinterpret_cast<void**>(&c->dev), w * (size_t)rows, s->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpy2DAsync(c->dev, w, src, sizeof(float) * (size_t)s->dv.npad, w, (size_t)rows,
+                          cudaMemcpyDeviceToDevice, s->stream);
+  if (e == cudaSuccess) e = cudaEventRecord(c->ready, s->stream);
+  if (e != cudaSuccess) {
+    pps_field_copy_destroy(c);
+    return cuda_error(e, "pps_field_copy_create");
+  }
+  *out = c;
+  return PPS_OK;
+}
+
+int pps_field_copy_read(pps_field_copy* c, float* out) {
+  if (!c || !out) return set_error(PPS_EINVAL, "NULL argument");
+  PPS_CUDA(cudaSetDevice(c->device));
+  PPS_CUDA(cudaStreamWaitEvent(c->stream, c->ready, 0));
+  const size_t w = sizeof(float) * (size_t)c->n;
+  return copy_rows_to_host(c->device, c->stream, reinterpret_cast<char*>(out), reinterpret_cast<const char*>(c->dev),
+                           w, w, (size_t)c->rows);
+}
+
+int pps_field_copy_destroy(pps_field_copy* c) {
+  if (!c) return PPS_OK;
+  cudaSetDevice(c->device);
+  if (c->dev) {
+    if (c->stream) cudaStreamWaitEvent(c->stream, c->ready, 0);
+    cudaFreeAsync(c->dev, c->stream);
+  }
+  if (c->stream) {
+    cudaStreamSynchronize(c->stream);
+    cudaStreamDestroy(c->stream);
+  }
+  if (c->ready) cudaEventDestroy(c->ready);
+  delete c;
   return PPS_OK;
 }
 

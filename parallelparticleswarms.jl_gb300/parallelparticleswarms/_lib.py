@@ -148,6 +148,9 @@ _SIGNATURES = {
     "pps_get_gbest": (ctypes.c_int, [_P, c_float_p, c_float_p, ctypes.POINTER(ctypes.c_int64)]),
     "pps_get_state": (ctypes.c_int, [_P, ctypes.c_int32, c_float_p]),
     "pps_set_state": (ctypes.c_int, [_P, ctypes.c_int32, c_float_p]),
+    "pps_field_copy_create": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.POINTER(_P)]),
+    "pps_field_copy_read": (ctypes.c_int, [_P, c_float_p]),
+    "pps_field_copy_destroy": (ctypes.c_int, [_P]),
     "pps_eval_objective": (ctypes.c_int, [ctypes.POINTER(Problem), ctypes.c_int64, c_float_p, c_float_p]),
     "pps_batch_create": (ctypes.c_int, [ctypes.POINTER(_P)]),
     "pps_batch_destroy": (ctypes.c_int, [_P]),

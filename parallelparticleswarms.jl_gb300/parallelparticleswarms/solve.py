@@ -30,7 +30,7 @@ class OptimizationSolution:
 
     u: np.ndarray
     objective: float
-    original: np.ndarray | None = None   # particle positions, (n, dim)
+    original: object = None              # particle positions, (n, dim): a DevicePositions
     stats: OptimizationStats = field(default_factory=OptimizationStats)
     retcode: str = "Default"             # the reference leaves ReturnCode.Default
     alg: object = None
@@ -122,9 +122,9 @@ def _pso_solve(cache: PSOCache, maxiters, w, wdamp, c1, c2) -> OptimizationSolut
     t1 = time.perf_counter()
     u, _, _ = sw.gbest()
     obj = float(evaluate(cache.prob, u))  # prob.f(gbest.position, prob.p), src/solve.jl:56
-    # sol.original: every particle's position, (n, dim), a view of the SoA copy
-    # (a transposed copy would be a strided 4 n dim byte shuffle on the host)
-    original = sw.positions().T
+    # sol.original: every particle's position, (n, dim), kept on the device
+    # as the reference's get_pos.(particles) is; copied to the host when read
+    original = sw.positions_on_device()
     return OptimizationSolution(u=u, objective=obj, original=original,
                                 stats=OptimizationStats(time=t1 - t0, device_ms=ms, iterations=int(maxiters)),
                                 alg=alg)

@@ -105,6 +105,10 @@ class Swarm:
         """(dim, n) SoA positions."""
         return self.get(_lib.FIELD_POSITION)
 
+    def positions_on_device(self) -> "DevicePositions":
+        """A device snapshot of the positions (the reference's sol.original)."""
+        return DevicePositions(self, _lib.FIELD_POSITION)
+
     def state(self) -> dict:
         return {
             "x": self.get(_lib.FIELD_POSITION),
@@ -118,3 +122,56 @@ class Swarm:
         inf = _lib.SwarmInfo()
         _lib.check(self._lib.pps_swarm_info_get(self._h, ctypes.byref(inf)))
         return inf
+
+
+class DevicePositions:
+    """Every particle's position as an (n, dim) array that stays in device memory
+    until it is read: the reference's sol.original = get_pos.(particles) is a new
+    device array (src/solve.jl:51-56).  ``np.asarray`` (or ``.numpy()``) copies it
+    to the host once; the swarm it came from may be re-run or closed meanwhile."""
+
+    def __init__(self, swarm: Swarm, field: int):
+        self._lib = swarm._lib
+        self._h = ctypes.c_void_p()
+        self.shape = (swarm.n, swarm.dim)
+        self.dtype = np.dtype(np.float32)
+        self._host = None
+        _lib.check(self._lib.pps_field_copy_create(swarm._h, int(field), ctypes.byref(self._h)))
+
+    def numpy(self) -> np.ndarray:
+        if self._host is None:
+            n, dim = self.shape
+            soa = np.empty((dim, n), np.float32)
+            _lib.check(self._lib.pps_field_copy_read(self._h, _lib.fptr(soa)))
+            self._host = soa.T  # (n, dim) view of the SoA copy
+            self.close()
+        return self._host
+
+    def __array__(self, dtype=None, copy=None):
+        a = self.numpy()
+        return a if dtype is None else a.astype(dtype)
+
+    def __len__(self) -> int:
+        return self.shape[0]
+
+    def __getitem__(self, idx):
+        return self.numpy()[idx]
+
+    @property
+    def ndim(self) -> int:
+        return 2
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) and self._h.value:
+            self._lib.pps_field_copy_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __repr__(self) -> str:
+        where = "host" if self._host is not None else "device"
+        return f"<DevicePositions {self.shape[0]} x {self.shape[1]} float32 on the {where}>"
