@@ -117,13 +117,27 @@ static inline float sinpi_poly(float b) {
 }
 static inline int is_odd_integer(float n) { return rintf(n * 0.5f) * 2.0f != n; }
 
+/* cos(2 pi x) = (-1)^n cos(pi a), y = 2x = n + r, n = rint(y), a = |r| <= 1/2,
+ * and cos(pi a) = (1/4 - a^2)(4 + z P(z)), z = a^2, P the degree-3 minimax
+ * fit of cospi_coefficients.py; 1/4 - a^2 is one fmaf. */
+static const float COS_P0 = -0x1.de9e60p+1f, COS_P1 = 0x1.472a8ap+0f, COS_P2 = -0x1.d47d94p-3f,
+                   COS_P3 = 0x1.8c391ap-6f;
 float orc_cos2pi(float x) {
-  float y = x + x;
-  float n = rintf(y);
-  float r = y - n;
-  float a = fabsf(r);
-  float c = (a <= 0.25f) ? cospi_poly(a) : sinpi_poly(0.5f - a);
-  return is_odd_integer(n) ? -c : c;
+  const float y = x + x;
+  const float n = rintf(y);
+  const uint32_t odd = is_odd_integer(n) ? 1u : 0u;
+  uint32_t cb;
+  const float a = fabsf(y - n);
+  const float z = a * a;
+  float q = fmaf(COS_P3, z, COS_P2);
+  q = fmaf(q, z, COS_P1);
+  q = fmaf(q, z, COS_P0);
+  const float p = fmaf(-a, a, 0.25f);
+  float c = fmaf(p, z * q, 4.0f * p);
+  memcpy(&cb, &c, 4);
+  cb ^= odd << 31;
+  memcpy(&c, &cb, 4);
+  return c;
 }
 
 float orc_sin2pi(float x) {

@@ -58,6 +58,16 @@ def _ulp(ref):
     return np.spacing(np.abs(ref).astype(np.float32)).astype(np.float64)
 
 
+def test_cos_polynomial_is_the_fit():
+    """The compiled polynomial of cos(2 pi x) is the minimax fit of
+    cospi_coefficients.py rounded to binary32, with relative error < 0.1 ulp."""
+    import cospi_coefficients as cc
+
+    fitted = [float(np.float32(v)) for v in cc.fit()]
+    assert fitted == [float.fromhex(h) for h in cc.COMPILED]
+    assert cc.max_rel_error([float.fromhex(h) for h in cc.COMPILED]) < 0.1 * 2.0 ** -24
+
+
 def test_cos_sin_exp_accuracy(orc):
     L = orc.load()
     rng = np.random.default_rng(0)
@@ -70,6 +80,9 @@ def test_cos_sin_exp_accuracy(orc):
     assert np.max(np.abs(c - rc)) < 1.2e-7 and np.max(np.abs(s - rs)) < 1.2e-7
     m = np.abs(rc) > 1e-3
     assert np.max(np.abs(c - rc)[m] / _ulp(rc[m])) <= 2.0
+    # the exact zeros of cos(2 pi x) at odd multiples of 1/4, signs of +-1 at the integers
+    q = np.array([L.orc_cos2pi(float(v)) for v in (0.25, 0.75, -1.25, 2.0, -3.0, 0.5, 1e7, 3e6 + 0.5)])
+    assert np.array_equal(q[:3], [0.0, 0.0, 0.0]) and np.array_equal(q[3:], [1.0, 1.0, -1.0, 1.0, -1.0])
     ex = np.concatenate([rng.uniform(-87, 88.7, 20000), np.linspace(-5, 5, 2001)]).astype(np.float32)
     e = np.array([L.orc_exp(float(x)) for x in ex])
     re = np.exp(ex.astype(np.float64))
