@@ -100,11 +100,14 @@ __global__ void __launch_bounds__(kSyncThreads) k_init(SwarmDev s, ObjParams op,
 // while the current tile runs: blocks on busier SMs or farther from the
 // memory take fewer tiles, and all finish within about one tile of each
 // other.  A particle's arithmetic does not depend on which block takes it.
+// Resident blocks: 2 for PPT = 4 (128 registers), 4 for PPT = 2 (64
+// registers, a 24-byte spill) and PPT = 1: with 32 warps per SM, two
+// particles per thread keep the most loads in flight.
 // CONS: the constrained path (PPT = 1 only): the cost adds calc_penalty with
 // iter = the 1-based particle index, as the reference's sync and queue-lock
 // kernels pass it (src/kernels.jl:77,151; handle_constraints adds 1, :28-31).
 template <int OBJ, int PPT, bool CONS = false>
-__global__ void __launch_bounds__(kSyncThreads, (PPT == 4 ? 2 : (PPT == 2 ? 3 : 4)))
+__global__ void __launch_bounds__(kSyncThreads, (PPT == 4 ? 2 : 4))
     k_sync_step(SwarmDev s, ObjParams op, PhiloxKeys keys, float c1, float c2, int from_position) {
   extern __shared__ float sm[];
   const int D = s.dim;
@@ -321,13 +324,15 @@ int launch_set_iter(pps_swarm* s, uint32_t t, float w, float wdamp) {
 }
 
 // particles per thread of the step kernel: PPS_SYNC_PPT=1|2|4 overrides the
-// default of 4 (every variant performs the same work and the same arithmetic;
-// measured on 2^20 x 100-D Rastrigin: 0.553 / 0.449 / 0.434 ms per iteration)
+// default of 2 (every variant performs the same work and the same arithmetic).
+// Measured on 2^20 x 100-D Rastrigin, ms per iteration (resident blocks):
+//   PPT 4: 0.387 (2), 0.401 (3, spills)   PPT 2: 0.393 (3), 0.378 (4), 0.422 (5)
+//   PPT 1: 0.464 (6), 0.481 (8)
 static int sync_ppt() {
   static int ppt = [] {
     const char* e = getenv("PPS_SYNC_PPT");
-    const int v = e ? atoi(e) : 4;
-    return (v == 1 || v == 2 || v == 4) ? v : 4;
+    const int v = e ? atoi(e) : 2;
+    return (v == 1 || v == 2 || v == 4) ? v : 2;
   }();
   return ppt;
 }
