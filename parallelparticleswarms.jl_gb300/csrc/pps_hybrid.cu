@@ -24,7 +24,8 @@
 // history (2 m D + 2 m floats per particle) lives in shared memory, particle
 // fastest (element (slot, d) of thread t at (slot D + d) blockDim + t, so a
 // warp's accesses hit 32 banks), with blocks of 32-128 threads sized to fit;
-// longer histories and the Broyden matrix (D^2) stay in thread-local memory.  The
+// longer histories stay in thread-local memory.  From 8 dims Broyden's inverse
+// Jacobian (D^2 floats) lives in shared memory the same way (blocks of 64).  The
 // argmin over the per-particle results (the reference's host findmin) runs on
 // the device with the 64-bit (cost, index) key.
 #include <cmath>
@@ -207,23 +208,44 @@ __device__ __forceinline__ void bounded_grad(const ObjParams& op, const float (&
   }
 }
 
-template <int OBJ, int MAXD>
-__global__ void __launch_bounds__(128) k_broyden(const float* __restrict__ X0, int64_t ld, int64_t n, ObjParams op,
-                                                 const float* __restrict__ lbp, const float* __restrict__ ubp,
-                                                 LocalOpts o, float* __restrict__ xout, float* __restrict__ fout,
-                                                 float* __restrict__ itout) {
+// Broyden's inverse Jacobian of one thread: in shared memory (SMEM; blocks of
+// kBroydenThreads, element (a, b) of thread t at (a MAXD + b) kBroydenThreads
+// + t, so every access is one load or store at a compile-time offset and a
+// warp's accesses hit 32 banks) or a register array (small MAXD)
+constexpr int kBroydenThreads = 64;
+template <int MAXD, bool SMEM>
+struct BroydenJ;
+template <int MAXD>
+struct BroydenJ<MAXD, true> {
+  float* base;
+  __device__ __forceinline__ explicit BroydenJ(float* sm) : base(sm + threadIdx.x) {}
+  __device__ __forceinline__ float& at(int a, int b) { return base[(a * MAXD + b) * kBroydenThreads]; }
+};
+template <int MAXD>
+struct BroydenJ<MAXD, false> {
+  float m[MAXD][MAXD];
+  __device__ __forceinline__ explicit BroydenJ(float*) {}
+  __device__ __forceinline__ float& at(int a, int b) { return m[a][b]; }
+};
+
+template <int OBJ, int MAXD, bool SMEM>
+__global__ void __launch_bounds__(SMEM ? kBroydenThreads : 128)
+    k_broyden(const float* __restrict__ X0, int64_t ld, int64_t n, ObjParams op, const float* __restrict__ lbp,
+              const float* __restrict__ ubp, LocalOpts o, float* __restrict__ xout, float* __restrict__ fout,
+              float* __restrict__ itout) {
+  extern __shared__ float jsm[];
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int D = op.dim;
   float lb[MAXD], ub[MAXD], x[MAXD], F[MAXD], xn[MAXD], Fn[MAXD], dx[MAXD], dF[MAXD], JdF[MAXD], dxJ[MAXD], step[MAXD];
-  float J[MAXD][MAXD];
+  BroydenJ<MAXD, SMEM> J(jsm);
   PPS_FOR_D(d) {
     lb[d] = lbp[d];
     ub[d] = ubp[d];
     x[d] = X0[(int64_t)d * ld + i];
   }
   PPS_FOR_D(a) {
-    PPS_FOR_D(b) J[a][b] = (a == b) ? 1.0f : 0.0f;
+    PPS_FOR_D(b) J.at(a, b) = (a == b) ? 1.0f : 0.0f;
   }
   bounded_grad<OBJ, MAXD>(op, x, lb, ub, F, D);
   float phi = dotv<MAXD>(F, F, D);
@@ -232,7 +254,7 @@ __global__ void __launch_bounds__(128) k_broyden(const float* __restrict__ X0, i
     if (!(__fsqrt_rn(phi) > o.gtol)) break;
     PPS_FOR_D(a) {
       float s = 0.0f;
-      PPS_FOR_D(b) s = __fadd_rn(s, __fmul_rn(J[a][b], F[b]));
+      PPS_FOR_D(b) s = __fadd_rn(s, __fmul_rn(J.at(a, b), F[b]));
       step[a] = -s;
     }
     float sc = 1.0f, phin = phi;
@@ -254,19 +276,19 @@ __global__ void __launch_bounds__(128) k_broyden(const float* __restrict__ X0, i
     }
     PPS_FOR_D(a) {
       float s = 0.0f;
-      PPS_FOR_D(b) s = __fadd_rn(s, __fmul_rn(J[a][b], dF[b]));
+      PPS_FOR_D(b) s = __fadd_rn(s, __fmul_rn(J.at(a, b), dF[b]));
       JdF[a] = s;
     }
     PPS_FOR_D(b) {
       float s = 0.0f;
-      PPS_FOR_D(a) s = __fadd_rn(s, __fmul_rn(dx[a], J[a][b]));
+      PPS_FOR_D(a) s = __fadd_rn(s, __fmul_rn(dx[a], J.at(a, b)));
       dxJ[b] = s;
     }
     const float den = dotv<MAXD>(dx, JdF, D);
     if (den != 0.0f && isfinite(den)) {
       PPS_FOR_D(a) {
         const float c = __fdiv_rn(__fsub_rn(dx[a], JdF[a]), den);
-        PPS_FOR_D(b) J[a][b] = __fadd_rn(J[a][b], __fmul_rn(c, dxJ[b]));
+        PPS_FOR_D(b) J.at(a, b) = __fadd_rn(J.at(a, b), __fmul_rn(c, dxJ[b]));
       }
     }
     PPS_FOR_D(d) {
@@ -389,13 +411,30 @@ static int launch_local_lbfgs(pps_swarm* s, const float* x0, const LocalOpts& o,
   return PPS_OK;
 }
 
+// Broyden: from 8 dims the inverse Jacobian (MAXD^2 floats a particle) lives
+// in shared memory, blocks of 64 (16 KB at MAXD 8, 25 KB at 10, 64 KB at 16)
+template <int OBJ, int MAXD>
+static int launch_local_broyden(pps_swarm* s, const float* x0, const LocalOpts& o, const LocalBufs& b) {
+  const int64_t n = s->dv.n;
+  if constexpr (MAXD >= 8) {
+    const size_t smem = sizeof(float) * MAXD * MAXD * kBroydenThreads;
+    if (smem > (48u << 10))
+      PPS_CUDA(cudaFuncSetAttribute(k_broyden<OBJ, MAXD, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const unsigned blocks = (unsigned)((n + kBroydenThreads - 1) / kBroydenThreads);
+    k_broyden<OBJ, MAXD, true><<<blocks, kBroydenThreads, smem, s->stream>>>(x0, s->dv.npad, n, s->op, s->dv.lb,
+                                                                             s->dv.ub, o, b.x, b.f, b.it);
+  } else {
+    const unsigned blocks = (unsigned)((n + 127) / 128);
+    k_broyden<OBJ, MAXD, false><<<blocks, 128, 0, s->stream>>>(x0, s->dv.npad, n, s->op, s->dv.lb, s->dv.ub, o,
+                                                                b.x, b.f, b.it);
+  }
+  return PPS_OK;
+}
+
 template <int OBJ, int MAXD>
 static int launch_local_t(pps_swarm* s, int kind, const float* x0, const LocalOpts& o, const LocalBufs& b) {
   if (kind == 0) return launch_local_lbfgs<OBJ, MAXD>(s, x0, o, b);
-  const int64_t n = s->dv.n;
-  const unsigned blocks = (unsigned)((n + 127) / 128);
-  k_broyden<OBJ, MAXD><<<blocks, 128, 0, s->stream>>>(x0, s->dv.npad, n, s->op, s->dv.lb, s->dv.ub, o, b.x, b.f, b.it);
-  return PPS_OK;
+  return launch_local_broyden<OBJ, MAXD>(s, x0, o, b);
 }
 
 template <int OBJ>
@@ -409,7 +448,8 @@ static int launch_local_obj(pps_swarm* s, int kind, const float* x0, const Local
     if (D <= 2) rc = launch_local_t<OBJ, 2>(s, kind, x0, o, b);
     else if (D <= 4) rc = launch_local_t<OBJ, 4>(s, kind, x0, o, b);
     else if (D <= 8) rc = launch_local_t<OBJ, 8>(s, kind, x0, o, b);
-    else if (D <= 10 && kind == 0) rc = launch_local_lbfgs<OBJ, 10>(s, x0, o, b);
+    else if (D <= 10) rc = kind == 0 ? launch_local_lbfgs<OBJ, 10>(s, x0, o, b)
+                                     : launch_local_broyden<OBJ, 10>(s, x0, o, b);
     else if (D <= 16) rc = launch_local_t<OBJ, 16>(s, kind, x0, o, b);
     else if (D <= 32) rc = launch_local_lbfgs<OBJ, 32>(s, x0, o, b);
     else rc = launch_local_lbfgs<OBJ, 64>(s, x0, o, b);
