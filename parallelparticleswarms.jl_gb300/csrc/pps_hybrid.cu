@@ -21,9 +21,9 @@
 //
 // GB300 design: one thread per particle; vectors of the particle's dimension
 // live in registers (compile-time bound MAXD).  Up to 16 dims the L-BFGS
-// history (2 m D + 2 m floats per particle) lives in shared memory, particle
-// fastest (element (slot, d) of thread t at (slot D + d) blockDim + t, so a
-// warp's accesses hit 32 banks), with blocks of 32-128 threads sized to fit;
+// history (2 m MAXD + 2 m floats per particle) lives in shared memory, particle
+// fastest (element (slot, d) of thread t at (slot MAXD + d) 64 + t in blocks of
+// 64, so a warp's accesses hit 32 banks at compile-time offsets);
 // longer histories stay in thread-local memory.  From 8 dims Broyden's inverse
 // Jacobian (D^2 floats) lives in shared memory the same way (blocks of 64).  The
 // argmin over the per-particle results (the reference's host findmin) runs on
@@ -55,18 +55,23 @@ __device__ __forceinline__ float dotv(const float (&a)[MAXD], const float (&b)[M
 // the history of one thread: in shared memory (SMEM) or thread-local arrays
 template <int MAXD, bool SMEM>
 struct LbfgsHistory;
+// blocks of the shared-memory variant: element e of a thread's history at
+// e * kLbfgsThreads + t, vectors of stride MAXD, so within a slot every access
+// is one load or store at a compile-time offset from the slot's row
+constexpr int kLbfgsThreads = 64;
 template <int MAXD>
 struct LbfgsHistory<MAXD, true> {
-  float* base;
-  int D, m, nt, t;
-  __device__ __forceinline__ LbfgsHistory(float* sm, int D_, int m_) : base(sm), D(D_), m(m_) {
-    nt = blockDim.x;
-    t = threadIdx.x;
+  float *s_, *y_, *rho_, *alpha_;
+  __device__ __forceinline__ LbfgsHistory(float* sm, int, int m) {
+    s_ = sm + threadIdx.x;
+    y_ = s_ + m * MAXD * kLbfgsThreads;
+    rho_ = y_ + m * MAXD * kLbfgsThreads;
+    alpha_ = rho_ + m * kLbfgsThreads;
   }
-  __device__ __forceinline__ float& S(int slot, int d) { return base[((size_t)slot * D + d) * nt + t]; }
-  __device__ __forceinline__ float& Y(int slot, int d) { return base[((size_t)(m + slot) * D + d) * nt + t]; }
-  __device__ __forceinline__ float& rho(int slot) { return base[((size_t)2 * m * D + slot) * nt + t]; }
-  __device__ __forceinline__ float& alpha(int slot) { return base[((size_t)2 * m * D + m + slot) * nt + t]; }
+  __device__ __forceinline__ float& S(int slot, int d) { return s_[(slot * MAXD + d) * kLbfgsThreads]; }
+  __device__ __forceinline__ float& Y(int slot, int d) { return y_[(slot * MAXD + d) * kLbfgsThreads]; }
+  __device__ __forceinline__ float& rho(int slot) { return rho_[slot * kLbfgsThreads]; }
+  __device__ __forceinline__ float& alpha(int slot) { return alpha_[slot * kLbfgsThreads]; }
 };
 template <int MAXD>
 struct LbfgsHistory<MAXD, false> {
@@ -79,10 +84,10 @@ struct LbfgsHistory<MAXD, false> {
 };
 
 // floats of shared memory one thread's L-BFGS history takes
-__host__ __device__ constexpr size_t lbfgs_hist_floats(int m, int D) { return (size_t)2 * m * D + 2 * (size_t)m; }
+__host__ __device__ constexpr size_t lbfgs_hist_floats(int m, int maxd) { return (size_t)2 * m * maxd + 2 * (size_t)m; }
 
 template <int OBJ, int MAXD, bool SMEM>
-__global__ void __launch_bounds__(128) k_lbfgs(const float* __restrict__ X0, int64_t ld, int64_t n, ObjParams op,
+__global__ void __launch_bounds__(SMEM ? kLbfgsThreads : 128) k_lbfgs(const float* __restrict__ X0, int64_t ld, int64_t n, ObjParams op,
                                                const float* __restrict__ lbp, const float* __restrict__ ubp,
                                                LocalOpts o, float* __restrict__ xout, float* __restrict__ fout,
                                                float* __restrict__ itout) {
@@ -111,7 +116,8 @@ __global__ void __launch_bounds__(128) k_lbfgs(const float* __restrict__ X0, int
     if (__fsqrt_rn(gn2) <= o.gtol) break;
     PPS_FOR_D(d) q[d] = pg[d];
     for (int j = 0; j < hist; ++j) {  // newest pair first
-      const int slot = (head - 1 - j + m) % m;
+      int slot = head - 1 - j;  // (head - 1 - j) mod m, head < m, j < m
+      if (slot < 0) slot += m;
       float sq_ = 0.0f;
       PPS_FOR_D(d) sq_ = __fadd_rn(sq_, __fmul_rn(H.S(slot, d), q[d]));
       const float a = __fmul_rn(H.rho(slot), sq_);
@@ -120,7 +126,7 @@ __global__ void __launch_bounds__(128) k_lbfgs(const float* __restrict__ X0, int
     }
     float gamma = 1.0f;
     if (hist > 0) {
-      const int nw = (head - 1 + m) % m;
+      const int nw = head > 0 ? head - 1 : m - 1;
       float sy = 0.0f, yy = 0.0f;
       PPS_FOR_D(d) sy = __fadd_rn(sy, __fmul_rn(H.S(nw, d), H.Y(nw, d)));
       PPS_FOR_D(d) yy = __fadd_rn(yy, __fmul_rn(H.Y(nw, d), H.Y(nw, d)));
@@ -128,7 +134,8 @@ __global__ void __launch_bounds__(128) k_lbfgs(const float* __restrict__ X0, int
     }
     PPS_FOR_D(d) q[d] = __fmul_rn(gamma, q[d]);
     for (int j = hist - 1; j >= 0; --j) {  // oldest pair first
-      const int slot = (head - 1 - j + m) % m;
+      int slot = head - 1 - j;
+      if (slot < 0) slot += m;
       float yq = 0.0f;
       PPS_FOR_D(d) yq = __fadd_rn(yq, __fmul_rn(H.Y(slot, d), q[d]));
       const float b = __fmul_rn(H.rho(slot), yq);
@@ -176,7 +183,7 @@ __global__ void __launch_bounds__(128) k_lbfgs(const float* __restrict__ X0, int
         H.Y(head, d) = yv[d];
       }
       H.rho(head) = __fdiv_rn(1.0f, sy);
-      head = (head + 1) % m;
+      head = head + 1 == m ? 0 : head + 1;
       if (hist < m) ++hist;
     }
     PPS_FOR_D(d) {
@@ -388,21 +395,18 @@ static LocalBufs local_bufs(pps_swarm* s) {
   return lb;
 }
 
-// L-BFGS: up to 16 dims the history lives in shared memory (blocks of 32-128
-// threads, at most 96 KB: two or more blocks per SM; 16 slots x 16 dims fit
-// 32 threads); above 16 dims in thread-local memory
+// L-BFGS: up to 16 dims the history lives in shared memory, blocks of 64
+// (m = 10: 56 KB at MAXD 10; the largest, m = 16 at MAXD 16: 136 KB, one
+// block per SM); above 16 dims in thread-local memory
 template <int OBJ, int MAXD>
 static int launch_local_lbfgs(pps_swarm* s, const float* x0, const LocalOpts& o, const LocalBufs& b) {
   const int64_t n = s->dv.n;
   if constexpr (MAXD <= 16) {
-    const size_t per_thread = sizeof(float) * lbfgs_hist_floats(o.history, s->dv.dim);
-    int nt = 128;
-    while (nt > 32 && per_thread * nt > (96u << 10)) nt /= 2;
-    const size_t smem = per_thread * nt;
+    const size_t smem = sizeof(float) * lbfgs_hist_floats(o.history, MAXD) * kLbfgsThreads;
     PPS_CUDA(cudaFuncSetAttribute(k_lbfgs<OBJ, MAXD, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    const unsigned blocks = (unsigned)((n + nt - 1) / nt);
-    k_lbfgs<OBJ, MAXD, true><<<blocks, nt, smem, s->stream>>>(x0, s->dv.npad, n, s->op, s->dv.lb, s->dv.ub, o, b.x,
-                                                               b.f, b.it);
+    const unsigned blocks = (unsigned)((n + kLbfgsThreads - 1) / kLbfgsThreads);
+    k_lbfgs<OBJ, MAXD, true><<<blocks, kLbfgsThreads, smem, s->stream>>>(x0, s->dv.npad, n, s->op, s->dv.lb,
+                                                                          s->dv.ub, o, b.x, b.f, b.it);
   } else {
     const unsigned blocks = (unsigned)((n + 127) / 128);
     k_lbfgs<OBJ, MAXD, false><<<blocks, 128, 0, s->stream>>>(x0, s->dv.npad, n, s->op, s->dv.lb, s->dv.ub, o, b.x,
