@@ -275,6 +275,15 @@ PPS_API int pps_get_gbest(pps_swarm* s, float* u, float* cost, int64_t* idx);
 /* copy a state field to / from host memory (SoA, particle fastest) */
 PPS_API int pps_get_state(pps_swarm* s, int32_t field, float* out);
 PPS_API int pps_set_state(pps_swarm* s, int32_t field, const float* in);
+/* The whole swarm in the reference's particle records, SPSOParticle{position, velocity,
+ * cost, best_position, best_cost} (src/ParallelParticleSwarms.jl:34-44): 3 dim + 2 floats
+ * per particle.  PPS_LAYOUT_AOS: n records one after another (a Julia caller wraps the
+ * buffer as Vector{SPSOParticle}); PPS_LAYOUT_SOA: the five fields one after another, each
+ * particle-fastest.  Setting the particles makes the global best the argmin of best_cost,
+ * as init does (src/init.jl:49-51). */
+enum { PPS_LAYOUT_SOA = 0, PPS_LAYOUT_AOS = 1 };
+PPS_API int pps_get_particles(pps_swarm* s, int32_t layout, float* out);
+PPS_API int pps_set_particles(pps_swarm* s, int32_t layout, const float* in);
 /* A device snapshot of a state field: sol.original = get_pos.(particles), which the
  * reference keeps on the device as a new array (src/solve.jl:51-56).  The swarm may be
  * re-run or destroyed while the snapshot lives; read copies it to host memory in

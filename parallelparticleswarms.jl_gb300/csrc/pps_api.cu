@@ -587,8 +587,8 @@ static HostStage& host_stage(int device) {
 
 // rows x row_bytes from dev (pitch src_pitch bytes) to the contiguous host
 // array out, on stream
-static int copy_rows_to_host(int device, cudaStream_t stream, char* out, const char* dev, size_t src_pitch,
-                             size_t row_bytes, size_t rows) {
+int copy_rows_to_host(int device, cudaStream_t stream, char* out, const char* dev, size_t src_pitch,
+                      size_t row_bytes, size_t rows) {
   const size_t total = row_bytes * rows;
   if (total < ((size_t)4 << 20) || device < 0 || device >= 64) {
     PPS_CUDA(cudaMemcpy2DAsync(out, row_bytes, dev, src_pitch, row_bytes, rows, cudaMemcpyDeviceToHost, stream));

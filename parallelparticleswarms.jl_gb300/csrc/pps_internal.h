@@ -105,6 +105,12 @@ int swarm_enqueue_init(pps_swarm* s);
 int swarm_enqueue_run(pps_swarm* s, int32_t maxiters, float w, float wdamp, float c1, float c2);
 // gbest (dim floats), its cost and index into mail, then done = 1, visible to the host
 int launch_publish_result(pps_swarm* s, float* mail, int* done);
+// rows x row_bytes of device memory (pitch src_pitch) to a pageable host
+// array through pinned staging buffers, on stream (pps_api.cu)
+int copy_rows_to_host(int device, cudaStream_t stream, char* out, const char* dev, size_t src_pitch,
+                      size_t row_bytes, size_t rows);
+// argmin of pcost into the global best (pps_noalloc.cu)
+int launch_select_gbest(pps_swarm* s);
 // user objectives compiled at run time (pps_user.cu)
 bool is_user(int objective);
 int user_prepare(pps_swarm* s);  // loads the kernels and sizes the grid; call outside stream capture

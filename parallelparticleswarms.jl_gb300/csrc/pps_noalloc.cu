@@ -103,6 +103,14 @@ __global__ void k_noalloc_select(SwarmDev s, int from_position) {
   }
 }
 
+// the global best of a swarm whose personal bests were just set (key and
+// count are canonical between calls: every step kernel resets them)
+int launch_select_gbest(pps_swarm* s) {
+  k_noalloc_select<<<s->sm_count, 256, 0, s->stream>>>(s->dv, (s->flags & PPS_FLAG_GBEST_FROM_POSITION) ? 1 : 0);
+  PPS_CUDA(cudaGetLastError());
+  return PPS_OK;
+}
+
 static bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
 
 }  // namespace pps

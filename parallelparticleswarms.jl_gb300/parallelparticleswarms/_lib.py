@@ -23,6 +23,7 @@ SAMPLER_AUTO, SAMPLER_UNIFORM, SAMPLER_UNBOUNDED, SAMPLER_LHS = 0, 1, 2, 3
 FLAG_GBEST_FROM_POSITION = 1
 FIELD_POSITION, FIELD_VELOCITY, FIELD_PBEST, FIELD_PCOST, FIELD_COST = range(5)
 FIELD_LOCAL_X, FIELD_LOCAL_F, FIELD_LOCAL_ITERS = 5, 6, 7
+LAYOUT_SOA, LAYOUT_AOS = 0, 1
 
 c_float_p = ctypes.POINTER(ctypes.c_float)
 
@@ -148,6 +149,8 @@ _SIGNATURES = {
     "pps_get_gbest": (ctypes.c_int, [_P, c_float_p, c_float_p, ctypes.POINTER(ctypes.c_int64)]),
     "pps_get_state": (ctypes.c_int, [_P, ctypes.c_int32, c_float_p]),
     "pps_set_state": (ctypes.c_int, [_P, ctypes.c_int32, c_float_p]),
+    "pps_get_particles": (ctypes.c_int, [_P, ctypes.c_int32, c_float_p]),
+    "pps_set_particles": (ctypes.c_int, [_P, ctypes.c_int32, c_float_p]),
     "pps_field_copy_create": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.POINTER(_P)]),
     "pps_field_copy_read": (ctypes.c_int, [_P, c_float_p]),
     "pps_field_copy_destroy": (ctypes.c_int, [_P]),

@@ -105,6 +105,30 @@ class Swarm:
         """(dim, n) SoA positions."""
         return self.get(_lib.FIELD_POSITION)
 
+    def record_dtype(self) -> np.dtype:
+        """SPSOParticle{position, velocity, cost, best_position, best_cost}
+        (src/ParallelParticleSwarms.jl:34-44) as a numpy record."""
+        D = self.dim
+        return np.dtype([("position", np.float32, (D,)), ("velocity", np.float32, (D,)), ("cost", np.float32),
+                         ("best_position", np.float32, (D,)), ("best_cost", np.float32)])
+
+    def particles(self) -> np.ndarray:
+        """Every particle as the reference's record (an (n,) structured array)."""
+        out = np.empty(self.n, self.record_dtype())
+        _lib.check(self._lib.pps_get_particles(self._h, _lib.LAYOUT_AOS,
+                                               out.ctypes.data_as(_lib.c_float_p)))
+        return out
+
+    def set_particles(self, records) -> None:
+        """Replace every particle by the given records (structured array or
+        (n, 3 dim + 2) floats); the global best becomes the argmin of best_cost."""
+        arr = np.ascontiguousarray(records)
+        if arr.dtype != self.record_dtype():
+            arr = np.ascontiguousarray(np.asarray(records, np.float32).reshape(self.n, 3 * self.dim + 2))
+        if arr.nbytes != self.n * (3 * self.dim + 2) * 4:
+            raise _lib.ArgumentError(_lib.EINVAL, f"expected {self.n} records of {3 * self.dim + 2} floats")
+        _lib.check(self._lib.pps_set_particles(self._h, _lib.LAYOUT_AOS, arr.ctypes.data_as(_lib.c_float_p)))
+
     def positions_on_device(self) -> "DevicePositions":
         """A device snapshot of the positions (the reference's sol.original)."""
         return DevicePositions(self, _lib.FIELD_POSITION)

@@ -98,3 +98,48 @@ def test_overflowing_costs_match_oracle(pps, orc):
             sw.sync_run(1)
             ref.sync_run(1)
             assert_state_equal(sw, ref, f"iteration {it + 1}")
+
+
+def test_original_is_a_device_snapshot(pps):
+    """sol.original stays on the device as a snapshot (the reference's
+    get_pos.(particles) is a new device array, src/solve.jl:51-56): it keeps
+    the positions of the solve while the swarm runs on or is closed, and reads
+    to the host as (n, dim)."""
+    D, n = 5, 3000
+    prob = pps.OptimizationProblem(pps.rastrigin, np.zeros(D, np.float32), [10.0],
+                                   lb=np.full(D, -5.12, np.float32), ub=np.full(D, 5.12, np.float32))
+    cache = pps.init(prob, pps.ParallelSyncPSOKernel(n), seed=3)
+    sol = pps.solve_(cache, maxiters=20)
+    want = cache.swarm.positions().T.copy()
+    assert sol.original.shape == (n, D) and "device" in repr(sol.original)
+    pps.solve_(cache, maxiters=30)          # the swarm moves on
+    cache.swarm.close()                     # and goes away
+    got = np.asarray(sol.original)
+    assert got.shape == (n, D) and np.array_equal(got, want)
+    assert "host" in repr(sol.original) and np.array_equal(sol.original[7], want[7])
+
+
+@pytest.mark.parametrize("D,n", [(3, 1000), (100, 777), (1000, 33)])
+def test_particle_records_round_trip(pps, D, n):
+    """pps_get_particles / pps_set_particles in the reference's SPSOParticle
+    layout (src/ParallelParticleSwarms.jl:34-44): the records hold the SoA
+    state field by field, and setting them reproduces that state and its
+    global best (the argmin of best_cost)."""
+    lb, ub = np.full(D, -5.12, np.float32), np.full(D, 5.12, np.float32)
+    prob = pps.OptimizationProblem(pps.rastrigin, np.zeros(D, np.float32), [10.0], lb=lb, ub=ub)
+    with pps.Swarm(prob, n, seed=2) as a, pps.Swarm(prob, n, seed=9) as b:
+        a.init()
+        a.sync_run(10)
+        rec = a.particles()
+        st = a.state()
+        assert np.array_equal(rec["position"], st["x"].T) and np.array_equal(rec["velocity"], st["v"].T)
+        assert np.array_equal(rec["best_position"], st["pbest"].T)
+        assert np.array_equal(rec["cost"], st["cost"]) and np.array_equal(rec["best_cost"], st["pcost"])
+        b.init()
+        b.set_particles(rec)
+        sb = b.state()
+        for k in ("x", "v", "pbest", "pcost", "cost"):
+            assert np.array_equal(sb[k], st[k]), k
+        ua, ca, ia = a.gbest()
+        ub_, cb, ib = b.gbest()
+        assert ia == ib and np.float32(ca) == np.float32(cb) and np.array_equal(ua, ub_)
