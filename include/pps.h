@@ -314,9 +314,10 @@ PPS_API int pps_eval_objective(const pps_problem* prob, int64_t npoints, const f
  * same id.  Errors: PPS_EINVAL with the compiler log (pps_last_error) when
  * the source does not compile, PPS_ENOTSUP without NVRTC.
  * A user objective runs through pps_swarm_create / pps_swarm_init,
- * pps_sync_run, pps_queue_run, pps_eval_objective and the server (as a swarm
- * of its own), constraints included; pps_async_run, the HybridPSO local
- * stage (no gradient), batches and pps_sync_run_noalloc return PPS_ENOTSUP.
+ * pps_sync_run, pps_queue_run, pps_async_run, pps_eval_objective and the
+ * server (as a swarm of its own), constraints included (not with
+ * pps_async_run); the HybridPSO local stage (no gradient), batches and
+ * pps_sync_run_noalloc return PPS_ENOTSUP.
  * The library cannot bound the running time of the user's code: a function
  * that does not return hangs the run. */
 PPS_API int pps_objective_register(const char* source, int32_t* objective);

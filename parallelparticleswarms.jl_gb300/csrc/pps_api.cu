@@ -520,12 +520,11 @@ int pps_async_run(pps_swarm* s, int32_t maxiters, float w, float wdamp, float c1
     return set_error(PPS_ENOTSUP, "the MLP objective runs synchronously (tensor-core evaluation); use pps_sync_run");
   if (s->dv.ncons > 0)
     return set_error(PPS_ENOTSUP, "constrained problems run with pps_sync_run / pps_queue_run");
-  if (is_user(s->objective))
-    return set_error(PPS_ENOTSUP, "user objectives run with pps_sync_run / pps_queue_run");
   if ((rc = launch_set_iter(s, s->t, w, wdamp))) return rc;
   PPS_CUDA(cudaEventRecord(s->ev0, s->stream));
   int lanes = 0;
-  if ((rc = launch_async(s, maxiters, c1, c2, &lanes))) return rc;
+  if ((rc = is_user(s->objective) ? launch_user_async(s, maxiters, c1, c2) : launch_async(s, maxiters, c1, c2, &lanes)))
+    return rc;
   PPS_CUDA(cudaEventRecord(s->ev1, s->stream));
   if ((rc = finish_timing(s, device_ms))) return rc;
   PPS_CUDA(cudaStreamSynchronize(s->stream));

@@ -116,6 +116,7 @@ bool is_user(int objective);
 int user_prepare(pps_swarm* s);  // loads the kernels and sizes the grid; call outside stream capture
 int launch_user_init(pps_swarm* s, int sampler, const float* u0_dev);
 int launch_user_step(pps_swarm* s, float c1, float c2);
+int launch_user_async(pps_swarm* s, int iters, float c1, float c2);
 int launch_user_eval(const ObjParams& op, const ObjData& od, int objective, const float* x, int64_t npts,
                      int64_t stride, float* f, cudaStream_t stream);
 int launch_mlp_points(const float* data_dev, int64_t ndata, const uint8_t* a_dev, const float* x, int64_t npts,

@@ -96,6 +96,7 @@ struct UserObjective {
   cudaKernel_t k_init = nullptr, k_eval = nullptr;
   cudaKernel_t k_step[3] = {};  // 1, 2, 4 particles per thread
   cudaKernel_t k_step_cons = nullptr;
+  cudaKernel_t k_async = nullptr;
 };
 
 constexpr int kMaxUser = 4096;
@@ -179,6 +180,7 @@ int ensure_loaded(UserObjective* u) {
   PPS_CUDA(cudaLibraryGetKernel(&u->k_step[1], u->lib, "pps_user_step2"));
   PPS_CUDA(cudaLibraryGetKernel(&u->k_step[2], u->lib, "pps_user_step4"));
   PPS_CUDA(cudaLibraryGetKernel(&u->k_step_cons, u->lib, "pps_user_step_cons"));
+  PPS_CUDA(cudaLibraryGetKernel(&u->k_async, u->lib, "pps_user_async"));
   PPS_CUDA(cudaLibraryGetKernel(&u->k_eval, u->lib, "pps_user_eval"));
   u->loaded.store(true, std::memory_order_release);
   return PPS_OK;
@@ -258,6 +260,27 @@ int launch_user_step(pps_swarm* s, float c1, float c2) {
   void* args[] = {&s->dv, &s->op, &data, &ndata, &keys, &c1, &c2, &from_pos};
   PPS_CUDA(cudaLaunchKernel(s->user_step_kernel, dim3((unsigned)s->user_grid), dim3(kUserThreads), args,
                             3 * sizeof(float) * (size_t)s->dv.dim, s->stream));
+  return PPS_OK;
+}
+
+int launch_user_async(pps_swarm* s, int iters, float c1, float c2) {
+  int rc;
+  UserObjective* u = loaded_or_error(s->objective, &rc);
+  if (!u) return rc;
+  const size_t smem = 3 * sizeof(float) * (size_t)s->dv.dim;
+  int per_sm = 0;
+  PPS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, reinterpret_cast<const void*>(u->k_async),
+                                                         kUserThreads, smem));
+  if (per_sm < 1) return set_error(PPS_EINVAL, "the objective's async kernel cannot be resident (dim %d)", s->dv.dim);
+  const int64_t blocks = (s->dv.n + kUserThreads - 1) / kUserThreads;
+  const int64_t resident = (int64_t)per_sm * s->sm_count;
+  const unsigned grid = (unsigned)(blocks < resident ? blocks : resident);
+  PhiloxKeys keys = philox_round_keys(s->seed);
+  const float* data = s->od.data;
+  long long ndata = (long long)s->od.ndata;
+  void* args[] = {&s->dv, &s->op, &data, &ndata, &keys, &iters, &c1, &c2};
+  PPS_CUDA(cudaLaunchKernel(reinterpret_cast<const void*>(u->k_async), dim3(grid), dim3(kUserThreads), args, smem,
+                            s->stream));
   return PPS_OK;
 }
 

@@ -258,6 +258,77 @@ extern "C" __global__ void __launch_bounds__(pps::kUserThreads, PPS_USER_MB2)
   pps::user_step<4, false>(s, op, data, ndata, keys, c1, c2, from_position);
 }
 
+// ParallelPSOKernel(global_update = false) for a user objective: the whole run
+// in one launch (src/kernels.jl:196-225, src/lowerlevel_solve.jl:95-121).
+// Each particle runs every iteration against a private global best that
+// starts as the swarm's and becomes its own personal best once that beats the
+// starting cost (:215-218); w is damped in the kernel (:219); personal-best
+// copies are immediate.  The state stays in HBM (one thread per particle,
+// grid-stride), as the objective reads the position back; the run ends with
+// the argmin over the personal bests (:119-120).
+extern "C" __global__ void __launch_bounds__(pps::kUserThreads, PPS_USER_MB4)
+    pps_user_async(pps::SwarmDev s, pps::ObjParams op, const float* data, long long ndata, pps::PhiloxKeys keys,
+                   int iters, float c1, float c2) {
+  using namespace pps;
+  extern __shared__ float sm[];
+  __shared__ float sp[8];
+  const int D = s.dim;
+  float* sg = sm;
+  float* slb = sm + D;
+  float* sub = sm + 2 * D;
+  IterState* st = s.st;
+  const uint32_t t0 = st->t;
+  const float w0 = st->w, wdamp = st->wdamp, gcost0 = st->gcost;
+  for (int d = threadIdx.x; d < D; d += blockDim.x) {
+    sg[d] = s.g[d];
+    slb[d] = s.lb[d];
+    sub[d] = s.ub[d];
+  }
+  user_params(sp, op);
+  __syncthreads();
+  const int64_t npad = s.npad, n = s.n;
+  float* X = s.X;  // not restrict: the objective reads back what this thread stores
+  float* V = s.V;
+  float* P = s.P;
+  unsigned long long best = ~0ull;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    bool own = false;
+    float w = w0;
+    float pc = s.pcost[i];
+    for (int it = 0; it < iters; ++it) {
+      const uint32_t t = t0 + (uint32_t)it;
+      for (int j = 0; j < D; j += 2) {
+        const Rand4 r = philox4x32_10((uint32_t)i, (uint32_t)(j >> 1), t, kTagStep, keys);
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const int d = j + h;
+          if (d >= D) break;
+          const int64_t o = (int64_t)d * npad + i;
+          const float x = X[o], p = P[o];
+          const float gd = own ? p : sg[d];
+          const float v = velocity(x, V[o], p, gd, w, c1, c2, u01(h ? r.c : r.a), u01(h ? r.d : r.b));
+          X[o] = clamp_lb_ub(__fadd_rn(x, v), slb[d], sub[d]);
+          V[o] = v;
+        }
+      }
+      const float c = pps_objective(pps_point{X + i, npad}, D, sp, data, ndata);
+      s.cost[i] = c;
+      if (c < pc) {  // strict <, src/kernels.jl:21-24
+        pc = c;
+        for (int d = 0; d < D; ++d) P[(int64_t)d * npad + i] = X[(int64_t)d * npad + i];
+      }
+      if (pc < gcost0) own = true;
+      w = __fmul_rn(w, wdamp);
+    }
+    s.pcost[i] = pc;
+    const unsigned long long key = argmin_key(pc, (uint32_t)i);
+    best = key < best ? key : best;
+  }
+  float wf = w0;  // the inertia after the run, for every block alike
+  for (int it = 0; it < iters; ++it) wf = __fmul_rn(wf, wdamp);
+  if (publish_block_min(best, st)) finish_iteration(s, false, t0 + (uint32_t)iters, wf);
+}
+
 // f[i] = objective at point i, coordinates x[d * stride + i]
 extern "C" __global__ void __launch_bounds__(pps::kUserThreads)
     pps_user_eval(pps::ObjParams op, const float* data, long long ndata, const float* x, long long npts,

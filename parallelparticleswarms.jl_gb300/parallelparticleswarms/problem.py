@@ -64,8 +64,8 @@ def cuda_objective(source: str, name: str = "user", default_params=()) -> Object
     and evaluation kernels; ``pps_exp``, ``pps_cos2pi`` and ``pps_sin2pi`` are
     the library's exp(x), cos(2 pi x) and sin(2 pi x).  Compile errors raise
     ArgumentError with the compiler's log.  Runs with ParallelSyncPSOKernel,
-    ParallelPSOKernel(global_update=True), ``evaluate`` and ``Server``;
-    the async kernel, HybridPSO and batches do not take it.
+    ParallelPSOKernel (both global_update modes), ``evaluate`` and
+    ``Server``; HybridPSO (no gradient) and batches do not take it.
     """
     oid = ctypes.c_int32()
     _lib.check(_lib.load().pps_objective_register(source.encode(), ctypes.byref(oid)))

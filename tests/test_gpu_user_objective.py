@@ -152,13 +152,31 @@ def test_user_solve_and_reference_threshold(pps):
     assert sol.original.shape == (2000, D)
 
 
+@pytest.mark.parametrize("src,D,n,iters", [(us.RASTRIGIN, 20, 3000, 50), (us.POLYFIT, 3, 777, 80),
+                                           (us.GRIEWANK, 1, 1, 10)])
+def test_user_async_matches_oracle(pps, orc, src, D, n, iters):
+    """ParallelPSOKernel(global_update=false) on a user objective: the
+    in-kernel iteration loop with each particle's private global best, bit
+    for bit against the oracle's async run, then a sync run after it."""
+    data = _polyfit_data() if src == us.POLYFIT else None
+    lo, hi = (-600.0, 600.0) if src == us.GRIEWANK else (-5.12, 5.12)
+    sw, ref = _pair(pps, orc, src, D, n, lo, hi, [10.0] if src == us.RASTRIGIN else [], seed=6, data=data)
+    with sw:
+        sw.init()
+        ref.init()
+        sw.async_run(iters, w=0.9, wdamp=0.995)
+        ref.async_run(iters, w=0.9, wdamp=0.995)
+        assert_state_equal(sw, ref, "async")
+        sw.sync_run(5)
+        ref.sync_run(5)
+        assert_state_equal(sw, ref, "sync after async")
+
+
 def test_user_refused_paths(pps):
     prob = pps.OptimizationProblem(pps.cuda_objective(us.ROSENBROCK), np.zeros(3, np.float32), [1.0, 100.0],
                                    lb=np.full(3, -1, np.float32), ub=np.full(3, 10, np.float32))
     with pps.Swarm(prob, 256, seed=1) as sw:
         sw.init()
-        with pytest.raises(pps.PPSError):
-            sw.async_run(3)
         sw.sync_run(3)
         with pytest.raises(pps.PPSError):
             sw.local_stage("lbfgs")
