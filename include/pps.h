@@ -316,8 +316,12 @@ PPS_API int pps_eval_objective(const pps_problem* prob, int64_t npoints, const f
  * A user objective runs through pps_swarm_create / pps_swarm_init,
  * pps_sync_run, pps_queue_run, pps_async_run, pps_eval_objective and the
  * server (as a swarm of its own), constraints included (not with
- * pps_async_run); the HybridPSO local stage (no gradient), batches and
- * pps_sync_run_noalloc return PPS_ENOTSUP.
+ * pps_async_run).  The HybridPSO local stage (pps_hybrid_lbfgs / _bfgs) needs
+ * a gradient: a source that defines PPS_HAS_GRADIENT also defines
+ *   PPS_DEVICE float pps_gradient(pps_point x, int dim, const float* p,
+ *                                 const float* data, long long ndata, float* g)
+ * (g = grad f(x), returns f(x)); without it, and for batches and
+ * pps_sync_run_noalloc, the call returns PPS_ENOTSUP.
  * The library cannot bound the running time of the user's code: a function
  * that does not return hangs the run. */
 PPS_API int pps_objective_register(const char* source, int32_t* objective);

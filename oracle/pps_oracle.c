@@ -377,6 +377,8 @@ float orc_objective(const orc_problem* prob, const float* x, int64_t stride, int
 
 float orc_objective_grad(const orc_problem* prob, const float* x, float* g) {
   const int D = prob->dim;
+  if (prob->objective == ORC_OBJ_USER && prob->user_grad)
+    return prob->user_grad(x, D, prob->params, prob->user_data, (long long)prob->user_ndata, g);
   float f = orc_objective(prob, x, 1, 1);
   switch (prob->objective) {
     case ORC_OBJ_SPHERE:

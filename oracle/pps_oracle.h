@@ -73,6 +73,9 @@ enum {
 
 /* f(x, dim, p, data, ndata) of a user objective, x contiguous */
 typedef float (*orc_user_fn)(const float* x, int dim, const float* p, const float* data, long long ndata);
+/* its gradient (a source that defines PPS_HAS_GRADIENT): g = grad f(x), returns f(x) */
+typedef float (*orc_user_grad_fn)(const float* x, int dim, const float* p, const float* data, long long ndata,
+                                  float* g);
 
 struct orc_ode_fit;
 
@@ -96,6 +99,7 @@ typedef struct orc_problem {
   orc_user_fn user_fn;
   const float* user_data;
   int64_t user_ndata;
+  orc_user_grad_fn user_grad;  /* NULL: no gradient */
 } orc_problem;
 
 /* structure-of-arrays swarm state: x[d*n + i] */

@@ -34,6 +34,7 @@ class OdeFit(ctypes.Structure):
 
 
 USER_FN = ctypes.CFUNCTYPE(ctypes.c_float, _fp, ctypes.c_int, _fp, _fp, ctypes.c_longlong)
+USER_GRAD = ctypes.CFUNCTYPE(ctypes.c_float, _fp, ctypes.c_int, _fp, _fp, ctypes.c_longlong, _fp)
 OBJ_USER = 256
 
 
@@ -42,7 +43,8 @@ class Problem(ctypes.Structure):
                 ("u0", _fp), ("params", ctypes.c_float * 8), ("nparams", ctypes.c_int32),
                 ("ode", ctypes.POINTER(OdeFit)), ("mlp_data", _fp), ("mlp_samples", ctypes.c_int32),
                 ("ncons", ctypes.c_int32), ("cons", _fp),
-                ("user_fn", USER_FN), ("user_data", _fp), ("user_ndata", ctypes.c_int64)]
+                ("user_fn", USER_FN), ("user_data", _fp), ("user_ndata", ctypes.c_int64),
+                ("user_grad", USER_GRAD)]
 
 
 class SwarmC(ctypes.Structure):
@@ -173,6 +175,8 @@ class OracleProblem:
         if user is not None:
             self.c.objective = OBJ_USER
             self.c.user_fn = user.fn
+            if user.grad is not None:
+                self.c.user_grad = user.grad
             if user_data is not None:
                 self.user_data = np.ascontiguousarray(np.asarray(user_data, np.float32).reshape(-1))
                 self.c.user_data = fp(self.user_data)
@@ -347,6 +351,8 @@ class UserObjective:
         self.source = source
         self.lib = ctypes.CDLL(str(so))
         self.fn = USER_FN(ctypes.cast(self.lib.pps_objective, ctypes.c_void_p).value)
+        g = getattr(self.lib, "pps_gradient", None) if "PPS_HAS_GRADIENT" in source else None
+        self.grad = USER_GRAD(ctypes.cast(g, ctypes.c_void_p).value) if g is not None else None
 
     def __call__(self, x, params=(), data=None) -> float:
         x = np.ascontiguousarray(np.asarray(x, np.float32))

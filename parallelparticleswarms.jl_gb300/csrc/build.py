@@ -37,8 +37,8 @@ NVCC_FLAGS = ARCH + [
 
 # device headers that NVRTC compiles with the source of a user objective
 # (pps_user.cu): embedded into the library as string literals
-RTC_HEADERS = ["pps_device.cuh", "pps_state.cuh", "pps_publish.cuh", "pps_vec.cuh", "pps_user_prelude.cuh",
-               "pps_user_kernels.cuh"]
+RTC_HEADERS = ["pps_device.cuh", "pps_state.cuh", "pps_publish.cuh", "pps_vec.cuh", "pps_objgrad.cuh", "pps_local.cuh",
+               "pps_user_prelude.cuh", "pps_user_kernels.cuh"]
 RTC_INC = OBJ_DIR / "pps_rtc_sources.inc"
 
 

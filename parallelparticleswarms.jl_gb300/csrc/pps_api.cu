@@ -208,6 +208,8 @@ static int swarm_setup(pps_swarm* s, const pps_problem* prob, int64_t n, uint64_
   s->dv.ncons = prob->ncons > 0 ? prob->ncons : 0;
   s->dv.cons = s->dv.ncons ? reinterpret_cast<const float*>(b + L.oCons) : nullptr;
   s->op = make_params(prob);
+  s->op.data = s->od.data;  // the local optimisers of a user objective read it through the parameters
+  s->op.ndata = s->od.ndata;
   s->objective = prob->objective;
   s->seed = seed;
   s->flags = flags;

@@ -341,6 +341,8 @@ struct ObjParams {
   float p[8];
   int np;
   int dim;
+  const float* data;  // a user objective's data buffer on the device (NULL otherwise)
+  long long ndata;
 };
 __device__ __forceinline__ float prm(const ObjParams& o, int k, float dflt) {
   return (k < o.np) ? o.p[k] : dflt;

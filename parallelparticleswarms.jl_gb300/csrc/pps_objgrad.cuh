@@ -15,8 +15,15 @@ namespace pps {
 // arrays of the caller stay in registers.
 #define PPS_FOR_D(d) _Pragma("unroll") for (int d = 0; d < MAXD; ++d) if (d < D)
 
+// a user objective (compiled by NVRTC with its source): f and, when the source
+// defines PPS_HAS_GRADIENT, pps_gradient(x, dim, p, data, ndata, g) returning f
+constexpr int kUserObjective = 255;
+
 template <int OBJ, int MAXD>
 __device__ __forceinline__ float obj_value(const ObjParams& op, const float (&x)[MAXD], int D) {
+#ifdef PPS_USER_SOURCE
+  if constexpr (OBJ == kUserObjective) return pps_objective(pps_point{x, 1}, D, op.p, op.data, op.ndata);
+#endif
   Acc<OBJ> acc;
   PPS_FOR_D(d) acc.add(op, d, x[d]);
   return finalize<OBJ>(op, acc.s1, acc.s2);
@@ -25,6 +32,9 @@ __device__ __forceinline__ float obj_value(const ObjParams& op, const float (&x)
 // f(x) and grad f(x) into g[0..D)
 template <int OBJ, int MAXD>
 __device__ __forceinline__ float obj_grad(const ObjParams& op, const float (&x)[MAXD], float (&g)[MAXD], int D) {
+#if defined(PPS_USER_SOURCE) && defined(PPS_HAS_GRADIENT)
+  if constexpr (OBJ == kUserObjective) return pps_gradient(pps_point{x, 1}, D, op.p, op.data, op.ndata, g);
+#endif
   const float f = obj_value<OBJ, MAXD>(op, x, D);
   if constexpr (OBJ == kSphere) {
     PPS_FOR_D(d) g[d] = __fmul_rn(2.0f, x[d]);

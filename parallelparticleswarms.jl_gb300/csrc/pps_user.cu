@@ -28,6 +28,7 @@
 #include <vector>
 
 #include "pps_internal.h"
+#include "pps_local.cuh"
 #include "pps_rtc_sources.inc"  // kRtcHeaderNames[], kRtcHeaderTexts[], kRtcHeaderCount (generated)
 
 namespace pps {
@@ -97,6 +98,8 @@ struct UserObjective {
   cudaKernel_t k_step[3] = {};  // 1, 2, 4 particles per thread
   cudaKernel_t k_step_cons = nullptr;
   cudaKernel_t k_async = nullptr;
+  // HybridPSO's local stage, when the source has a gradient (else NULL)
+  cudaKernel_t k_lbfgs16 = nullptr, k_lbfgs64 = nullptr, k_broyden16 = nullptr;
 };
 
 constexpr int kMaxUser = 4096;
@@ -181,6 +184,13 @@ int ensure_loaded(UserObjective* u) {
   PPS_CUDA(cudaLibraryGetKernel(&u->k_step[2], u->lib, "pps_user_step4"));
   PPS_CUDA(cudaLibraryGetKernel(&u->k_step_cons, u->lib, "pps_user_step_cons"));
   PPS_CUDA(cudaLibraryGetKernel(&u->k_async, u->lib, "pps_user_async"));
+  if (cudaLibraryGetKernel(&u->k_lbfgs16, u->lib, "pps_user_lbfgs16") != cudaSuccess) {
+    cudaGetLastError();  // no gradient in the source: no local stage
+    u->k_lbfgs16 = nullptr;
+  } else {
+    PPS_CUDA(cudaLibraryGetKernel(&u->k_lbfgs64, u->lib, "pps_user_lbfgs64"));
+    PPS_CUDA(cudaLibraryGetKernel(&u->k_broyden16, u->lib, "pps_user_broyden16"));
+  }
   PPS_CUDA(cudaLibraryGetKernel(&u->k_eval, u->lib, "pps_user_eval"));
   u->loaded.store(true, std::memory_order_release);
   return PPS_OK;
@@ -281,6 +291,44 @@ int launch_user_async(pps_swarm* s, int iters, float c1, float c2) {
   void* args[] = {&s->dv, &s->op, &data, &ndata, &keys, &iters, &c1, &c2};
   PPS_CUDA(cudaLaunchKernel(reinterpret_cast<const void*>(u->k_async), dim3(grid), dim3(kUserThreads), args, smem,
                             s->stream));
+  return PPS_OK;
+}
+
+int launch_user_local(pps_swarm* s, int kind, const float* x0, const LocalOpts& o, float* xout, float* fout,
+                      float* itout) {
+  int rc;
+  UserObjective* u = loaded_or_error(s->objective, &rc);
+  if (!u) return rc;
+  if (!u->k_lbfgs16)
+    return set_error(PPS_ENOTSUP, "the HybridPSO local stage needs a gradient: define PPS_HAS_GRADIENT and "
+                                  "pps_gradient in the objective's source");
+  const int D = s->dv.dim;
+  const int64_t n = s->dv.n;
+  int64_t ld = s->dv.npad, nn = n;
+  ObjParams op = s->op;
+  LocalOpts oo = o;
+  const float *lb = s->dv.lb, *ub = s->dv.ub;
+  void* args[] = {&x0, &ld, &nn, &op, &lb, &ub, &oo, &xout, &fout, &itout};
+  const void* k;
+  int threads;
+  size_t smem = 0;
+  if (kind == 1) {
+    if (D > 16) return set_error(PPS_ENOTSUP, "the Broyden local stage supports dim <= 16 (got %d)", D);
+    k = reinterpret_cast<const void*>(u->k_broyden16);
+    threads = kBroydenThreads;
+    smem = sizeof(float) * 16 * 16 * kBroydenThreads;
+  } else if (D <= 16) {
+    k = reinterpret_cast<const void*>(u->k_lbfgs16);
+    threads = kLbfgsThreads;
+    smem = sizeof(float) * lbfgs_hist_floats(o.history, 16) * kLbfgsThreads;
+  } else {
+    k = reinterpret_cast<const void*>(u->k_lbfgs64);
+    threads = 128;
+  }
+  if (smem > ((size_t)48 << 10))
+    PPS_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const unsigned blocks = (unsigned)((n + threads - 1) / threads);
+  PPS_CUDA(cudaLaunchKernel(k, dim3(blocks), dim3(threads), args, smem, s->stream));
   return PPS_OK;
 }
 

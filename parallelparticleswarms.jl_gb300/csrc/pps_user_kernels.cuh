@@ -340,3 +340,28 @@ extern "C" __global__ void __launch_bounds__(pps::kUserThreads)
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < npts) f[i] = pps_objective(pps_point{x + i, stride}, op.dim, sp, data, ndata);
 }
+
+#ifdef PPS_HAS_GRADIENT
+// HybridPSO's local stage on a user objective with a gradient: L-BFGS with the
+// history in shared memory (dim <= 16) or thread-local memory (dim <= 64),
+// Broyden with the inverse Jacobian in shared memory (dim <= 16)
+#include "pps_local.cuh"
+
+extern "C" __global__ void __launch_bounds__(pps::kLbfgsThreads)
+    pps_user_lbfgs16(const float* X0, int64_t ld, int64_t n, pps::ObjParams op, const float* lbp, const float* ubp,
+                     pps::LocalOpts o, float* xout, float* fout, float* itout) {
+  pps::lbfgs_run<pps::kUserObjective, 16, true>(X0, ld, n, op, lbp, ubp, o, xout, fout, itout);
+}
+
+extern "C" __global__ void __launch_bounds__(128)
+    pps_user_lbfgs64(const float* X0, int64_t ld, int64_t n, pps::ObjParams op, const float* lbp, const float* ubp,
+                     pps::LocalOpts o, float* xout, float* fout, float* itout) {
+  pps::lbfgs_run<pps::kUserObjective, 64, false>(X0, ld, n, op, lbp, ubp, o, xout, fout, itout);
+}
+
+extern "C" __global__ void __launch_bounds__(pps::kBroydenThreads)
+    pps_user_broyden16(const float* X0, int64_t ld, int64_t n, pps::ObjParams op, const float* lbp, const float* ubp,
+                       pps::LocalOpts o, float* xout, float* fout, float* itout) {
+  pps::broyden_run<pps::kUserObjective, 16, true>(X0, ld, n, op, lbp, ubp, o, xout, fout, itout);
+}
+#endif

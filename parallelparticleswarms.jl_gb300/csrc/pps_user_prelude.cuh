@@ -16,8 +16,18 @@
 // pps_exp, pps_cos2pi and pps_sin2pi are the library's own exp(x),
 // cos(2 pi x) and sin(2 pi x) (the functions of the registered objectives);
 // CUDA's math functions (expf, cosf, ...) are available as well.
+//
+// HybridPSO's local stage needs a gradient: a source that defines
+// PPS_HAS_GRADIENT also defines
+//
+//   PPS_DEVICE float pps_gradient(pps_point x, int dim, const float* p,
+//                                 const float* data, long long ndata, float* g)
+//
+// writing grad f(x) to g[0..dim) and returning f(x).
 #pragma once
 #include "pps_device.cuh"
+
+#define PPS_USER_SOURCE 1
 
 // coordinate accessor over a strided column of the SoA state: one particle
 // per thread, so a warp's x[d] is one coalesced 128-byte line

@@ -65,7 +65,10 @@ def cuda_objective(source: str, name: str = "user", default_params=()) -> Object
     the library's exp(x), cos(2 pi x) and sin(2 pi x).  Compile errors raise
     ArgumentError with the compiler's log.  Runs with ParallelSyncPSOKernel,
     ParallelPSOKernel (both global_update modes), ``evaluate`` and
-    ``Server``; HybridPSO (no gradient) and batches do not take it.
+    ``Server``; with HybridPSO when the source also defines PPS_HAS_GRADIENT
+    and ``PPS_DEVICE float pps_gradient(pps_point x, int dim, const float* p,
+    const float* data, long long ndata, float* g)`` (g = grad f, returns f);
+    batches do not take it.
     """
     oid = ctypes.c_int32()
     _lib.check(_lib.load().pps_objective_register(source.encode(), ctypes.byref(oid)))

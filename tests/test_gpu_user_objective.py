@@ -196,3 +196,31 @@ def test_user_request_served_alone(pps):
         sw.sync_run(70)
         au, ac, ai = sw.gbest()
     assert i == ai and np.float32(c) == np.float32(ac) and np.array_equal(u, au)
+
+
+@pytest.mark.parametrize("kind,D,n", [("lbfgs", 10, 4096), ("bfgs", 10, 2048), ("lbfgs", 24, 777)])
+def test_user_hybrid_local_stage(pps, orc, kind, D, n):
+    """HybridPSO's local stage on a user objective with a gradient
+    (PPS_HAS_GRADIENT): the NVRTC-compiled L-BFGS / Broyden kernels reproduce
+    the registered Rosenbrock's local optima, values and iteration counts bit
+    for bit (dim 24 takes the thread-local L-BFGS history), and the oracle's."""
+    from parallelparticleswarms import _lib
+    lb, ub = _box(D, -5.0, 5.0)
+    reg = pps.OptimizationProblem(pps.rosenbrock, np.zeros(D, np.float32), [1.0, 100.0], lb=lb, ub=ub)
+    usr = reg.remake(f=pps.cuda_objective(us.ROSENBROCK_GRAD))
+    with pps.Swarm(reg, n, seed=3) as a, pps.Swarm(usr, n, seed=3) as b:
+        a.init()
+        b.init()
+        a.sync_run(40)
+        b.sync_run(40)
+        ra = a.local_stage(kind, maxiters=60)
+        rb = b.local_stage(kind, maxiters=60)
+        assert ra[2] == rb[2] and np.float32(ra[1]) == np.float32(rb[1]) and np.array_equal(ra[0], rb[0])
+        for field in (_lib.FIELD_LOCAL_X, _lib.FIELD_LOCAL_F, _lib.FIELD_LOCAL_ITERS):
+            assert np.array_equal(a.get(field), b.get(field), equal_nan=True), field
+        start = b.get(_lib.FIELD_PBEST if kind == "lbfgs" else _lib.FIELD_POSITION)
+        got_x, got_it = b.get(_lib.FIELD_LOCAL_X), b.get(_lib.FIELD_LOCAL_ITERS)
+    oprob = orc.OracleProblem(0, D, lb, ub, params=[1.0, 100.0], user=orc.UserObjective(us.ROSENBROCK_GRAD))
+    xo, fo, its = orc.lbfgs(oprob, start, maxiters=60, broyden=(kind == "bfgs"))
+    assert np.array_equal(xo, got_x) and np.array_equal(got_it.reshape(-1).astype(np.int32), its)
+

@@ -72,3 +72,23 @@ GRIEWANK = HEAD + """ {
   return (s / 4000.0f - q) + 1.0f;
 }
 """
+
+# Rosenbrock with its gradient, both spelled as the registered objective's
+# (pps_objgrad.cuh): the HybridPSO local stage on it is the registered one
+ROSENBROCK_GRAD = "#define PPS_HAS_GRADIENT 1\n" + ROSENBROCK + """
+PPS_DEVICE float pps_gradient(pps_point x, int dim, const float* p, const float* data, long long ndata, float* g) {
+  for (int d = 0; d < dim; ++d) {
+    float gd = 0.0f;
+    if (d < dim - 1) {
+      const float t = x[d + 1] - x[d] * x[d];
+      gd = ((-4.0f * p[1]) * x[d]) * t - 2.0f * (p[0] - x[d]);
+    }
+    if (d > 0) {
+      const float t = x[d] - x[d - 1] * x[d - 1];
+      gd = gd + (2.0f * p[1]) * t;
+    }
+    g[d] = gd;
+  }
+  return pps_objective(x, dim, p, data, ndata);
+}
+"""
