@@ -27,7 +27,10 @@
 // longer histories stay in thread-local memory.  From 8 dims Broyden's inverse
 // Jacobian (D^2 floats) lives in shared memory the same way (blocks of 64).  The
 // argmin over the per-particle results (the reference's host findmin) runs on
-// the device with the 64-bit (cost, index) key.
+// the device with the 64-bit (cost, index) key.  The optimisers' device code
+// is in pps_local.cuh, which NVRTC also compiles for a user objective with a
+// gradient (pps_user.cu); this file holds the registered objectives' kernels
+// and the launch logic.
 #include <cmath>
 
 #include "pps_internal.h"

@@ -74,3 +74,23 @@ def test_register_reports_compile_errors():
     assert "objective(1)" in str(e.value) and "undefined_name" in str(e.value)
     with pytest.raises(pkg.ArgumentError):
         pkg.cuda_objective("")
+
+
+def test_register_with_gradient_compiles_the_local_stage():
+    """A source with PPS_HAS_GRADIENT compiles the HybridPSO local-stage
+    kernels too (the shared device code of pps_local.cuh under NVRTC), and
+    the oracle's C build of it has the gradient of the registered Rosenbrock."""
+    pkg = pytest.importorskip("parallelparticleswarms")
+    f = _register(pkg, us.ROSENBROCK_GRAD)
+    assert f.id >= 256
+
+
+def test_user_gradient_on_the_oracle(orc):
+    user = orc.UserObjective(us.ROSENBROCK_GRAD)
+    assert user.grad is not None and orc.UserObjective(us.ROSENBROCK).grad is None
+    reg = orc.OracleProblem(1, 12, params=[1.0, 100.0])
+    usr = orc.OracleProblem(0, 12, params=[1.0, 100.0], user=user)
+    for x in _points(12, 200, -3.0, 3.0, seed=5):
+        fa, ga = reg.objective_grad(x)
+        fb, gb = usr.objective_grad(x)
+        assert np.float32(fa) == np.float32(fb) and np.array_equal(ga, gb)
