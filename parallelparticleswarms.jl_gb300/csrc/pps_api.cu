@@ -744,6 +744,8 @@ int pps_eval_objective(const pps_problem* prob, int64_t npoints, const float* x,
   if (rc) return rc;
   if (npoints < 0 || (npoints > 0 && (!x || !f))) return set_error(PPS_EINVAL, "bad points");
   if (npoints == 0) return PPS_OK;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return set_error(PPS_ENODEV, "no CUDA device");
   const int D = prob->dim;
   float* dx = nullptr;
   cudaStream_t st = nullptr;
