@@ -9,8 +9,8 @@ from .algorithms import (BFGS, CUDA, GPUUniformSampler, GPUUnboundedSampler, Hyb
 from .problem import (REGISTRY, Objective, OptimizationProblem, ackley, beale, booth, boundary_quadratic,
                       cuda_objective, evaluate, fitzhugh_nagumo_fit, himmelblau, lotka_volterra_fit,
                       mlp_regression, quadratic, quadratic_constraint, rastrigin, rosenbrock, shifted_sphere, sphere)
-from .solve import (HybridPSOCache, OptimizationSolution, OptimizationStats, PSOCache, init, reinit_, solve,
-                    solve_)
+from .solve import (HybridPSOCache, OptimizationSolution, OptimizationStats, PSOCache, init, pso_solve, reinit_,
+                    solve, solve_)
 from .swarm import Swarm
 from .batch import Batch
 from .serve import Server
@@ -18,7 +18,8 @@ from . import mlp, ode
 
 __all__ = [
     "ParallelPSOKernel", "ParallelSyncPSOKernel", "PSOAlgorithm", "HybridPSO", "SimpleLBFGS", "BFGS",
-    "OptimizationProblem", "solve", "solve_", "init", "reinit_", "GPUUniformSampler", "GPUUnboundedSampler",
+    "OptimizationProblem", "solve", "solve_", "init", "reinit_", "pso_solve", "GPUUniformSampler",
+    "GPUUnboundedSampler",
     "LatinHypercubeSample",
     "PSOCache", "HybridPSOCache", "OptimizationSolution", "OptimizationStats", "Swarm", "PPSError",
     "ArgumentError", "evaluate", "Objective", "REGISTRY", "sphere", "rosenbrock", "rastrigin", "ackley",

@@ -20,7 +20,23 @@ def _check_backend(backend):
 
 
 class PSOAlgorithm:
-    """Abstract supertype of the particle-swarm algorithms (src/algorithms.jl:1-15)."""
+    """Abstract supertype of the particle-swarm algorithms (src/algorithms.jl:1-15).
+
+    To add an algorithm of one's own, subclass it and implement ``pso_solve``
+    (src/algorithms.jl:17-28); ``solve(prob, alg)`` then runs it and builds the
+    solution as the reference does for such algorithms (src/solve.jl:69-87).
+    The engine's own kernels (``ParallelSyncPSOKernel``, ``ParallelPSOKernel``,
+    ``HybridPSO``) do not go through this hook.
+    """
+
+    def pso_solve(self, prob, *, maxiters: int, **kwargs):
+        """Run the algorithm's loop; return ``(global_best, particles, solve_time)``.
+
+        ``global_best`` exposes ``position`` and ``cost`` (attributes or mapping
+        keys), each entry of ``particles`` exposes ``position``, and
+        ``solve_time`` is in seconds.
+        """
+        raise NotImplementedError(f"{type(self).__name__} does not implement pso_solve(prob, *, maxiters, **kwargs)")
 
 
 @dataclass

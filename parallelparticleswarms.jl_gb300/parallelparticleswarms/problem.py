@@ -8,11 +8,17 @@ their default parameters.  They are markers, not Python callables: objective
 values are always computed on the GPU (``evaluate`` below).  Any other
 objective is given as CUDA C source (``cuda_objective``), which the library
 compiles at run time into its own kernels.
+
+A plain Python callable ``f(x, p)`` is accepted only for algorithms that bring
+their own loop through the ``PSOAlgorithm`` / ``pso_solve`` interface
+(src/algorithms.jl:1-28, src/solve.jl:69-87); every device path (the swarm
+kernels, batches, the server, ``evaluate``) refuses it with ``ArgumentError``.
 """
 from __future__ import annotations
 
 import ctypes
 from dataclasses import dataclass, field
+from typing import Callable
 
 import numpy as np
 
@@ -109,7 +115,7 @@ class OptimizationProblem:
     enter the cost through the reference's penalty (src/utils.jl:320-372).
     """
 
-    f: Objective
+    f: Objective | Callable
     u0: np.ndarray
     p: np.ndarray | None = None
     lb: np.ndarray | None = None
@@ -121,12 +127,12 @@ class OptimizationProblem:
     def __post_init__(self):
         if isinstance(self.f, str):
             self.f = REGISTRY[self.f]
-        if not isinstance(self.f, Objective):
-            raise _lib.ArgumentError(_lib.EINVAL, "f must be a registered objective (see problem.REGISTRY) or a "
-                                                  "cuda_objective; the engine has no path for Python callables")
+        if not isinstance(self.f, Objective) and not callable(self.f):
+            raise _lib.ArgumentError(_lib.EINVAL, "f must be a registered objective (see problem.REGISTRY), a "
+                                                  "cuda_objective, or a callable f(x, p) for a pso_solve algorithm")
         self.u0 = _f32(self.u0)
         self.dim = int(self.u0.size)
-        if self.p is None:
+        if self.p is None and self.on_device:
             self.p = np.asarray(self.f.default_params, dtype=np.float32) if self.f.default_params else None
         self.p = _f32(self.p)
         self.lb = _f32(self.lb, self.dim) if self.lb is not None else None
@@ -138,6 +144,16 @@ class OptimizationProblem:
                 raise _lib.ArgumentError(_lib.EINVAL, f"cons rows have 1 + 2 dim = {1 + 2 * self.dim} values")
             self.cons = c.reshape(-1, 1 + 2 * self.dim)
 
+    @property
+    def on_device(self) -> bool:
+        """True when f is one of the engine's objectives (registered or CUDA source)."""
+        return isinstance(self.f, Objective)
+
+    def require_device_objective(self) -> None:
+        if not self.on_device:
+            raise _lib.ArgumentError(_lib.EINVAL, "a Python callable f(x, p) cannot run on the device: use a "
+                                                  "registered objective or cuda_objective(source)")
+
     def remake(self, **kw) -> "OptimizationProblem":
         args = dict(f=self.f, u0=self.u0, p=self.p, lb=self.lb, ub=self.ub, data=self.data, cons=self.cons)
         args.update(kw)
@@ -145,6 +161,7 @@ class OptimizationProblem:
 
     def to_c(self) -> _lib.Problem:
         """C struct view; the numpy buffers stay referenced by this problem."""
+        self.require_device_objective()
         pr = _lib.Problem()
         pr.objective = self.f.id
         pr.dim = self.dim
@@ -162,6 +179,7 @@ class OptimizationProblem:
 
 def evaluate(prob: OptimizationProblem, x) -> np.ndarray:
     """Objective values at points ``x`` (shape (npoints, dim) or (dim,)) on the GPU."""
+    prob.require_device_objective()
     x = np.asarray(x, dtype=np.float32)
     single = x.ndim == 1
     pts = x.reshape(-1, prob.dim)

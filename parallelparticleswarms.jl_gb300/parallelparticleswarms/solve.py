@@ -11,8 +11,7 @@ import numpy as np
 
 from . import _lib
 from .algorithms import (BFGS, GPUUniformSampler, GPUUnboundedSampler, HybridPSO, LatinHypercubeSample,
-                         ParallelPSOKernel,
-                         ParallelSyncPSOKernel, SimpleLBFGS)
+                         ParallelPSOKernel, ParallelSyncPSOKernel, PSOAlgorithm, SimpleLBFGS)
 from .problem import OptimizationProblem, evaluate
 from .swarm import C1_DEFAULT, C2_DEFAULT, W_DEFAULT, WDAMP_DEFAULT, Swarm
 
@@ -92,6 +91,7 @@ def _resolve_sampler(prob: OptimizationProblem, sampler):
 
 def init(prob: OptimizationProblem, alg, *, sampler=None, seed: int = 0):
     """Allocate the device swarm and sample the initial particles."""
+    prob.require_device_objective()
     if isinstance(alg, HybridPSO):
         return HybridPSOCache(init(prob, alg.pso, sampler=sampler, seed=seed), alg)
     if not isinstance(alg, (ParallelSyncPSOKernel, ParallelPSOKernel)):
@@ -141,9 +141,51 @@ def solve_(cache, *, maxiters: int = 100, w: float = W_DEFAULT, wdamp: float = W
     return _pso_solve(cache, maxiters, w, wdamp, c1, c2)
 
 
+def _field(obj, name):
+    return obj[name] if isinstance(obj, dict) else getattr(obj, name)
+
+
+def check_init_bounds(prob: OptimizationProblem):
+    """(lb, ub) with missing bounds as -Inf / +Inf (src/utils.jl:310-318)."""
+    lb = np.full(prob.dim, -np.inf, np.float32) if prob.lb is None else prob.lb
+    ub = np.full(prob.dim, np.inf, np.float32) if prob.ub is None else prob.ub
+    return lb, ub
+
+
+def pso_solve(prob: OptimizationProblem, alg: PSOAlgorithm, *, maxiters: int = 100, **kwargs):
+    """pso_solve(prob, alg; maxiters, kwargs...) (src/algorithms.jl:17-28): the algorithm's own loop."""
+    return alg.pso_solve(prob, maxiters=maxiters, **kwargs)
+
+
+def _plugin_solve(prob: OptimizationProblem, alg: PSOAlgorithm, maxiters: int, kwargs) -> OptimizationSolution:
+    """solve(prob, ::PSOAlgorithm) (src/solve.jl:69-87): bounds made explicit, the
+    algorithm's pso_solve, then u = gbest.position, objective = f(u, p),
+    original = every particle's position, stats.time = the reported time."""
+    lb, ub = check_init_bounds(prob)
+    prob = prob.remake(lb=lb, ub=ub)
+    gbest, particles, solve_time = pso_solve(prob, alg, maxiters=maxiters, **kwargs)
+    u = np.asarray(_field(gbest, "position"))
+    if prob.on_device:
+        objective = float(evaluate(prob, u))
+    else:
+        objective = prob.f(u, prob.p)
+    original = [_field(q, "position") for q in particles]
+    return OptimizationSolution(u=u, objective=objective, original=original,
+                                stats=OptimizationStats(time=float(solve_time), iterations=int(maxiters)), alg=alg)
+
+
 def solve(prob: OptimizationProblem, alg, *, maxiters: int = 100, sampler=None, seed: int = 0,
           **kwargs) -> OptimizationSolution:
-    """solve(prob, alg; maxiters) = solve!(init(prob, alg)) (src/solve.jl:61-67)."""
+    """solve(prob, alg; maxiters) = solve!(init(prob, alg)) (src/solve.jl:61-67).
+
+    Any other ``PSOAlgorithm`` runs through its ``pso_solve`` (src/solve.jl:69-87);
+    ``sampler`` and ``seed`` reach it as keywords when they are given."""
+    if isinstance(alg, PSOAlgorithm) and not isinstance(alg, (ParallelSyncPSOKernel, ParallelPSOKernel, HybridPSO)):
+        if sampler is not None:
+            kwargs["sampler"] = sampler
+        if seed:
+            kwargs["seed"] = seed
+        return _plugin_solve(prob, alg, maxiters, kwargs)
     cache = init(prob, alg, sampler=sampler, seed=seed)
     try:
         return solve_(cache, maxiters=maxiters, **kwargs)
@@ -151,5 +193,5 @@ def solve(prob: OptimizationProblem, alg, *, maxiters: int = 100, sampler=None, 
         (cache.pso_cache if isinstance(cache, HybridPSOCache) else cache).swarm.close()
 
 
-__all__ = ["init", "solve", "solve_", "reinit_", "PSOCache", "HybridPSOCache", "OptimizationSolution",
-           "OptimizationStats", "SimpleLBFGS", "BFGS"]
+__all__ = ["init", "solve", "solve_", "reinit_", "pso_solve", "check_init_bounds", "PSOCache", "HybridPSOCache",
+           "OptimizationSolution", "OptimizationStats", "SimpleLBFGS", "BFGS"]

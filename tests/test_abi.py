@@ -91,5 +91,16 @@ def test_python_layer_rejects_other_backends(pps):
         pps.ParallelSyncPSOKernel(10, backend="cpu")
     with pytest.raises(pps.ArgumentError):
         pps.ParallelPSOKernel(0)
+    # a Python callable is a problem only for a pso_solve algorithm: every
+    # device path refuses it before touching the device
+    prob = pps.OptimizationProblem(lambda x, p: 0.0, np.zeros(2))
+    with pytest.raises(pps.ArgumentError, match="callable"):
+        pps.init(prob, pps.ParallelSyncPSOKernel(10))
+    with pytest.raises(pps.ArgumentError, match="callable"):
+        pps.solve(prob, pps.HybridPSO(pps.ParallelPSOKernel(10)))
+    with pytest.raises(pps.ArgumentError, match="callable"):
+        pps.evaluate(prob, np.zeros(2))
+    with pytest.raises(pps.ArgumentError, match="callable"):
+        pps.Swarm(prob, 10)
     with pytest.raises(pps.ArgumentError):
-        pps.OptimizationProblem(lambda x, p: 0.0, np.zeros(2))
+        pps.OptimizationProblem(42, np.zeros(2))
