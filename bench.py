@@ -287,6 +287,22 @@ USER_RASTRIGIN = """PPS_DEVICE float pps_objective(pps_point x, int dim, const f
 }
 """
 
+# the same with the fold the step kernel evaluates as each coordinate moves
+USER_RASTRIGIN_STREAM = "#define PPS_HAS_STREAM 1\n" + USER_RASTRIGIN + """
+typedef struct { float s; } pps_stream;
+PPS_DEVICE void pps_stream_start(pps_stream* st, int dim, const float* p, const float* data, long long ndata) {
+  st->s = 0.0f;
+}
+PPS_DEVICE void pps_stream_add(pps_stream* st, int d, float v, int dim, const float* p, const float* data,
+                               long long ndata) {
+  st->s = st->s + (v * v - p[0] * pps_cos2pi(v));
+}
+PPS_DEVICE float pps_stream_finish(const pps_stream* st, int dim, const float* p, const float* data,
+                                   long long ndata) {
+  return p[0] * (float)dim + st->s;
+}
+"""
+
 
 def run_user(pps, n: int = N_PARTICLES, iters: int = ITERS) -> dict:
     """C2 Rastrigin (n x 100-D, bounds [-5.12, 5.12]) with f given as CUDA C
@@ -296,21 +312,37 @@ def run_user(pps, n: int = N_PARTICLES, iters: int = ITERS) -> dict:
     reg = pps.OptimizationProblem(pps.rastrigin, np.zeros(DIM, np.float32), [10.0], lb=lb, ub=ub)
     usr = reg.remake(f=pps.cuda_objective(USER_RASTRIGIN, "rastrigin_source"))
     res = {}
-    for key, prob in (("registered", reg), ("source", usr)):
+
+    def measure(key, prob):
         with pps.Swarm(prob, n, seed=2) as sw:
             sw.init()
             sw.sync_run(10)  # warm (the first use loads the compiled library)
             sw.init()
             ms = sw.sync_run(iters)
             res[key] = (ms, sw.gbest())
+
+    def same(key):
+        return bool(np.array_equal(res[key][1][0], res["registered"][1][0])
+                    and res[key][1][2] == res["registered"][1][2])
+
+    measure("registered", reg)
+    measure("source", usr)
     ms = res["source"][0]
-    return {"workload": f"{n} particles x {DIM}-D Rastrigin, {iters} sync iterations, f as CUDA C source "
-                        "(NVRTC, 2 particles per thread)",
-            "device_ms": ms, "particle_iters_per_s": n * iters / (ms / 1e3),
-            "hbm_gbs": n * BYTES_PER_PARTICLE_ITER / (ms / iters / 1e3) / 1e9,
-            "registered_device_ms": res["registered"][0], "vs_registered": res["registered"][0] / ms,
-            "same_result_as_registered": bool(np.array_equal(res["source"][1][0], res["registered"][1][0])
-                                              and res["source"][1][2] == res["registered"][1][2])}
+    out = {"workload": f"{n} particles x {DIM}-D Rastrigin, {iters} sync iterations, f as CUDA C source "
+                       "(NVRTC, 2 particles per thread)",
+           "device_ms": ms, "particle_iters_per_s": n * iters / (ms / 1e3),
+           "hbm_gbs": n * BYTES_PER_PARTICLE_ITER / (ms / iters / 1e3) / 1e9,
+           "registered_device_ms": res["registered"][0], "vs_registered": res["registered"][0] / ms,
+           "same_result_as_registered": same("source")}
+    try:  # the same source with PPS_HAS_STREAM: the step folds f in registers
+        measure("stream", reg.remake(f=pps.cuda_objective(USER_RASTRIGIN_STREAM, "rastrigin_stream")))
+        sms = res["stream"][0]
+        out["stream"] = {"device_ms": sms, "particle_iters_per_s": n * iters / (sms / 1e3),
+                         "hbm_gbs": n * BYTES_PER_PARTICLE_ITER / (sms / iters / 1e3) / 1e9,
+                         "vs_registered": res["registered"][0] / sms, "same_result_as_registered": same("stream")}
+    except pps.PPSError as e:
+        out["stream"] = {"error": str(e)}
+    return out
 
 
 def run_configs(pps) -> dict:

@@ -322,6 +322,12 @@ PPS_API int pps_eval_objective(const pps_problem* prob, int64_t npoints, const f
  *                                 const float* data, long long ndata, float* g)
  * (g = grad f(x), returns f(x)); without it, and for batches and
  * pps_sync_run_noalloc, the call returns PPS_ENOTSUP.
+ * A source that defines PPS_HAS_STREAM also gives f as a fold over the
+ * coordinates in increasing order (a state type pps_stream and
+ * pps_stream_start / pps_stream_add / pps_stream_finish, declared in
+ * pps_user_prelude.cuh); the synchronous step then evaluates f in registers
+ * as each coordinate moves instead of reading the new position back.  The
+ * fold must equal pps_objective bit for bit.
  * The library cannot bound the running time of the user's code: a function
  * that does not return hangs the run. */
 PPS_API int pps_objective_register(const char* source, int32_t* objective);

@@ -331,6 +331,18 @@ float orc_sin2pi(float x);
 """
 
 
+# the fold of a PPS_HAS_STREAM source driven as the step kernel drives it:
+# start, add for d = 0 .. dim-1, finish
+_USER_STREAM_SHIM = """
+float pps_stream_eval(const float* x, int dim, const float* p, const float* data, long long ndata) {
+  pps_stream s;
+  pps_stream_start(&s, dim, p, data, ndata);
+  for (int d = 0; d < dim; ++d) pps_stream_add(&s, d, x[d], dim, p, data, ndata);
+  return pps_stream_finish(&s, dim, p, data, ndata);
+}
+"""
+
+
 class UserObjective:
     """A user objective's source compiled as C by gcc (-ffp-contract=off) into
     oracle/_build/user_<hash>.so, linked against the oracle for pps_exp etc."""
@@ -342,7 +354,7 @@ class UserObjective:
         so = HERE / "_build" / f"user_{h}.so"
         if not so.exists():
             c = HERE / "_build" / f"user_{h}.c"
-            c.write_text(_USER_PREFIX + source + "\n")
+            c.write_text(_USER_PREFIX + source + "\n" + (_USER_STREAM_SHIM if "PPS_HAS_STREAM" in source else ""))
             tmp = so.with_suffix(f".{os.getpid()}.tmp")
             subprocess.run(["gcc", "-O2", "-fPIC", "-shared", "-std=gnu11", "-ffp-contract=off", "-fno-fast-math",
                             "-o", str(tmp), str(c), str(LIB_PATH), f"-Wl,-rpath,{LIB_PATH.parent}", "-lm"],
@@ -353,14 +365,26 @@ class UserObjective:
         self.fn = USER_FN(ctypes.cast(self.lib.pps_objective, ctypes.c_void_p).value)
         g = getattr(self.lib, "pps_gradient", None) if "PPS_HAS_GRADIENT" in source else None
         self.grad = USER_GRAD(ctypes.cast(g, ctypes.c_void_p).value) if g is not None else None
+        st = getattr(self.lib, "pps_stream_eval", None) if "PPS_HAS_STREAM" in source else None
+        self.stream_fn = USER_FN(ctypes.cast(st, ctypes.c_void_p).value) if st is not None else None
 
     def __call__(self, x, params=(), data=None) -> float:
+        return self._call(self.fn, x, params, data)
+
+    def stream(self, x, params=(), data=None) -> float:
+        """f(x) through the source's fold (start, add in increasing d, finish)."""
+        if self.stream_fn is None:
+            raise ValueError("the source does not define PPS_HAS_STREAM")
+        return self._call(self.stream_fn, x, params, data)
+
+    @staticmethod
+    def _call(fn, x, params, data) -> float:
         x = np.ascontiguousarray(np.asarray(x, np.float32))
         p = np.zeros(8, np.float32)
         p[:len(params)] = params
         d = None if data is None else np.ascontiguousarray(np.asarray(data, np.float32).reshape(-1))
-        return float(self.fn(fp(x), x.size, fp(p), fp(d) if d is not None else ctypes.cast(None, _fp),
-                             0 if d is None else d.size))
+        return float(fn(fp(x), x.size, fp(p), fp(d) if d is not None else ctypes.cast(None, _fp),
+                        0 if d is None else d.size))
 
 
 def ode_fit_problem(prob) -> OracleProblem:

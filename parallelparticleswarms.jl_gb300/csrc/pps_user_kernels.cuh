@@ -100,7 +100,11 @@ extern "C" __global__ void __launch_bounds__(pps::kUserThreads, PPS_USER_MB4)
 // blocks strides over the groups.  Dims are walked in pairs, one Philox call
 // per particle and pair, the loads of the next pair issued before the current
 // pair is computed.  The objective then runs once per particle over the
-// column this thread has just written.
+// column this thread has just written; that read-back mostly misses L2 at
+// large swarms (at 2^20 particles x 100 dims about 124 MB of new positions
+// are in flight across the GPU).  A source that defines PPS_HAS_STREAM folds
+// the objective into registers as each dim moves (pps_stream_add in
+// increasing d) and reads nothing back, as the registered kernels do.
 namespace pps {
 
 template <int PPT, bool CONS>
@@ -140,6 +144,11 @@ __device__ __forceinline__ void user_step(const SwarmDev& s, const ObjParams& op
 #pragma unroll
       for (int k = 0; k < PPT; ++k) ca[k].start(s.cons, s.ncons, D);
     }
+#ifdef PPS_HAS_STREAM
+    pps_stream fs[PPT];  // the objective folded over the dims as they move
+#pragma unroll
+    for (int k = 0; k < PPT; ++k) pps_stream_start(&fs[k], D, sp, data, ndata);
+#endif
     float xa[PPT], va[PPT], pa[PPT], xb[PPT], vb[PPT], pb[PPT];
     ldv<PPT>(xa, X + i0);
     ldv<PPT>(va, V + i0);
@@ -178,6 +187,9 @@ __device__ __forceinline__ void user_step(const SwarmDev& s, const ObjParams& op
           va[k] = velocity(xa[k], va[k], pa[k], sg[j], w, c1, c2, u01(r[k].a), u01(r[k].b));
           xa[k] = clamp_lb_ub(__fadd_rn(xa[k], va[k]), slb[j], sub[j]);
           if constexpr (CONS) ca[k].add(s.cons, s.ncons, D, j, xa[k]);
+#ifdef PPS_HAS_STREAM
+          pps_stream_add(&fs[k], j, xa[k], D, sp, data, ndata);
+#endif
         }
         stv<PPT>(X + o, xa);
         stv<PPT>(V + o, va);
@@ -194,6 +206,9 @@ __device__ __forceinline__ void user_step(const SwarmDev& s, const ObjParams& op
           vb[k] = velocity(xb[k], vb[k], pb[k], sg[j + 1], w, c1, c2, u01(r[k].c), u01(r[k].d));
           xb[k] = clamp_lb_ub(__fadd_rn(xb[k], vb[k]), slb[j + 1], sub[j + 1]);
           if constexpr (CONS) ca[k].add(s.cons, s.ncons, D, j + 1, xb[k]);
+#ifdef PPS_HAS_STREAM
+          pps_stream_add(&fs[k], j + 1, xb[k], D, sp, data, ndata);
+#endif
         }
         stv<PPT>(X + o, xb);
         stv<PPT>(V + o, vb);
@@ -211,7 +226,11 @@ __device__ __forceinline__ void user_step(const SwarmDev& s, const ObjParams& op
       const bool valid = i0 + k < n;
       float c = __int_as_float(0x7f800000);
       if (valid) {
+#ifdef PPS_HAS_STREAM
+        c = pps_stream_finish(&fs[k], D, sp, data, ndata);
+#else
         c = pps_objective(pps_point{X + i0 + k, npad}, D, sp, data, ndata);
+#endif
         if constexpr (CONS) c = __fadd_rn(c, penalty(ca[k], s.ncons, __uint2float_rn((uint32_t)(i0 + k + 2))));
       }
       cc[k] = c;

@@ -24,6 +24,24 @@
 //                                 const float* data, long long ndata, float* g)
 //
 // writing grad f(x) to g[0..dim) and returning f(x).
+//
+// The synchronous step can evaluate f without reading the new position back
+// from memory when f is a fold over the coordinates in increasing order.  A
+// source that defines PPS_HAS_STREAM also defines a state type pps_stream and
+//
+//   PPS_DEVICE void  pps_stream_start(pps_stream* s, int dim, const float* p,
+//                                     const float* data, long long ndata)
+//   PPS_DEVICE void  pps_stream_add(pps_stream* s, int d, float xd, int dim,
+//                                   const float* p, const float* data,
+//                                   long long ndata)
+//   PPS_DEVICE float pps_stream_finish(const pps_stream* s, int dim,
+//                                      const float* p, const float* data,
+//                                      long long ndata)
+//
+// The step kernel calls start, add for d = 0, 1, ..., dim - 1, then finish,
+// whose value must equal pps_objective at the same point bit for bit (the
+// same operations in the same order); the other kernels keep calling
+// pps_objective.
 #pragma once
 #include "pps_device.cuh"
 

@@ -40,13 +40,18 @@ CASES = [
     ("styblinski-sqrt", us.STYBLINSKI_SQRT, 9, 513, -5.0, 5.0, [], 20, None, False),
     ("griewank-D1", us.GRIEWANK, 1, 1, -600.0, 600.0, [], 10, None, False),
     ("griewank-ragged", us.GRIEWANK, 17, 4099, -600.0, 600.0, [], 10, None, False),
+    # the fold of PPS_HAS_STREAM sources in the step kernel (no read-back)
+    ("rastrigin-stream-D100", us.RASTRIGIN_STREAM, 100, 1024, -5.12, 5.12, [10.0], 8, None, False),
+    ("rosenbrock-stream-C1-pos", us.ROSENBROCK_STREAM, 3, 1000, -1.0, 10.0, [1.0, 100.0], 20, None, True),
+    ("rosenbrock-stream-D1", us.ROSENBROCK_STREAM, 1, 65, -1.0, 10.0, [1.0, 100.0], 10, None, False),
+    ("weighted-stream-ragged", us.WEIGHTED_SPHERE_STREAM, 13, 4099, -5.0, 5.0, [], 12, "weights", False),
 ]
 
 
 @pytest.mark.parametrize("case", CASES, ids=lambda c: c[0])
 def test_user_sync_matches_oracle_every_iteration(pps, orc, case):
     _, src, D, n, lo, hi, prm, iters, data, gpos = case
-    data = _polyfit_data() if data == "poly" else None
+    data = {"poly": _polyfit_data(), "weights": np.linspace(0.5, 4.5, D, dtype=np.float32)}.get(data)
     sw, ref = _pair(pps, orc, src, D, n, lo, hi, prm, seed=7, data=data, gpos=gpos)
     gsrc = orc.GBEST_FROM_POSITION if gpos else orc.GBEST_FROM_PBEST
     with sw:
@@ -66,6 +71,8 @@ def test_user_sync_matches_oracle_every_iteration(pps, orc, case):
     (us.ROSENBROCK, "rosenbrock", 100, 4096, -5.12, 5.12, [1.0, 100.0]),
     (us.RASTRIGIN, "rastrigin", 100, 8192, -5.12, 5.12, [10.0]),
     (us.SHIFTED_SPHERE, "shifted_sphere", 6, 3000, -3.0, 3.0, [0.5, -1.0, 2.0]),
+    (us.ROSENBROCK_STREAM, "rosenbrock", 100, 4096, -5.12, 5.12, [1.0, 100.0]),
+    (us.RASTRIGIN_STREAM, "rastrigin", 100, 8192, -5.12, 5.12, [10.0]),
 ])
 def test_user_source_reproduces_registered_kernel(pps, src, name, D, n, lo, hi, prm):
     """The NVRTC kernel over a source that spells a registered objective gives
@@ -86,13 +93,14 @@ def test_user_source_reproduces_registered_kernel(pps, src, name, D, n, lo, hi, 
         assert ia == ib and np.float32(ca) == np.float32(cb) and np.array_equal(ua, ub_)
 
 
-def test_user_constrained_matches_registered_and_oracle(pps, orc):
+@pytest.mark.parametrize("src", [us.SHIFTED_SPHERE, us.SHIFTED_SPHERE_STREAM], ids=["read-back", "stream"])
+def test_user_constrained_matches_registered_and_oracle(pps, orc, src):
     """test/constraints.jl's problem with f as a user source: the penalty
     path of the NVRTC kernel equals the registered one and the oracle."""
     lb, ub = np.zeros(2, np.float32), np.full(2, 2, np.float32)
     reg = pps.OptimizationProblem(pps.shifted_sphere, np.zeros(2, np.float32), [2.0, 1.0], lb=lb, ub=ub, cons=CONS)
-    usr = reg.remake(f=pps.cuda_objective(us.SHIFTED_SPHERE))
-    oprob = orc.OracleProblem(0, 2, lb, ub, params=[2.0, 1.0], cons=CONS, user=orc.UserObjective(us.SHIFTED_SPHERE))
+    usr = reg.remake(f=pps.cuda_objective(src))
+    oprob = orc.OracleProblem(0, 2, lb, ub, params=[2.0, 1.0], cons=CONS, user=orc.UserObjective(src))
     ref = orc.OracleSwarm(oprob, 1000, 5)
     with pps.Swarm(reg, 1000, seed=5) as a, pps.Swarm(usr, 1000, seed=5) as b:
         a.init()

@@ -57,8 +57,8 @@ def _register(pps, src):
         raise
 
 
-def test_register_compiles_and_deduplicates():
-    pkg = pytest.importorskip("parallelparticleswarms")
+def test_register_compiles_and_deduplicates(pps):
+    pkg = pps
     a = _register(pkg, us.ROSENBROCK)
     b = _register(pkg, us.ROSENBROCK)
     c = _register(pkg, us.RASTRIGIN)
@@ -66,8 +66,8 @@ def test_register_compiles_and_deduplicates():
     assert a.source == us.ROSENBROCK
 
 
-def test_register_reports_compile_errors():
-    pkg = pytest.importorskip("parallelparticleswarms")
+def test_register_reports_compile_errors(pps):
+    pkg = pps
     _register(pkg, us.SHIFTED_SPHERE)  # skips without NVRTC
     with pytest.raises(pkg.ArgumentError) as e:
         pkg.cuda_objective(us.HEAD + " { return undefined_name; }")
@@ -76,11 +76,11 @@ def test_register_reports_compile_errors():
         pkg.cuda_objective("")
 
 
-def test_register_with_gradient_compiles_the_local_stage():
+def test_register_with_gradient_compiles_the_local_stage(pps):
     """A source with PPS_HAS_GRADIENT compiles the HybridPSO local-stage
     kernels too (the shared device code of pps_local.cuh under NVRTC), and
     the oracle's C build of it has the gradient of the registered Rosenbrock."""
-    pkg = pytest.importorskip("parallelparticleswarms")
+    pkg = pps
     f = _register(pkg, us.ROSENBROCK_GRAD)
     assert f.id >= 256
 
@@ -94,3 +94,41 @@ def test_user_gradient_on_the_oracle(orc):
         fa, ga = reg.objective_grad(x)
         fb, gb = usr.objective_grad(x)
         assert np.float32(fa) == np.float32(fb) and np.array_equal(ga, gb)
+
+
+@pytest.mark.parametrize("name,D,params,data", [
+    ("RASTRIGIN_STREAM", 33, [10.0], None),
+    ("ROSENBROCK_STREAM", 7, [1.0, 100.0], None),
+    ("ROSENBROCK_STREAM", 1, [1.0, 100.0], None),
+    ("SHIFTED_SPHERE_STREAM", 11, [2.0, 1.0, -0.5], None),
+    ("WEIGHTED_SPHERE_STREAM", 9, [], np.linspace(0.5, 4.5, 9, dtype=np.float32)),
+])
+def test_stream_fold_equals_the_objective(orc, name, D, params, data):
+    """The contract of PPS_HAS_STREAM on the test sources: the fold the step
+    kernel drives (start, add in increasing d, finish) equals pps_objective bit
+    for bit, NaN and Inf inputs included, and the objective part is the
+    source it extends."""
+    user = orc.UserObjective(getattr(us, name))
+    assert user.stream_fn is not None and orc.UserObjective(us.RASTRIGIN).stream_fn is None
+    pts = list(_points(D, 400, -6.0, 6.0, seed=D + 1))
+    pts += [np.full(D, v, np.float32) for v in (0.0, -0.0, 1e30, np.inf, np.nan)]
+    for x in pts:
+        want, got = np.float32(user(x, params, data)), np.float32(user.stream(x, params, data))
+        assert got.tobytes() == want.tobytes() or (np.isnan(got) and np.isnan(want)), (name, x, got, want)
+    base = name.replace("_STREAM", "")
+    if hasattr(us, base):
+        plain = orc.UserObjective(getattr(us, base))
+        for x in pts[:50]:
+            assert np.float32(plain(x, params, data)).tobytes() == np.float32(user(x, params, data)).tobytes()
+
+
+def test_register_with_stream_compiles(pps):
+    """NVRTC compiles the step kernels' fold for PPS_HAS_STREAM sources, and a
+    source that declares the macro without the functions is a compile error."""
+    pkg = pps
+    ids = {_register(pkg, getattr(us, n)).id for n in ("RASTRIGIN_STREAM", "ROSENBROCK_STREAM",
+                                                          "SHIFTED_SPHERE_STREAM", "WEIGHTED_SPHERE_STREAM")}
+    assert len(ids) == 4 and min(ids) >= 256
+    with pytest.raises(pkg.ArgumentError) as e:
+        pkg.cuda_objective("#define PPS_HAS_STREAM 1\n" + us.SHIFTED_SPHERE)
+    assert "pps_stream" in str(e.value)

@@ -92,3 +92,62 @@ PPS_DEVICE float pps_gradient(pps_point x, int dim, const float* p, const float*
   return pps_objective(x, dim, p, data, ndata);
 }
 """
+
+# The same objectives with the fold the synchronous step uses instead of
+# reading the new position back (PPS_HAS_STREAM): each add performs the
+# objective loop's operations for one coordinate, in the same order, so the
+# fold equals pps_objective bit for bit.
+STREAM_ARGS = "const float* p, const float* data, long long ndata"
+
+RASTRIGIN_STREAM = "#define PPS_HAS_STREAM 1\n" + RASTRIGIN + f"""
+typedef struct {{ float s; }} pps_stream;
+PPS_DEVICE void pps_stream_start(pps_stream* st, int dim, {STREAM_ARGS}) {{ st->s = 0.0f; }}
+PPS_DEVICE void pps_stream_add(pps_stream* st, int d, float v, int dim, {STREAM_ARGS}) {{
+  st->s = st->s + (v * v - p[0] * pps_cos2pi(v));
+}}
+PPS_DEVICE float pps_stream_finish(const pps_stream* st, int dim, {STREAM_ARGS}) {{
+  return p[0] * (float)dim + st->s;
+}}
+"""
+
+ROSENBROCK_STREAM = "#define PPS_HAS_STREAM 1\n" + ROSENBROCK + f"""
+typedef struct {{ float s, prev; }} pps_stream;
+PPS_DEVICE void pps_stream_start(pps_stream* st, int dim, {STREAM_ARGS}) {{
+  st->s = 0.0f;
+  st->prev = 0.0f;
+}}
+PPS_DEVICE void pps_stream_add(pps_stream* st, int d, float v, int dim, {STREAM_ARGS}) {{
+  if (d > 0) {{
+    const float t = v - st->prev * st->prev;
+    const float u = p[0] - st->prev;
+    st->s = st->s + (p[1] * (t * t) + u * u);
+  }}
+  st->prev = v;
+}}
+PPS_DEVICE float pps_stream_finish(const pps_stream* st, int dim, {STREAM_ARGS}) {{ return st->s; }}
+"""
+
+SHIFTED_SPHERE_STREAM = "#define PPS_HAS_STREAM 1\n" + SHIFTED_SPHERE + f"""
+typedef struct {{ float s; }} pps_stream;
+PPS_DEVICE void pps_stream_start(pps_stream* st, int dim, {STREAM_ARGS}) {{ st->s = 0.0f; }}
+PPS_DEVICE void pps_stream_add(pps_stream* st, int d, float v, int dim, {STREAM_ARGS}) {{
+  const float t = v - (d < 8 ? p[d] : 0.0f);
+  st->s = st->s + t * t;
+}}
+PPS_DEVICE float pps_stream_finish(const pps_stream* st, int dim, {STREAM_ARGS}) {{ return st->s; }}
+"""
+
+# sum_d w_d x_d^2 with the weights w in the problem's data (one per coordinate)
+WEIGHTED_SPHERE_STREAM = "#define PPS_HAS_STREAM 1\n" + HEAD + """ {
+  float s = 0.0f;
+  for (int i = 0; i < dim; ++i) s = s + data[i] * (x[i] * x[i]);
+  return s;
+}
+""" + f"""
+typedef struct {{ float s; }} pps_stream;
+PPS_DEVICE void pps_stream_start(pps_stream* st, int dim, {STREAM_ARGS}) {{ st->s = 0.0f; }}
+PPS_DEVICE void pps_stream_add(pps_stream* st, int d, float v, int dim, {STREAM_ARGS}) {{
+  st->s = st->s + data[d] * (v * v);
+}}
+PPS_DEVICE float pps_stream_finish(const pps_stream* st, int dim, {STREAM_ARGS}) {{ return st->s; }}
+"""
