@@ -74,7 +74,11 @@ def cuda_objective(source: str, name: str = "user", default_params=()) -> Object
     ``Server``; with HybridPSO when the source also defines PPS_HAS_GRADIENT
     and ``PPS_DEVICE float pps_gradient(pps_point x, int dim, const float* p,
     const float* data, long long ndata, float* g)`` (g = grad f, returns f);
-    batches do not take it.
+    batches do not take it.  A source that defines PPS_HAS_STREAM also gives
+    f as a fold over the coordinates (``pps_stream`` with
+    ``pps_stream_start`` / ``pps_stream_add`` / ``pps_stream_finish``, equal
+    to ``pps_objective`` bit for bit), which the synchronous step evaluates in
+    registers instead of reading the new position back.
     """
     oid = ctypes.c_int32()
     _lib.check(_lib.load().pps_objective_register(source.encode(), ctypes.byref(oid)))
