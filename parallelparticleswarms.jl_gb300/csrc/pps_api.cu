@@ -651,8 +651,8 @@ int pps_get_state(pps_swarm* s, int32_t field, float* out) {
   if (!s || !out) return set_error(PPS_EINVAL, "NULL argument");
   int rc = use_device(s);
   if (rc) return rc;
-  float* dev;
-  int rows;
+  float* dev = nullptr;
+  int rows = 0;
   if ((rc = field_ptr(s, field, &dev, &rows))) return rc;
   const size_t w = sizeof(float) * (size_t)s->dv.n;
   return copy_rows_to_host(s->device, s->stream, reinterpret_cast<char*>(out), reinterpret_cast<const char*>(dev),
@@ -664,8 +664,8 @@ int pps_set_state(pps_swarm* s, int32_t field, const float* in) {
   if (field > PPS_FIELD_COST) return set_error(PPS_EINVAL, "field %d is read-only", field);
   int rc = use_device(s);
   if (rc) return rc;
-  float* dev;
-  int rows;
+  float* dev = nullptr;
+  int rows = 0;
   if ((rc = field_ptr(s, field, &dev, &rows))) return rc;
   const size_t w = sizeof(float) * (size_t)s->dv.n;
   PPS_CUDA(cudaMemcpy2DAsync(dev, sizeof(float) * (size_t)s->dv.npad, in, w, w, rows,
@@ -690,8 +690,8 @@ int pps_field_copy_create(pps_swarm* s, int32_t field, pps_field_copy** out) {
   if (!s || !out) return set_error(PPS_EINVAL, "NULL argument");
   int rc = use_device(s);
   if (rc) return rc;
-  float* src;
-  int rows;
+  float* src = nullptr;
+  int rows = 0;
   if ((rc = field_ptr(s, field, &src, &rows))) return rc;
   pps_field_copy* c = new (std::nothrow) pps_field_copy();
   if (!c) return set_error(PPS_ENOMEM, "host allocation failed");

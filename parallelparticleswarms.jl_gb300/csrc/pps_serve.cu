@@ -485,8 +485,9 @@ int pps_serve_submit(pps_server* s, const pps_problem* prob, int64_t n, uint64_t
     r->bytes = batch_swarm_bytes(r->desc.dim, r->desc.ld, r->desc.ndata);
   }
   if (r->bytes > s->cfg.memory_budget) {
+    const size_t need = r->bytes;
     delete r;
-    return set_error(PPS_ENOMEM, "request needs %zu bytes, more than the serving arena (%llu)", r->bytes,
+    return set_error(PPS_ENOMEM, "request needs %zu bytes, more than the serving arena (%llu)", need,
                      (unsigned long long)s->cfg.memory_budget);
   }
   r->t_submit = Clock::now();

@@ -111,7 +111,7 @@ def test_poll_and_errors(pps):
             srv.poll(t)  # released
         huge = pps.OptimizationProblem(pps.sphere, np.zeros(64, np.float32), lb=np.full(64, -1, np.float32),
                                        ub=np.full(64, 1, np.float32))
-        with pytest.raises(pps.PPSError):
+        with pytest.raises(pps.PPSError, match="more than the serving arena"):
             srv.submit(huge, 60000)  # 46 MB of state, more than the 16 MiB arena
         with pytest.raises(pps.ArgumentError):
             srv.submit(prob, 0)
