@@ -11,8 +11,8 @@
  *   - Arrays of particle data are structure-of-arrays, particle fastest:
  *     element (particle i, dim d) of an n-particle array is at [d*n + i].
  *     The reference keeps an array of SPSOParticle structs
- *     (src/ParallelParticleSwarms.jl:34-40); the Julia glue converts at the
- *     boundary.
+ *     (src/ParallelParticleSwarms.jl:34-40); pps_get_particles /
+ *     pps_set_particles move a swarm in that record layout.
  *   - A pps_swarm handle owns one CUDA stream.  A handle is not thread-safe;
  *     distinct handles may be used from distinct threads.
  *   - All arithmetic is IEEE binary32 (the reference's Float32 problems).
@@ -262,7 +262,9 @@ PPS_API int pps_serve_submit(pps_server* s, const pps_problem* prob, int64_t n, 
 /* PPS_OK and the result (the ticket is then released), or PPS_EBUSY */
 PPS_API int pps_serve_poll(pps_server* s, uint64_t ticket, float* u, float* cost, int64_t* idx,
                            double* latency_ms);
-/* block until done or timeout_s (PPS_ETIMEOUT) */
+/* block until done or timeout_s seconds pass (PPS_ETIMEOUT; a negative timeout
+ * does not wait, NaN is PPS_EINVAL); a ticket whose result another call has
+ * taken is PPS_EINVAL */
 PPS_API int pps_serve_wait(pps_server* s, uint64_t ticket, float* u, float* cost, int64_t* idx,
                            double* latency_ms, double timeout_s);
 PPS_API int pps_serve_stats_get(pps_server* s, pps_serve_stats* stats);

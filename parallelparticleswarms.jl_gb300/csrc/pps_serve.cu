@@ -535,16 +535,25 @@ int pps_serve_poll(pps_server* s, uint64_t ticket, float* u, float* cost, int64_
 int pps_serve_wait(pps_server* s, uint64_t ticket, float* u, float* cost, int64_t* idx, double* latency_ms,
                    double timeout_s) {
   if (!s) return set_error(PPS_EINVAL, "server is NULL");
+  if (std::isnan(timeout_s)) return set_error(PPS_EINVAL, "timeout_s is NaN");
+  // negative: no wait; at most about a year, so the deadline stays representable
+  const double limit_s = timeout_s < 0.0 ? 0.0 : std::min(timeout_s, 3.0e7);
   std::unique_lock<std::mutex> lock(s->mu);
-  auto it = s->reqs.find(ticket);
-  if (it == s->reqs.end()) return set_error(PPS_EINVAL, "unknown ticket %llu", (unsigned long long)ticket);
-  Request* r = it->second;
-  const auto deadline = Clock::now() + std::chrono::duration_cast<Clock::duration>(std::chrono::duration<double>(timeout_s));
-  while (r->state != 2) {
-    if (s->cv_done.wait_until(lock, deadline) == std::cv_status::timeout && r->state != 2)
-      return set_error(PPS_ETIMEOUT, "request %llu not done within %.3f s", (unsigned long long)ticket, timeout_s);
+  const auto deadline =
+      Clock::now() + std::chrono::duration_cast<Clock::duration>(std::chrono::duration<double>(limit_s));
+  while (true) {
+    // looked up again after every wake-up: another caller may have taken the
+    // result (and freed the request) meanwhile
+    auto it = s->reqs.find(ticket);
+    if (it == s->reqs.end()) return set_error(PPS_EINVAL, "unknown ticket %llu", (unsigned long long)ticket);
+    if (it->second->state == 2) return take_result(s, it->second, u, cost, idx, latency_ms);
+    if (s->cv_done.wait_until(lock, deadline) == std::cv_status::timeout) {
+      it = s->reqs.find(ticket);
+      if (it != s->reqs.end() && it->second->state == 2) return take_result(s, it->second, u, cost, idx, latency_ms);
+      if (it == s->reqs.end()) return set_error(PPS_EINVAL, "unknown ticket %llu", (unsigned long long)ticket);
+      return set_error(PPS_ETIMEOUT, "request %llu not done within %.3f s", (unsigned long long)ticket, limit_s);
+    }
   }
-  return take_result(s, r, u, cost, idx, latency_ms);
 }
 
 int pps_serve_stats_get(pps_server* s, pps_serve_stats* st) {
