@@ -424,16 +424,20 @@ static int step_once(pps_swarm* s, float c1, float c2) {
   return launch_sync_step(s, c1, c2);
 }
 
+// the run's flags for the duration of a run, the swarm's own again on every return
+struct RunFlags {
+  pps_swarm* s;
+  uint32_t saved;
+  RunFlags(pps_swarm* sw, uint32_t f) : s(sw), saved(sw->flags) { s->flags = f; }
+  ~RunFlags() { s->flags = saved; }
+};
+
 static int run_steps(pps_swarm* s, int32_t maxiters, float c1, float c2, uint32_t run_flags) {
   int rc;
-  const uint32_t saved = s->flags;
-  s->flags = run_flags;
+  RunFlags scoped(s, run_flags);
   // resolve occupancy (and load a user objective's kernels) outside any capture
   if (is_user(s->objective)) {
-    if ((rc = user_prepare(s))) {
-      s->flags = saved;
-      return rc;
-    }
+    if ((rc = user_prepare(s))) return rc;
   } else if (!is_ode(s->objective)) {
     sync_grid(s);
   }
@@ -449,7 +453,6 @@ static int run_steps(pps_swarm* s, int32_t maxiters, float c1, float c2, uint32_
         if ((rc = step_once(s, c1, c2))) {
           cudaStreamEndCapture(s->stream, &g);
           if (g) cudaGraphDestroy(g);
-          s->flags = saved;
           return rc;
         }
       }
@@ -457,7 +460,7 @@ static int run_steps(pps_swarm* s, int32_t maxiters, float c1, float c2, uint32_
       cudaError_t e = cudaGraphInstantiate(&s->graph, g, 0);
       cudaGraphDestroy(g);
       if (e != cudaSuccess) {
-        s->flags = saved;
+        s->graph = nullptr;  // unspecified after a failed instantiation
         return cuda_error(e, "cudaGraphInstantiate");
       }
       s->graph_len = kGraphChunk;
@@ -469,19 +472,12 @@ static int run_steps(pps_swarm* s, int32_t maxiters, float c1, float c2, uint32_
   int32_t left = maxiters;
   while (left >= kGraphChunk) {
     cudaError_t e = cudaGraphLaunch(s->graph, s->stream);
-    if (e != cudaSuccess) {
-      s->flags = saved;
-      return cuda_error(e, "cudaGraphLaunch");
-    }
+    if (e != cudaSuccess) return cuda_error(e, "cudaGraphLaunch");
     left -= kGraphChunk;
   }
   for (; left > 0; --left) {
-    if ((rc = step_once(s, c1, c2))) {
-      s->flags = saved;
-      return rc;
-    }
+    if ((rc = step_once(s, c1, c2))) return rc;
   }
-  s->flags = saved;
   return PPS_OK;
 }
 
