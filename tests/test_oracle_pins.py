@@ -6,9 +6,10 @@ particle count, iteration count and threshold:
   - statistical thresholds under fixed seeds (test/regression.jl, test/gpu.jl);
   - the exact loss reduction of ode_pso (test/regression.jl:345-389);
   - the L-BFGS known answers (test/lbfgs.jl:38-72), tested in test_hybrid_oracle.py.
-The random stream itself is pinned structurally against numpy's Philox4x64-10
-(same round function, different word size) and, on the GPU, against cuRAND's
-Philox4_32_10 (tests/test_gpu_philox.py).  The math functions are pinned
+The random stream itself is pinned by the published Philox4x32-10 known-answer
+vectors, structurally against numpy's Philox4x64-10 (same round function,
+different word size) and, on the GPU, against cuRAND's Philox4_32_10
+(tests/test_gpu_philox.py).  The math functions are pinned
 against float64 numpy within stated ulp bounds.
 """
 import json
@@ -28,6 +29,20 @@ def test_philox_round_structure_matches_numpy(orc):
         raw = [int(bg.random_raw()) for _ in range(8)]
         assert orc.philox4x64_10([1, 0, 0, 0], key) == raw[:4]
         assert orc.philox4x64_10([2, 0, 0, 0], key) == raw[4:]
+
+
+def test_philox4x32_known_answers(orc):
+    # the published known-answer vectors of Philox4x32-10 (Salmon, Moraes, Dror
+    # and Shaw, "Parallel random numbers: as easy as 1, 2, 3", SC'11; the
+    # Random123 distribution's kat_vectors): counter, key -> output
+    kat = [
+        ([0, 0, 0, 0], [0, 0], [0x6627E8D5, 0xE169C58D, 0xBC57AC4C, 0x9B00DBD8]),
+        ([0xFFFFFFFF] * 4, [0xFFFFFFFF] * 2, [0x408F276D, 0x41C83B0E, 0xA20BC7C6, 0x6D5451FD]),
+        ([0x243F6A88, 0x85A308D3, 0x13198A2E, 0x03707344], [0xA4093822, 0x299F31D0],
+         [0xD16CFE09, 0x94FDCCEB, 0x5001E420, 0x24126EA1]),
+    ]
+    for ctr, key, want in kat:
+        assert orc.philox4x32_10(ctr, key) == want
 
 
 def test_philox4x32_counter_sensitivity(orc):
