@@ -11,10 +11,16 @@ from .algorithms import BFGS, SimpleLBFGS
 
 def hybrid_solve(cache, *, maxiters=100, w=0.7298, wdamp=1.0, c1=1.4962, c2=1.4962, local_maxiters=50,
                  abstol=None, reltol=None, **kwargs):
+    """``abstol`` replaces the local optimiser's gradient-norm tolerance (gtol);
+    the local stages have no relative tolerance, so a ``reltol`` is refused
+    rather than ignored."""
     from .solve import OptimizationSolution, OptimizationStats, _pso_solve
 
     if kwargs:
         raise _lib.ArgumentError(_lib.EINVAL, f"unexpected keyword arguments {sorted(kwargs)}")
+    if reltol is not None:
+        raise _lib.ArgumentError(_lib.EINVAL, "reltol is not supported: the local stages stop on the gradient "
+                                              "norm (abstol, else the optimiser's gtol) or after local_maxiters")
     alg = cache.alg
     sol_pso = _pso_solve(cache.pso_cache, maxiters, w, wdamp, c1, c2)
     best_u, best_obj = sol_pso.u, sol_pso.objective

@@ -143,3 +143,12 @@ def test_valid_calls_fail_loudly_without_a_device(pps, lib):
     assert lib.pps_eval_objective(ctypes.byref(pr), 4, _lib.fptr(x), _lib.fptr(f)) == _lib.ENODEV
     with pytest.raises(pps.PPSError):
         pps.solve(prob, pps.ParallelSyncPSOKernel(16), maxiters=2)
+
+
+def test_hybrid_refuses_tolerances_it_does_not_have(pps):
+    from parallelparticleswarms.hybrid import hybrid_solve
+
+    with pytest.raises(pps.ArgumentError, match="reltol"):
+        hybrid_solve(None, reltol=1e-6)
+    with pytest.raises(pps.ArgumentError, match="linesearch"):
+        hybrid_solve(None, linesearch="strong_wolfe")
