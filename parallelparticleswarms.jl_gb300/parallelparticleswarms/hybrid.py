@@ -44,3 +44,31 @@ def hybrid_solve(cache, *, maxiters=100, w=0.7298, wdamp=1.0, c1=1.4962, c2=1.49
                                                         device_ms=ms + sol_pso.stats.device_ms,
                                                         iterations=int(maxiters)),
                                 alg=alg)
+
+
+def bfgs_solve(prob, alg: BFGS, *, maxiters=1000, abstol=None, reltol=None, **kwargs):
+    """solve(prob, BFGS(); maxiters) (src/bfgs.jl:2-36): Broyden's method on
+    grad f = 0 from u0 alone, the HybridPSO local stage on a single start
+    point.  Like the reference's, it takes no bounds and no constraints: f and
+    its gradient are used as they are.  ``abstol`` replaces ``alg.gtol``;
+    u = the solver's point, objective = f(u, p) evaluated on the device."""
+    from .problem import evaluate
+    from .solve import OptimizationSolution, OptimizationStats
+    from .swarm import Swarm
+
+    if kwargs:
+        raise _lib.ArgumentError(_lib.EINVAL, f"unexpected keyword arguments {sorted(kwargs)}")
+    if reltol is not None:
+        raise _lib.ArgumentError(_lib.EINVAL, "reltol is not supported: Broyden's method here stops on the "
+                                              "gradient norm (abstol, else BFGS.gtol) or after maxiters")
+    free = prob.remake(lb=None, ub=None, cons=None)
+    gtol = alg.gtol if abstol is None else float(abstol)
+    with Swarm(free, 1, seed=0) as sw:
+        sw.init()
+        sw.set(_lib.FIELD_POSITION, free.u0.reshape(free.dim, 1))
+        t0 = time.perf_counter()
+        u, _, _, ms = sw.local_stage("bfgs", maxiters=int(maxiters), gtol=gtol, max_backtracks=alg.max_backtracks)
+        t1 = time.perf_counter()
+    return OptimizationSolution(u=u, objective=float(evaluate(free, u)), original=None,
+                                stats=OptimizationStats(time=t1 - t0, device_ms=ms, iterations=int(maxiters)),
+                                alg=alg)

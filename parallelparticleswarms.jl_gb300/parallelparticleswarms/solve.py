@@ -174,12 +174,21 @@ def _plugin_solve(prob: OptimizationProblem, alg: PSOAlgorithm, maxiters: int, k
                                 stats=OptimizationStats(time=float(solve_time), iterations=int(maxiters)), alg=alg)
 
 
-def solve(prob: OptimizationProblem, alg, *, maxiters: int = 100, sampler=None, seed: int = 0,
+def solve(prob: OptimizationProblem, alg, *, maxiters: int | None = None, sampler=None, seed: int = 0,
           **kwargs) -> OptimizationSolution:
     """solve(prob, alg; maxiters) = solve!(init(prob, alg)) (src/solve.jl:61-67).
 
     Any other ``PSOAlgorithm`` runs through its ``pso_solve`` (src/solve.jl:69-87);
-    ``sampler`` and ``seed`` reach it as keywords when they are given."""
+    ``sampler`` and ``seed`` reach it as keywords when they are given.
+    ``BFGS()`` alone is Broyden's method from u0 (src/bfgs.jl:2-36).
+    ``maxiters`` defaults to 100, and to 1000 for ``BFGS()`` as in the reference."""
+    if isinstance(alg, BFGS):
+        if sampler is not None:
+            raise _lib.ArgumentError(_lib.EINVAL, "BFGS() starts from u0: it takes no sampler")
+        from .hybrid import bfgs_solve
+        return bfgs_solve(prob, alg, maxiters=1000 if maxiters is None else maxiters, **kwargs)
+    if maxiters is None:
+        maxiters = 100
     if isinstance(alg, PSOAlgorithm) and not isinstance(alg, (ParallelSyncPSOKernel, ParallelPSOKernel, HybridPSO)):
         if sampler is not None:
             kwargs["sampler"] = sampler

@@ -152,3 +152,30 @@ def test_hybrid_refuses_tolerances_it_does_not_have(pps):
         hybrid_solve(None, reltol=1e-6)
     with pytest.raises(pps.ArgumentError, match="linesearch"):
         hybrid_solve(None, linesearch="strong_wolfe")
+
+
+def test_standalone_bfgs_arguments(pps, monkeypatch):
+    """solve(prob, BFGS()) (src/bfgs.jl:2-36): refuses what it does not have
+    before any device work, defaults to 1000 iterations as the reference, and
+    without a device fails loudly."""
+    import parallelparticleswarms.hybrid as hy
+
+    prob = pps.OptimizationProblem(pps.rosenbrock, [-1.2, 1.0], [1.0, 100.0])
+    with pytest.raises(pps.ArgumentError, match="reltol"):
+        pps.solve(prob, pps.BFGS(), reltol=1e-8)
+    with pytest.raises(pps.ArgumentError, match="sampler"):
+        pps.solve(prob, pps.BFGS(), sampler=pps.GPUUniformSampler())
+    with pytest.raises(pps.ArgumentError, match="unexpected"):
+        pps.solve(prob, pps.BFGS(), local_maxiters=3)
+    seen = {}
+    monkeypatch.setattr(hy, "bfgs_solve", lambda prob, alg, **kw: seen.update(kw) or "ran")
+    assert pps.solve(prob, pps.BFGS()) == "ran" and seen["maxiters"] == 1000
+    assert pps.solve(prob, pps.BFGS(), maxiters=7) == "ran" and seen["maxiters"] == 7
+    monkeypatch.undo()
+    from parallelparticleswarms import _lib
+
+    n = ctypes.c_int32(-1)
+    if _lib.load().pps_device_count(ctypes.byref(n)) == _lib.OK and n.value > 0:
+        return
+    with pytest.raises(pps.PPSError):
+        pps.solve(prob, pps.BFGS())

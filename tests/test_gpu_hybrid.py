@@ -78,3 +78,24 @@ def test_hybrid_config_small(pps):
         assert np.isfinite(sol.objective) and np.all(np.isfinite(sol.u))
         assert np.all(sol.u >= -5) and np.all(sol.u <= 5)
         assert sol.objective < 1e-3, (name, sol.objective)
+
+
+@pytest.mark.parametrize("obj,name,u0,prm", [
+    (1, "rosenbrock", [-1.2, 1.0], [1.0, 100.0]),
+    (0, "sphere", [0.5, -2.0, 3.0], []),
+    (3, "ackley", [0.3, -0.2, 0.1, 0.05], [20.0, 0.2, 1.0]),
+])
+def test_standalone_bfgs_matches_oracle(pps, orc, obj, name, u0, prm):
+    """solve(prob, BFGS()) (src/bfgs.jl:2-36): Broyden's method from u0 without
+    bounds, 1000 iterations by default, bit-identical to the oracle's Broyden
+    from the same point; objective = f(u, p)."""
+    D = len(u0)
+    u0 = np.asarray(u0, np.float32)
+    prob = pps.OptimizationProblem(pps.REGISTRY[name], u0, prm or None)
+    sol = pps.solve(prob, pps.BFGS())
+    oprob = orc.OracleProblem(obj, D, None, None, params=prm)
+    rx, rf, rit = orc.lbfgs(oprob, u0.reshape(D, 1), maxiters=1000, gtol=1e-5, broyden=True)
+    assert np.array_equal(sol.u, rx[:, 0], equal_nan=True)
+    want = np.float32(oprob.objective(rx[:, 0]))
+    assert np.float32(sol.objective) == want or (np.isnan(sol.objective) and np.isnan(want))
+    assert sol.stats.iterations == 1000
