@@ -5,7 +5,8 @@ Exports mirror src/ParallelParticleSwarms.jl:102-104.
 """
 from ._lib import ArgumentError, PPSError
 from .algorithms import (BFGS, CUDA, GPUUniformSampler, GPUUnboundedSampler, HybridPSO, LatinHypercubeSample,
-                         ParallelPSOKernel, ParallelSyncPSOKernel, PSOAlgorithm, SimpleLBFGS)
+                         ParallelPSOArray, ParallelPSOKernel, ParallelSyncPSOKernel, PSOAlgorithm, SerialPSO,
+                         SimpleLBFGS)
 from .problem import (REGISTRY, Objective, OptimizationProblem, ackley, beale, booth, boundary_quadratic,
                       cuda_objective, evaluate, fitzhugh_nagumo_fit, himmelblau, lotka_volterra_fit,
                       mlp_regression, quadratic, quadratic_constraint, rastrigin, rosenbrock, shifted_sphere, sphere)
@@ -17,7 +18,8 @@ from .serve import Server
 from . import mlp, ode
 
 __all__ = [
-    "ParallelPSOKernel", "ParallelSyncPSOKernel", "PSOAlgorithm", "HybridPSO", "SimpleLBFGS", "BFGS",
+    "ParallelPSOKernel", "ParallelSyncPSOKernel", "ParallelPSOArray", "SerialPSO", "PSOAlgorithm", "HybridPSO",
+    "SimpleLBFGS", "BFGS",
     "OptimizationProblem", "solve", "solve_", "init", "reinit_", "pso_solve", "GPUUniformSampler",
     "GPUUnboundedSampler",
     "LatinHypercubeSample",

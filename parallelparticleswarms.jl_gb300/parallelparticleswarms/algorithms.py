@@ -107,6 +107,30 @@ class BFGS:
     max_backtracks: int = 30
 
 
+class _CpuOnly(PSOAlgorithm):
+    """A CPU algorithm of the reference, named so code written for it finds the
+    name; this engine has no CPU path, so solving with one raises."""
+
+    def __init__(self, num_particles: int, **kwargs):
+        self.num_particles = int(num_particles)
+
+    def pso_solve(self, prob, *, maxiters, **kwargs):
+        raise _lib.PPSError(_lib.ENOTSUP, f"{type(self).__name__} is the reference's CPU algorithm and this engine "
+                                          "has no CPU path: use ParallelSyncPSOKernel (synchronous) or "
+                                          "ParallelPSOKernel (asynchronous / queue-lock) on the GPU")
+
+
+class ParallelPSOArray(_CpuOnly):
+    """The reference's multithreaded CPU swarm over Julia arrays, global best
+    updated racily between threads (src/algorithms.jl:123-159,206-208,
+    src/lowerlevel_solve.jl:123-181)."""
+
+
+class SerialPSO(_CpuOnly):
+    """The reference's serial CPU swarm, the global best updated particle by
+    particle (src/algorithms.jl:161-190,210-212, src/lowerlevel_solve.jl:183-220)."""
+
+
 @dataclass
 class HybridPSO(PSOAlgorithm):
     """Particle-swarm search followed by a local refinement of every particle

@@ -110,3 +110,14 @@ def _u0_algorithm(pps):
 def test_device_objective_through_the_plugin(pps):
     sol = pps.solve(pps.OptimizationProblem(pps.sphere, [1.0, -2.0]), _u0_algorithm(pps))
     assert sol.objective == 5.0
+
+
+def test_reference_cpu_algorithms_are_named_and_refused(pps):
+    """ParallelPSOArray and SerialPSO (the reference's CPU algorithms) exist as
+    names; solving with them says which GPU algorithm replaces them."""
+    prob = pps.OptimizationProblem(pps.sphere, [1.0, -2.0], lb=[-5, -5], ub=[5, 5])
+    for alg in (pps.ParallelPSOArray(100), pps.SerialPSO(100)):
+        assert isinstance(alg, pps.PSOAlgorithm) and alg.num_particles == 100
+        with pytest.raises(pps.PPSError, match="ParallelSyncPSOKernel") as e:
+            pps.solve(prob, alg)
+        assert e.value.code == 6  # PPS_ENOTSUP
