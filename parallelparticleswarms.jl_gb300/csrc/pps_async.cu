@@ -8,7 +8,7 @@
 // personal best (the personal best only improves from then on and each
 // improvement beats the copy again), so the private state is one flag:
 // g_private = own ? pbest : g_start.  w is damped in-kernel (:219).  The run
-// ends with the argmin over personal bests (:119-120, src/lowerlevel_solve.jl:344).
+// ends with the argmin over personal bests (src/lowerlevel_solve.jl:119-120).
 //
 // GB300 design.  A particle's state lives in registers for the whole run: a
 // group of `lanes` threads (a power of two dividing 32) shares one particle,
