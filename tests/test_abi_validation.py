@@ -179,3 +179,36 @@ def test_standalone_bfgs_arguments(pps, monkeypatch):
         return
     with pytest.raises(pps.PPSError):
         pps.solve(prob, pps.BFGS())
+
+
+def test_problem_limits(pps, lib):
+    """The limits pps_swarm_create checks before it allocates anything."""
+    from parallelparticleswarms import _lib
+
+    def rc_of(pr, n=16):
+        h = ctypes.c_void_p()
+        rc = lib.pps_swarm_create(ctypes.byref(pr), n, 0, 0, ctypes.byref(h))
+        assert h.value is None
+        return rc, lib.pps_last_error().decode()
+
+    base = pps.OptimizationProblem(pps.sphere, np.zeros(3, np.float32), lb=np.full(3, -1.0, np.float32),
+                                   ub=np.full(3, 1.0, np.float32))
+    assert rc_of(base.to_c(), n=(1 << 32))[0] == _lib.EINVAL          # n beyond 2^32 - 256
+    big = pps.OptimizationProblem(pps.sphere, np.zeros(4097, np.float32))
+    rc, msg = rc_of(big.to_c())
+    assert rc == _lib.EINVAL and "dim" in msg
+    p9 = pps.OptimizationProblem(pps.sphere, np.zeros(3, np.float32), np.ones(9, np.float32))
+    rc, msg = rc_of(p9.to_c())
+    assert rc == _lib.EINVAL and "nparams" in msg
+    pr = base.to_c()
+    pr.nparams = 2  # count without a pointer
+    rc, msg = rc_of(pr)
+    assert rc == _lib.EINVAL and "params" in msg
+    row = pps.quadratic_constraint(3, c=-1.0, a=[1, 0, 0])
+    five = base.remake(cons=np.stack([row] * 5))
+    rc, msg = rc_of(five.to_c())
+    assert rc == _lib.EINVAL and "ncons" in msg
+    bad = row.copy()
+    bad[2] = np.nan
+    rc, msg = rc_of(base.remake(cons=bad[None, :]).to_c())
+    assert rc == _lib.EINVAL and "finite" in msg
