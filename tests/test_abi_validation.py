@@ -212,3 +212,23 @@ def test_problem_limits(pps, lib):
     bad[2] = np.nan
     rc, msg = rc_of(base.remake(cons=bad[None, :]).to_c())
     assert rc == _lib.EINVAL and "finite" in msg
+
+
+def test_serve_config_validation(lib):
+    """pps_serve_start checks its configuration before it looks for a device;
+    a valid one without a device is PPS_ENODEV."""
+    from parallelparticleswarms import _lib
+
+    h = ctypes.c_void_p()
+    assert lib.pps_serve_start(None, None) == _lib.EINVAL
+    for field, value in (("max_launches", 65), ("max_pack", 4097), ("threads", 96), ("ppt", 3)):
+        cfg = _lib.ServeConfig()
+        setattr(cfg, field, value)
+        assert lib.pps_serve_start(ctypes.byref(cfg), ctypes.byref(h)) == _lib.EINVAL, field
+        assert h.value is None
+    n = ctypes.c_int32(-1)
+    if lib.pps_device_count(ctypes.byref(n)) == _lib.OK and n.value > 0:
+        return
+    assert lib.pps_serve_start(ctypes.byref(_lib.ServeConfig()), ctypes.byref(h)) == _lib.ENODEV
+    assert lib.pps_serve_stop(None) == _lib.OK
+    assert lib.pps_serve_submit(None, None, 1, 0, 1, 0.7, 1.0, 1.4, 1.4, None) == _lib.EINVAL
