@@ -25,6 +25,8 @@
 // needs).  Calls whose work overlaps on the GPU -- on different streams, or
 // from several host threads without ordering -- race on it and give wrong
 // results; serialise them.
+#include <cmath>
+#include <cstddef>
 #include <mutex>
 
 #include "pps_internal.h"
@@ -103,9 +105,14 @@ __global__ void k_noalloc_select(SwarmDev s, int from_position) {
   }
 }
 
-// the global best of a swarm whose personal bests were just set (key and
-// count are canonical between calls: every step kernel resets them)
+// the global best of a swarm whose personal bests were just set.  The argmin
+// slot and the block ticket are reset first: a swarm that was created but
+// never initialised holds zeros there (a zero key would make particle 0 the
+// winner whatever its cost); t and w are left as they are.
 int launch_select_gbest(pps_swarm* s) {
+  static_assert(offsetof(IterState, key) == 0 && offsetof(IterState, count) == 8, "IterState layout");
+  PPS_CUDA(cudaMemsetAsync(&s->dv.st->key, 0xFF, sizeof(s->dv.st->key), s->stream));
+  PPS_CUDA(cudaMemsetAsync(&s->dv.st->count, 0, sizeof(s->dv.st->count), s->stream));
   k_noalloc_select<<<s->sm_count, 256, 0, s->stream>>>(s->dv, (s->flags & PPS_FLAG_GBEST_FROM_POSITION) ? 1 : 0);
   PPS_CUDA(cudaGetLastError());
   return PPS_OK;
@@ -132,7 +139,12 @@ extern "C" int pps_sync_run_noalloc(int32_t objective, const float* params, int3
   if (nparams < 0 || nparams > 8 || (nparams > 0 && !params))
     return set_error(PPS_EINVAL, "nparams must be in [0, 8] with params set");
   if (maxiters < 0) return set_error(PPS_EINVAL, "maxiters must be >= 0");
-  const void* ptrs[] = {sw->x, sw->v, sw->pbest, sw->pcost, sw->cost, sw->lb, sw->ub, sw->g};
+  if (!std::isfinite(w) || !std::isfinite(wdamp) || !std::isfinite(c1) || !std::isfinite(c2))
+    return set_error(PPS_EINVAL, "coefficients must be finite");
+  // the Philox counters of an iteration include its number: a wrapped counter repeats draws
+  if ((uint64_t)iteration + (uint64_t)maxiters > 0xFFFFFFFFull)
+    return set_error(PPS_EINVAL, "iteration counter would overflow (iteration %u + maxiters %d)", iteration, maxiters);
+  const void* ptrs[]= {sw->x, sw->v, sw->pbest, sw->pcost, sw->cost, sw->lb, sw->ub, sw->g};
   for (const void* p : ptrs) {
     if (!p) return set_error(PPS_EINVAL, "a device buffer of the swarm is NULL");
     if (!aligned16(p)) return set_error(PPS_EINVAL, "device buffers must be 16-byte aligned");
@@ -157,7 +169,7 @@ extern "C" int pps_sync_run_noalloc(int32_t objective, const float* params, int3
   pps_swarm h;
   h.device = device;
   h.stream = static_cast<cudaStream_t>(stream);
-  cudaDeviceGetAttribute(&h.sm_count, cudaDevAttrMultiProcessorCount, device);
+  PPS_CUDA(cudaDeviceGetAttribute(&h.sm_count, cudaDevAttrMultiProcessorCount, device));
   h.dv.X = sw->x;
   h.dv.V = sw->v;
   h.dv.P = sw->pbest;

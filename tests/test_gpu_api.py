@@ -143,3 +143,37 @@ def test_particle_records_round_trip(pps, D, n):
         ua, ca, ia = a.gbest()
         ub_, cb, ib = b.gbest()
         assert ia == ib and np.float32(ca) == np.float32(cb) and np.array_equal(ua, ub_)
+
+
+@pytest.mark.parametrize("layout", ["aos", "soa"])
+def test_set_particles_on_a_fresh_swarm(pps, layout):
+    """Setting the particles of a swarm that was created but never
+    initialised: the global best is the argmin of best_cost (lowest index on
+    ties), not particle 0 of the zeroed state, and a run continues from it as
+    from the same records set after an init."""
+    from parallelparticleswarms import _lib
+
+    D, n = 7, 2500
+    lb, ub = np.full(D, -5.12, np.float32), np.full(D, 5.12, np.float32)
+    prob = pps.OptimizationProblem(pps.rastrigin, np.zeros(D, np.float32), [10.0], lb=lb, ub=ub)
+    with pps.Swarm(prob, n, seed=4) as a, pps.Swarm(prob, n, seed=4) as fresh, pps.Swarm(prob, n, seed=4) as b:
+        a.init()
+        a.sync_run(6)
+        rec = a.particles()
+        if layout == "aos":
+            fresh.set_particles(rec)
+        else:
+            soa = np.concatenate([rec["position"].T.ravel(), rec["velocity"].T.ravel(), rec["cost"],
+                                  rec["best_position"].T.ravel(), rec["best_cost"]]).astype(np.float32)
+            _lib.check(fresh._lib.pps_set_particles(fresh._h, _lib.LAYOUT_SOA, _lib.fptr(soa)))
+        u, c, i = fresh.gbest()
+        want = int(np.argmin(rec["best_cost"]))
+        assert i == want  # the zeroed argmin slot of a fresh swarm would give particle 0
+        assert np.float32(c) == rec["best_cost"][want] and np.array_equal(u, rec["best_position"][want])
+        b.init()
+        b.set_particles(rec)
+        fresh.sync_run(5)
+        b.sync_run(5)
+        sf, sb = fresh.state(), b.state()
+        for k in ("x", "v", "pbest", "pcost", "cost"):
+            assert np.array_equal(sf[k], sb[k]), k
