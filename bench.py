@@ -614,6 +614,74 @@ def _open_loop(pps, cfg, rate, window, with_mlp, seed) -> dict:
             "mean_pack": st["mean_pack"], "arena_peak_bytes": st["arena_peak_bytes"]}
 
 
+def run_sharded(pps, args, rank, world, local, dist) -> int:
+    """--shard: the 2^20 x 100-D swarm split into `world` particle ranges, one
+    per rank; every iteration is the shard's step, an all-gather of the ranks'
+    records (NCCL) and the global best applied, all on the shard's stream.
+    The whole job processes the same 2^20 particles per iteration at every N
+    (strong scaling)."""
+    import torch
+
+    prob = make_problem(pps)
+    iters = args.iters
+    torch.cuda.set_device(local)
+    sh = pps.ShardedSwarm(prob, N_PARTICLES, rank, world, seed=0)
+    stream = sh.shard.stream
+    for k in range(args.warmup):
+        sh.init()
+        sh.sync_run(iters)
+    step_ms = []
+    if dist:
+        dist.barrier()
+    with ClockSampler(local) as clk:
+        for k in range(args.steps):
+            sh.init()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            sh.sync_run(iters)  # ends with a wait for the shard's stream
+            e1.record(stream)
+            e1.synchronize()
+            step_ms.append(e0.elapsed_time(e1))
+    if dist:
+        dist.barrier()
+    total_ms = multi_max(sum(step_ms), dist, local)
+    _, gcost, gidx = sh.gbest()
+    count = sh.shard.n
+    sh.close()
+    value = N_PARTICLES * iters * args.steps / (total_ms / 1e3)
+    launch_ms = total_ms / (args.steps * iters)
+    algo_bytes = count * BYTES_PER_PARTICLE_ITER
+    peak, peak_src = measured_hbm_peak()
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+                "scaling": "strong", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+                "config": {"workload": WORKLOAD, "particles": N_PARTICLES, "dim": DIM, "iterations_per_step": iters,
+                           "objective": "rastrigin", "algorithm": "ParallelSyncPSOKernel",
+                           "l2": "inputs larger than L2: 2.1 GB of swarm state streamed per iteration",
+                           "parallelism": f"one swarm in {world} particle-range shard(s), one per GPU, "
+                                          "all-gather of the shards' best-particle records per iteration"},
+                "e2e": None,
+                "gpu_launches": args.steps * (2 * iters + 3),
+                "roofline": {"bound": "hbm", "unit": "GB/s", "kernel": "k_sync_step<Rastrigin> on one shard",
+                             "achieved_per_iteration_incl_exchange": algo_bytes / (launch_ms / 1e3) / 1e9,
+                             "peak": peak, "peak_source": peak_src,
+                             "frac": algo_bytes / (launch_ms / 1e3) / 1e9 / peak,
+                             "algorithmic_bytes_per_launch": algo_bytes, "avg_iteration_ms": launch_ms,
+                             "traffic": None},
+                "cpu_baseline": None, "clocks": clk.summary(), "final_gbest_cost": gcost, "final_gbest_index": gidx}
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def multi_max(value, dist, local):
+    from parallelparticleswarms import multi
+
+    return multi.max_over_ranks(value, dist, f"cuda:{local}")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -643,6 +711,9 @@ def main():
     ap.add_argument("--serve-seconds-mlp", type=float, default=0.25,
                     help="arrival window of the open-loop served run of the full mix")
     ap.add_argument("--ode-fits", type=int, default=512, help="fits of each model in the batched ODE run")
+    ap.add_argument("--shard", action="store_true",
+                    help="one swarm of 2^20 particles split by particle ranges over the ranks, one global-best "
+                         "exchange (all-gather of 416-byte records) per iteration: strong scaling")
     args = ap.parse_args()
     from parallelparticleswarms import multi
 
@@ -677,6 +748,8 @@ def main():
         if rank == 0:
             print(json.dumps({args.only: fn()}), flush=True)
         return 0
+    if args.shard:
+        return run_sharded(pps, args, rank, world, local, dist)
     if args.only == "async":
         sa = pps.Swarm(prob, N_PARTICLES, seed=seed0 + 1)
         sa.init()

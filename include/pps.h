@@ -334,6 +334,49 @@ PPS_API int pps_eval_objective(const pps_problem* prob, int64_t npoints, const f
  * that does not return hangs the run. */
 PPS_API int pps_objective_register(const char* source, int32_t* objective);
 
+/* ---- particle-range shards of one swarm ---- */
+/* The synchronous loop couples particles only through its per-iteration
+ * global best: block bests, then their minimum (src/kernels.jl:156-171,
+ * src/lowerlevel_solve.jl:23-33).  A shard holds particles first .. first +
+ * count - 1 of an n_global-particle swarm and moves them exactly as the whole
+ * swarm does (random streams, argmin keys and the penalty's particle index
+ * use the global index), so the swarm splits over processes or GPUs with one
+ * exchange per iteration:
+ *   pps_shard_step (or pps_swarm_init)  writes the shard's exchange record:
+ *        its best particle's argmin key (uint64 at byte 0: orderable cost << 32
+ *        | global index), cost (float at byte 8) and vector (dim floats from
+ *        byte 16), pps_shard_record's `bytes` in all;
+ *   the caller gathers every shard's record into one array (an all-gather of
+ *        fixed-size records, e.g. ncclAllGather, or device copies);
+ *   pps_shard_apply makes the lowest key of that array the global best.
+ * Objectives: the registered closed-form ones (constraints included).  A
+ * shard is stepped only through the calls below: pps_sync_run, pps_async_run,
+ * pps_queue_run, the local stage and pps_set_particles return PPS_ENOTSUP on
+ * it.  Nothing below waits for the device except pps_shard_finish; all work of
+ * a shard is ordered on its stream (pps_shard_record returns it). */
+PPS_API int pps_shard_create(const pps_problem* prob, int64_t n_global, int64_t first, int64_t count,
+                             uint64_t seed, uint32_t flags, pps_swarm** out);
+/* the shard's own exchange record (device address), its size in bytes and the
+ * shard's cudaStream_t; any may be NULL */
+PPS_API int pps_shard_record(pps_swarm* s, void** record, int64_t* bytes, void** stream);
+/* Exchange buffers of the caller's (device memory, 16-byte aligned): the shard
+ * writes its record to `record` and pps_shard_apply reads `nrecords` records
+ * from `records` (record r at r * bytes).  Until bound, both are the shard's
+ * own record with nrecords = 1 (a swarm of one shard). */
+PPS_API int pps_shard_bind(pps_swarm* s, void* record, const void* records, int32_t nrecords);
+/* One synchronous iteration of the shard's particles (vectorized_solve! of
+ * ParallelSyncPSOKernel, one trip of src/lowerlevel_solve.jl:1-36); begin != 0
+ * starts a run: inertia w, damped by wdamp after each iteration. */
+PPS_API int pps_shard_step(pps_swarm* s, int32_t begin, float w, float wdamp, float c1, float c2);
+/* ParallelPSOKernel(global_update=false) on the shard (src/kernels.jl:196-225):
+ * maxiters iterations in one launch, the record written after the last */
+PPS_API int pps_shard_async(pps_swarm* s, int32_t maxiters, float w, float wdamp, float c1, float c2);
+/* the global best := the bound record with the lowest key */
+PPS_API int pps_shard_apply(pps_swarm* s);
+/* the deferred personal-best copies (so pps_get_state reads canonical state);
+ * waits for the shard's stream */
+PPS_API int pps_shard_finish(pps_swarm* s);
+
 /* ---- caller-owned device buffers, no allocation ---- */
 /* A swarm whose device arrays belong to the caller.  All pointers are DEVICE
  * pointers, 16-byte aligned.  Element (particle i, dim d) is at [d*ld + i];

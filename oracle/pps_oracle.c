@@ -530,13 +530,16 @@ uint32_t orc_lhs_stratum(uint32_t i, uint32_t n, uint32_t d, uint64_t seed) {
 /* ------------------------------------------------------------------------ */
 /* init (src/utils.jl:23-84, src/init.jl:38-54)                             */
 /* ------------------------------------------------------------------------ */
+static inline int64_t swarm_nglobal(const orc_swarm* s) { return s->nglobal > 0 ? s->nglobal : s->n; }
+
 void orc_init(const orc_problem* prob, orc_swarm* s, uint64_t seed, int32_t sampler) {
   const int D = prob->dim;
-  const int64_t n = s->n;
+  const int64_t n = s->n, ng = swarm_nglobal(s);
   for (int64_t i = 0; i < n; ++i) {
+    const uint32_t gi = (uint32_t)(s->first + i);  /* index in the whole swarm */
     for (int j = 0; j < (D + 3) / 4; ++j) {
       uint32_t o[4];
-      philox_step(seed, (uint32_t)i, (uint32_t)j, 0u, ORC_TAG_INIT, o);
+      philox_step(seed, gi, (uint32_t)j, 0u, ORC_TAG_INIT, o);
       for (int k = 0; k < 4; ++k) {
         int d = 4 * j + k;
         if (d >= D) break;
@@ -548,7 +551,7 @@ void orc_init(const orc_problem* prob, orc_swarm* s, uint64_t seed, int32_t samp
           xv = (a > 0.0f) ? (u0 + (u * a)) : u;
         } else if (sampler == ORC_SAMPLER_LHS) {
           /* x = ((stratum + U) / n) (ub - lb) + lb */
-          const float t = ((float)orc_lhs_stratum((uint32_t)i, (uint32_t)n, (uint32_t)d, seed) + u) / (float)n;
+          const float t = ((float)orc_lhs_stratum(gi, (uint32_t)ng, (uint32_t)d, seed) + u) / (float)ng;
           xv = (t * (prob->ub[d] - prob->lb[d])) + prob->lb[d];
         } else {
           /* uniform_itr: rand(T) * (ub[i] - lb[i]) + lb[i] */
@@ -567,17 +570,41 @@ void orc_init(const orc_problem* prob, orc_swarm* s, uint64_t seed, int32_t samp
   orc_select_gbest(prob, s, ORC_GBEST_FROM_PBEST);
 }
 
+/* the uniform draws of init and of step t, exported so that an independent
+ * restatement (the float64 one, oracle/pso_f64.py) consumes the same random
+ * numbers: u / r1 / r2 [d*n + i] of particle first + i in dim d */
+void orc_init_draws(uint64_t seed, int64_t first, int64_t n, int32_t dim, float* u) {
+  for (int64_t i = 0; i < n; ++i)
+    for (int j = 0; j < (dim + 3) / 4; ++j) {
+      uint32_t o[4];
+      philox_step(seed, (uint32_t)(first + i), (uint32_t)j, 0u, ORC_TAG_INIT, o);
+      for (int k = 0; k < 4 && 4 * j + k < dim; ++k) u[(int64_t)(4 * j + k) * n + i] = orc_u01(o[k]);
+    }
+}
+
+void orc_step_draws(uint64_t seed, int64_t first, int64_t n, int32_t dim, uint32_t t, float* r1, float* r2) {
+  for (int64_t i = 0; i < n; ++i)
+    for (int j = 0; j < (dim + 1) / 2; ++j) {
+      uint32_t o[4];
+      philox_step(seed, (uint32_t)(first + i), (uint32_t)j, t, ORC_TAG_STEP, o);
+      for (int h = 0; h < 2 && 2 * j + h < dim; ++h) {
+        r1[(int64_t)(2 * j + h) * n + i] = orc_u01(o[2 * h]);
+        r2[(int64_t)(2 * j + h) * n + i] = orc_u01(o[2 * h + 1]);
+      }
+    }
+}
+
 void orc_select_gbest(const orc_problem* prob, orc_swarm* s, int32_t gbest_source) {
   const int64_t n = s->n;
   uint64_t best = ~0ull;
   for (int64_t i = 0; i < n; ++i) {
-    uint64_t k = orc_argmin_key(s->pcost[i], (uint32_t)i);
+    uint64_t k = orc_argmin_key(s->pcost[i], (uint32_t)(s->first + i));
     if (k < best) best = k;
   }
-  int64_t gi = (int64_t)(uint32_t)best;
+  int64_t gi = (int64_t)(uint32_t)best, li = gi - s->first;
   const float* src = (gbest_source == ORC_GBEST_FROM_POSITION) ? s->x : s->pbest;
-  for (int d = 0; d < prob->dim; ++d) s->g[d] = src[d * n + gi];
-  s->gcost = s->pcost[gi];
+  for (int d = 0; d < prob->dim; ++d) s->g[d] = src[d * n + li];
+  s->gcost = s->pcost[li];
   s->gidx = gi;
 }
 
@@ -632,11 +659,12 @@ static void sync_worker(void* a_, int tid, int nth) {
   int64_t b, e;
   split_range(n, tid, nth, &b, &e);
   for (int64_t i = b; i < e; ++i) {
-    update_dims(a->prob, s->x + i, s->v + i, s->pbest + i, s->g, n, (uint32_t)i, a->t, a->seed,
+    const int64_t gi = s->first + i;  /* index in the whole swarm */
+    update_dims(a->prob, s->x + i, s->v + i, s->pbest + i, s->g, n, (uint32_t)gi, a->t, a->seed,
                 a->w, a->c1, a->c2);
     float c = orc_objective(a->prob, s->x + i, n, 1);
     /* the sync step passes the 1-based particle index as iter (src/kernels.jl:151) */
-    if (a->prob->ncons > 0) c = c + orc_penalty(a->prob, s->x + i, n, (float)(i + 2));
+    if (a->prob->ncons > 0) c = c + orc_penalty(a->prob, s->x + i, n, (float)(gi + 2));
     s->cost[i] = c;
     if (c < s->pcost[i]) {
       s->pcost[i] = c;
@@ -699,7 +727,7 @@ static void async_worker(void* a_, int tid, int nth) {
     float w = a->w;
     for (int32_t it = 0; it < a->iters; ++it) {
       for (int d = 0; d < D; ++d) gp[d] = own ? s->pbest[d * n + i] : s->g[d];
-      update_dims(prob, s->x + i, s->v + i, s->pbest + i, gp, n, (uint32_t)i,
+      update_dims(prob, s->x + i, s->v + i, s->pbest + i, gp, n, (uint32_t)(s->first + i),
                   a->t0 + (uint32_t)it, a->seed, w, a->c1, a->c2);
       float c = orc_objective(prob, s->x + i, n, a->lanes);
       s->cost[i] = c;

@@ -114,6 +114,13 @@ typedef struct orc_swarm {
   float* g;       /* dim floats: global best position */
   float gcost;
   int64_t gidx;
+  /* Particle-range shard of a larger swarm: local particle i is particle
+   * first + i of nglobal (0: nglobal = n, a whole swarm).  Random streams,
+   * argmin keys, the penalty's particle index and the Latin-hypercube strata
+   * use the global index; g / gcost / gidx then hold the shard's own best
+   * (gidx global) until the caller replaces them by the exchanged winner. */
+  int64_t first;
+  int64_t nglobal;
 } orc_swarm;
 
 /* ---- primitives ---- */
@@ -151,6 +158,11 @@ uint32_t orc_lhs_stratum(uint32_t i, uint32_t n, uint32_t d, uint64_t seed);
 enum { ORC_GBEST_FROM_PBEST = 0, ORC_GBEST_FROM_POSITION = 1 };
 
 void orc_init(const orc_problem* prob, orc_swarm* s, uint64_t seed, int32_t sampler);
+/* the uniform draws of init (u) and of step t (r1, r2) as [d*n + i] arrays for
+ * particles first .. first + n - 1: the random numbers orc_init / orc_sync_run
+ * consume, for an independent restatement to consume too */
+void orc_init_draws(uint64_t seed, int64_t first, int64_t n, int32_t dim, float* u);
+void orc_step_draws(uint64_t seed, int64_t first, int64_t n, int32_t dim, uint32_t t, float* r1, float* r2);
 /* argmin of pcost (lowest index on ties), gather g from pbest or position */
 void orc_select_gbest(const orc_problem* prob, orc_swarm* s, int32_t gbest_source);
 /* `iters` synchronous iterations starting at iteration counter t0.

@@ -49,7 +49,8 @@ class Problem(ctypes.Structure):
 
 class SwarmC(ctypes.Structure):
     _fields_ = [("n", ctypes.c_int64), ("dim", ctypes.c_int32), ("x", _fp), ("v", _fp), ("pbest", _fp),
-                ("pcost", _fp), ("cost", _fp), ("g", _fp), ("gcost", ctypes.c_float), ("gidx", ctypes.c_int64)]
+                ("pcost", _fp), ("cost", _fp), ("g", _fp), ("gcost", ctypes.c_float), ("gidx", ctypes.c_int64),
+                ("first", ctypes.c_int64), ("nglobal", ctypes.c_int64)]
 
 
 class LbfgsOpts(ctypes.Structure):
@@ -228,9 +229,14 @@ class OracleOdeFit:
 
 
 class OracleSwarm:
-    """SoA swarm state on the host, stepped by the restatement."""
+    """SoA swarm state on the host, stepped by the restatement.  With
+    ``nglobal`` > 0 it is the shard of particles first .. first + n - 1 of an
+    nglobal-particle swarm: after each init / step its g, gcost, gidx hold the
+    shard's own best, and :meth:`record` / :meth:`apply` are the global-best
+    exchange (the whole swarm's argmin over the shards' bests,
+    src/lowerlevel_solve.jl:23-33)."""
 
-    def __init__(self, prob: OracleProblem, n: int, seed: int):
+    def __init__(self, prob: OracleProblem, n: int, seed: int, first: int = 0, nglobal: int = 0):
         self.prob, self.n, self.dim, self.seed = prob, int(n), prob.dim, int(seed)
         D, n = self.dim, self.n
         self.x = np.zeros((D, n), np.float32)
@@ -240,8 +246,29 @@ class OracleSwarm:
         self.cost = np.zeros(n, np.float32)
         self.g = np.zeros(D, np.float32)
         self.c = SwarmC(n, D, fp(self.x), fp(self.v), fp(self.pbest), fp(self.pcost), fp(self.cost), fp(self.g),
-                        0.0, 0)
+                        0.0, 0, int(first), int(nglobal))
         self.t = 0
+
+    def record(self) -> np.ndarray:
+        """The shard's exchange record: argmin key (uint64), cost (float32), 0,
+        then the vector, padded to a multiple of 16 bytes."""
+        nbytes = (16 + 4 * self.dim + 15) // 16 * 16
+        rec = np.zeros(nbytes, np.uint8)
+        rec[0:8] = np.frombuffer(np.uint64(argmin_key(self.c.gcost, self.gidx)).tobytes(), np.uint8)
+        rec[8:12] = np.frombuffer(np.float32(self.c.gcost).tobytes(), np.uint8)
+        rec[16:16 + 4 * self.dim] = np.frombuffer(self.g.tobytes(), np.uint8)
+        return rec
+
+    def apply(self, records) -> None:
+        """The global best := the record with the lowest key (records: nrec x bytes
+        or the flat concatenation)."""
+        nbytes = (16 + 4 * self.dim + 15) // 16 * 16
+        recs = np.asarray(records, np.uint8).reshape(-1, nbytes)
+        keys = [int(np.frombuffer(r[0:8].tobytes(), np.uint64)[0]) for r in recs]
+        w = min(range(len(keys)), key=keys.__getitem__)  # the first of equal keys (equal keys are one particle)
+        self.g[:] = np.frombuffer(recs[w, 16:16 + 4 * self.dim].tobytes(), np.float32)
+        self.c.gcost = float(np.frombuffer(recs[w, 8:12].tobytes(), np.float32)[0])
+        self.c.gidx = keys[w] & 0xFFFFFFFF
 
     @property
     def gcost(self) -> float:
@@ -274,6 +301,11 @@ class OracleSwarm:
     def state(self) -> dict:
         return {"x": self.x.copy(), "v": self.v.copy(), "pbest": self.pbest.copy(), "pcost": self.pcost.copy(),
                 "cost": self.cost.copy()}
+
+
+def argmin_key(cost: float, idx: int) -> int:
+    """(orderable cost << 32) | idx, the key every argmin minimises."""
+    return int(load().orc_argmin_key(float(np.float32(cost)), int(idx) & 0xFFFFFFFF))
 
 
 def async_lanes(dim: int):

@@ -136,12 +136,12 @@ namespace pps {
 
 // One device block per swarm, carved into 256-byte-aligned arrays.
 struct SwarmLayout {
-  size_t oX, oV, oP, oPc, oC, oF, oG, oLb, oUb, oU0, oSt, oData, oMlpA, oCons, bytes;
+  size_t oX, oV, oP, oPc, oC, oF, oG, oLb, oUb, oU0, oSt, oData, oMlpA, oCons, oRec, bytes;
   int64_t npad;
   int mlp_samples;
 };
 
-static SwarmLayout swarm_layout(const pps_problem* prob, int64_t n) {
+static SwarmLayout swarm_layout(const pps_problem* prob, int64_t n, bool shard = false) {
   SwarmLayout L{};
   const int D = prob->dim;
   L.npad = (int64_t)align_up((size_t)n, 64);
@@ -166,6 +166,7 @@ static SwarmLayout swarm_layout(const pps_problem* prob, int64_t n) {
   L.mlp_samples = prob->objective == kMlp ? (int)(prob->ndata / 17) : 0;
   L.oMlpA = take(L.mlp_samples ? mlp_a_bytes(L.mlp_samples) : 0);
   L.oCons = take(sizeof(float) * (size_t)(prob->ncons > 0 ? prob->ncons : 0) * (1 + 2 * (size_t)D));
+  L.oRec = take(shard ? (size_t)shard_record_bytes(D) : 0);
   L.bytes = off;
   return L;
 }
@@ -204,6 +205,9 @@ static int swarm_setup(pps_swarm* s, const pps_problem* prob, int64_t n, uint64_
   if (L.mlp_samples) s->mlp_a_dev = b + L.oMlpA;
   s->dv.n = n;
   s->dv.npad = L.npad;
+  s->dv.first = 0;
+  s->dv.nglobal = n;
+  s->dv.xrec = nullptr;
   s->dv.dim = D;
   s->dv.ncons = prob->ncons > 0 ? prob->ncons : 0;
   s->dv.cons = s->dv.ncons ? reinterpret_cast<const float*>(b + L.oCons) : nullptr;
@@ -252,7 +256,11 @@ int swarm_attach(const pps_problem* prob, int64_t n, uint64_t seed, uint32_t fla
   if (!s) return set_error(PPS_ENOMEM, "host allocation failed");
   s->owns_memory = false;
   cudaGetDevice(&s->device);
-  cudaDeviceGetAttribute(&s->sm_count, cudaDevAttrMultiProcessorCount, s->device);
+  const cudaError_t ea = cudaDeviceGetAttribute(&s->sm_count, cudaDevAttrMultiProcessorCount, s->device);
+  if (ea != cudaSuccess) {
+    delete s;
+    return cuda_error(ea, "cudaDeviceGetAttribute(multiprocessor count)");
+  }
   s->stream = stream;
   if ((rc = swarm_setup(s, prob, n, seed, flags, static_cast<char*>(mem), swarm_layout(prob, n)))) {
     swarm_detach(s);
@@ -275,8 +283,14 @@ void swarm_detach(pps_swarm* s) {
 
 extern "C" {
 
-int pps_swarm_create(const pps_problem* prob, int64_t n, uint64_t seed, uint32_t flags,
-                     pps_swarm** out) {
+}  // extern "C"
+
+namespace pps {
+
+// pps_swarm_create, and for a shard (nglobal > 0) pps_shard_create: the
+// swarm holds n particles, particles first .. first + n - 1 of nglobal
+int swarm_create(const pps_problem* prob, int64_t n, uint64_t seed, uint32_t flags, int64_t first,
+                 int64_t nglobal, pps_swarm** out) {
   if (!out) return set_error(PPS_EINVAL, "out is NULL");
   *out = nullptr;
   int rc = swarm_check(prob, n);
@@ -286,8 +300,13 @@ int pps_swarm_create(const pps_problem* prob, int64_t n, uint64_t seed, uint32_t
   pps_swarm* s = new (std::nothrow) pps_swarm();
   if (!s) return set_error(PPS_ENOMEM, "host allocation failed");
   cudaGetDevice(&s->device);
-  cudaDeviceGetAttribute(&s->sm_count, cudaDevAttrMultiProcessorCount, s->device);
-  const SwarmLayout L = swarm_layout(prob, n);
+  cudaError_t ea = cudaDeviceGetAttribute(&s->sm_count, cudaDevAttrMultiProcessorCount, s->device);
+  if (ea != cudaSuccess) {
+    delete s;
+    return cuda_error(ea, "cudaDeviceGetAttribute(multiprocessor count)");
+  }
+  const bool shard = nglobal > 0;
+  const SwarmLayout L = swarm_layout(prob, n, shard);
   cudaError_t e = cudaMalloc(&s->block, L.bytes);
   if (e != cudaSuccess) {
     delete s;
@@ -304,6 +323,14 @@ int pps_swarm_create(const pps_problem* prob, int64_t n, uint64_t seed, uint32_t
       break;
     }
     if ((rc = swarm_setup(s, prob, n, seed, flags, static_cast<char*>(s->block), L))) break;
+    if (shard) {
+      s->shard = 1;
+      s->dv.first = first;
+      s->dv.nglobal = nglobal;
+      s->dv.xrec = static_cast<unsigned char*>(s->block) + L.oRec;
+      s->shard_records = s->dv.xrec;  // until pps_shard_bind: a lone shard exchanges with itself
+      s->shard_nrecords = 1;
+    }
     if ((e = cudaStreamSynchronize(s->stream)) != cudaSuccess) rc = cuda_error(e, "cudaStreamSynchronize");
   } while (0);
   if (rc) {
@@ -312,6 +339,15 @@ int pps_swarm_create(const pps_problem* prob, int64_t n, uint64_t seed, uint32_t
   }
   *out = s;
   return PPS_OK;
+}
+
+}  // namespace pps
+
+extern "C" {
+
+int pps_swarm_create(const pps_problem* prob, int64_t n, uint64_t seed, uint32_t flags,
+                     pps_swarm** out) {
+  return swarm_create(prob, n, seed, flags, 0, 0, out);
 }
 
 int pps_swarm_destroy(pps_swarm* s) {
@@ -398,6 +434,8 @@ int pps_swarm_info_get(pps_swarm* s, pps_swarm_info* info) {
 static int check_run(pps_swarm* s, int32_t maxiters, float w, float wdamp, float c1, float c2) {
   if (!s) return set_error(PPS_EINVAL, "swarm is NULL");
   if (!s->initialized) return set_error(PPS_EINVAL, "swarm is not initialised (call pps_swarm_init)");
+  if (s->shard)
+    return set_error(PPS_ENOTSUP, "a shard runs through pps_shard_step / pps_shard_async and the global-best exchange");
   if (maxiters < 0) return set_error(PPS_EINVAL, "maxiters must be >= 0");
   if (!std::isfinite(w) || !std::isfinite(wdamp) || !std::isfinite(c1) || !std::isfinite(c2))
     return set_error(PPS_EINVAL, "coefficients must be finite");

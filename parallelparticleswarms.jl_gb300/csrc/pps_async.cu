@@ -21,6 +21,7 @@
 #include <cuda_runtime.h>
 
 #include "pps_internal.h"
+#include "pps_publish.cuh"
 
 namespace pps {
 
@@ -61,6 +62,7 @@ __global__ void __launch_bounds__(kAsyncThreads) k_async(SwarmDev s, ObjParams o
   const int lane = (int)(gtid - i * lanes);
   const bool active = i < s.n;
   const int64_t il = active ? i : (s.n - 1);  // inactive threads mirror a real particle
+  const uint32_t gil = (uint32_t)(s.first + il);  // its index in the whole swarm (a shard's is offset)
   const int d0 = lane * slice;
   int cnt = D - d0;
   cnt = cnt < 0 ? 0 : (cnt > slice ? slice : cnt);
@@ -86,7 +88,7 @@ __global__ void __launch_bounds__(kAsyncThreads) k_async(SwarmDev s, ObjParams o
 #pragma unroll
     for (int k = 0; k < S; k += 2) {
       if (k < cnt) {
-        const Rand4 r = philox4x32_10((uint32_t)il, (uint32_t)((d0 + k) >> 1), t, kTagStep, keys);
+        const Rand4 r = philox4x32_10(gil, (uint32_t)((d0 + k) >> 1), t, kTagStep, keys);
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
           const int kk = k + h;
@@ -142,7 +144,7 @@ __global__ void __launch_bounds__(kAsyncThreads) k_async(SwarmDev s, ObjParams o
       s.flag[i] = 0;
     }
   }
-  unsigned long long key = (active && lane == 0) ? argmin_key(pc, (uint32_t)i) : ~0ull;
+  unsigned long long key = (active && lane == 0) ? argmin_key(pc, gil) : ~0ull;
 
   // block argmin + last-block publication of the final global best
   __shared__ unsigned long long wmin[32];
@@ -165,17 +167,8 @@ __global__ void __launch_bounds__(kAsyncThreads) k_async(SwarmDev s, ObjParams o
   __syncthreads();
   if (!last) return;
   __threadfence();
-  const unsigned long long bk = atomicAdd(&st->key, 0ull);
-  const uint32_t gi = (uint32_t)bk;
-  for (int d = threadIdx.x; d < D; d += blockDim.x) s.g[d] = __ldcg(s.P + (int64_t)d * s.npad + gi);
-  if (threadIdx.x == 0) {
-    st->gcost = __ldcg(s.pcost + gi);
-    st->gidx = gi;
-    st->key = ~0ull;
-    st->count = 0u;
-    st->t = t0 + (uint32_t)iters;
-    st->w = w;
-  }
+  // every flag is clear now, so the winner's vector is its personal best
+  finish_iteration(s, false, t0 + (uint32_t)iters, w);
 }
 
 int async_lanes(int dim, int* slice) {

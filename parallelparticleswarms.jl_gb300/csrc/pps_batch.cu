@@ -850,8 +850,11 @@ int pps_batch_create(pps_batch** out) {
   pps_batch* b = new (std::nothrow) pps_batch();
   if (!b) return set_error(PPS_ENOMEM, "host allocation failed");
   cudaGetDevice(&b->device);
-  cudaDeviceGetAttribute(&b->sm_count, cudaDevAttrMultiProcessorCount, b->device);
-  cudaError_t e;
+  cudaError_t e = cudaDeviceGetAttribute(&b->sm_count, cudaDevAttrMultiProcessorCount, b->device);
+  if (e != cudaSuccess) {
+    delete b;
+    return cuda_error(e, "cudaDeviceGetAttribute(multiprocessor count)");
+  }
   if ((e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking)) != cudaSuccess ||
       (e = cudaEventCreate(&b->ev0)) != cudaSuccess || (e = cudaEventCreate(&b->ev1)) != cudaSuccess) {
     pps_batch_destroy(b);

@@ -216,6 +216,7 @@ int run_local(pps_swarm* s, int kind, const pps_local_opts* opts, float* u_out, 
               float* device_ms) {
   if (!s) return set_error(PPS_EINVAL, "swarm is NULL");
   if (!s->initialized) return set_error(PPS_EINVAL, "swarm is not initialised");
+  if (s->shard) return set_error(PPS_ENOTSUP, "the local stage runs on a whole swarm, not on a shard");
   if (!opts) return set_error(PPS_EINVAL, "options are NULL");
   if (kind == 0 && (opts->history < 1 || opts->history > kMaxHistory))
     return set_error(PPS_EINVAL, "history must be in [1, %d] (got %d)", kMaxHistory, opts->history);

@@ -55,6 +55,9 @@ struct pps_swarm {
   bool owns_memory = true;    // false: device block and stream belong to a server
   int user_grid = 0;          // user objective: blocks of its step kernel (0: not resolved yet)
   const void* user_step_kernel = nullptr;  // user objective: the step kernel variant in use
+  int shard = 0;              // 1: a particle-range shard (pps_shard_create); dv.xrec is its exchange record
+  const unsigned char* shard_records = nullptr;  // shard: every shard's record after the exchange
+  int shard_nrecords = 0;
 };
 
 namespace pps {
@@ -109,6 +112,9 @@ int launch_publish_result(pps_swarm* s, float* mail, int* done);
 // array through pinned staging buffers, on stream (pps_api.cu)
 int copy_rows_to_host(int device, cudaStream_t stream, char* out, const char* dev, size_t src_pitch,
                       size_t row_bytes, size_t rows);
+// pps_swarm_create / pps_shard_create (pps_api.cu)
+int swarm_create(const pps_problem* prob, int64_t n, uint64_t seed, uint32_t flags, int64_t first, int64_t nglobal,
+                 pps_swarm** out);
 // argmin of pcost into the global best (pps_noalloc.cu)
 int launch_select_gbest(pps_swarm* s);
 // user objectives compiled at run time (pps_user.cu)

@@ -118,6 +118,7 @@ int pps_get_particles(pps_swarm* s, int32_t layout, float* out) {
 
 int pps_set_particles(pps_swarm* s, int32_t layout, const float* in) {
   if (!s || !in) return set_error(PPS_EINVAL, "NULL argument");
+  if (s->shard) return set_error(PPS_ENOTSUP, "the particles of a shard are set through pps_set_state");
   if (layout != PPS_LAYOUT_AOS && layout != PPS_LAYOUT_SOA) return set_error(PPS_EINVAL, "unknown layout %d", layout);
   const int D = s->dv.dim;
   const int64_t n = s->dv.n;

@@ -46,18 +46,30 @@ __device__ __forceinline__ bool publish_block_min(unsigned long long key, IterSt
 }
 
 // Last block: gather the winner into g, publish cost/index, reset the
-// argmin slot and advance (t, w).
+// argmin slot and advance (t, w).  A shard writes its winner to its exchange
+// record instead; the global best is then set by the exchange.
 __device__ __forceinline__ void finish_iteration(const SwarmDev& s, bool from_position,
                                                  uint32_t t_next, float w_next) {
   IterState* st = s.st;
   const unsigned long long key = atomicAdd(&st->key, 0ull);
-  const uint32_t gi = (uint32_t)key;
-  const bool use_x = from_position || (__ldcg(s.flag + gi) != 0);
+  const uint32_t gi = (uint32_t)key;                  // global particle index
+  const int64_t li = (int64_t)gi - s.first;           // its column in this swarm
+  const bool found = key != ~0ull;
+  const bool use_x = found && (from_position || (__ldcg(s.flag + li) != 0));
   const float* src = use_x ? s.X : s.P;
-  for (int d = threadIdx.x; d < s.dim; d += blockDim.x) s.g[d] = __ldcg(src + (int64_t)d * s.npad + gi);
+  float* dst = s.xrec ? reinterpret_cast<float*>(s.xrec + 16) : s.g;
+  if (found)
+    for (int d = threadIdx.x; d < s.dim; d += blockDim.x) dst[d] = __ldcg(src + (int64_t)d * s.npad + li);
   if (threadIdx.x == 0) {
-    st->gcost = __ldcg(s.pcost + gi);
-    st->gidx = gi;
+    const float c = found ? __ldcg(s.pcost + li) : __int_as_float(0x7f800000);
+    if (s.xrec) {
+      *reinterpret_cast<unsigned long long*>(s.xrec) = key;
+      reinterpret_cast<float*>(s.xrec)[2] = c;
+      reinterpret_cast<unsigned int*>(s.xrec)[3] = 0u;
+    } else {
+      st->gcost = c;
+      st->gidx = gi;
+    }
     st->key = ~0ull;
     st->count = 0u;
     st->tile_next = 0u;  // every block has taken its last tile

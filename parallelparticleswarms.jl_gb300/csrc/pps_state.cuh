@@ -47,6 +47,24 @@ struct SwarmDev {
   int dim;
   int ncons;          // constraints of the penalty path (0: none)
   const float* cons;  // ncons rows of (c_k, a_k[dim], b_k[dim])
+  // Particle-range shard of a larger swarm: local particle i is particle
+  // first + i of nglobal.  Random-stream counters, argmin keys and the
+  // penalty's particle index are global, so a shard's particles move exactly
+  // as they do in the whole swarm.  A whole swarm has first = 0, nglobal = n.
+  int64_t first;
+  int64_t nglobal;
+  // Shard: the last block of an init or step launch writes the shard's best
+  // particle to this exchange record instead of publishing it as the global
+  // best (nullptr: publish into g / gcost / gidx).
+  unsigned char* xrec;
 };
+
+// Exchange record of a shard (16-byte aligned, shard_record_bytes(dim) bytes):
+//   [0, 8)    argmin key of the shard's best particle: orderable cost << 32 | global index
+//   [8, 12)   its personal-best cost
+//   [12, 16)  zero
+//   [16, ...) its vector (dim floats): the position if it improved in the
+//             step that produced the record (or with the CPU-backend rule), else its personal best
+__host__ __device__ inline int64_t shard_record_bytes(int dim) { return (16 + 4 * (int64_t)dim + 15) / 16 * 16; }
 
 }  // namespace pps

@@ -40,11 +40,12 @@ __global__ void __launch_bounds__(kSyncThreads) k_init(SwarmDev s, ObjParams op,
   unsigned long long key = ~0ull;
   if (i < s.npad) {
     const bool valid = i < s.n;
+    const uint32_t gi = (uint32_t)(s.first + i);  // the particle's index in the whole swarm
     Acc<OBJ> acc;
     ConsAcc ca;
     if constexpr (CONS) ca.start(s.cons, s.ncons, D);
     for (int j = 0; j < D; j += 4) {
-      const Rand4 r = philox4x32_10((uint32_t)i, (uint32_t)(j >> 2), 0u, kTagInit, k0, k1);
+      const Rand4 r = philox4x32_10(gi, (uint32_t)(j >> 2), 0u, kTagInit, k0, k1);
       const uint32_t rr[4] = {r.a, r.b, r.c, r.d};
 #pragma unroll
       for (int h = 0; h < 4; ++h) {
@@ -57,7 +58,7 @@ __global__ void __launch_bounds__(kSyncThreads) k_init(SwarmDev s, ObjParams op,
           const float a = fabsf(z);
           x = (a > 0.0f) ? __fadd_rn(z, __fmul_rn(u, a)) : u;
         } else if (sampler == PPS_SAMPLER_LHS) {
-          x = valid ? lhs_position((uint32_t)i, (uint32_t)s.n, (uint32_t)d, u, s.lb[d], s.ub[d], k0, k1) : 0.0f;
+          x = valid ? lhs_position(gi, (uint32_t)s.nglobal, (uint32_t)d, u, s.lb[d], s.ub[d], k0, k1) : 0.0f;
         } else {
           const float lo = s.lb[d], hi = s.ub[d];
           x = __fadd_rn(__fmul_rn(u, __fsub_rn(hi, lo)), lo);  // rand(T) * (ub - lb) + lb
@@ -79,7 +80,7 @@ __global__ void __launch_bounds__(kSyncThreads) k_init(SwarmDev s, ObjParams op,
       s.cost[i] = c;
       s.pcost[i] = c;
       s.flag[i] = 0;
-      if (valid) key = argmin_key(c, (uint32_t)i);
+      if (valid) key = argmin_key(c, gi);
     }
   }
   // the MLP objective is evaluated (and published) by the tensor-core kernel
@@ -144,6 +145,7 @@ __global__ void __launch_bounds__(kSyncThreads, (PPT == 4 ? 2 : 4))
     // the barrier after it is not (every thread reaches the same barrier)
     if (q < ngroups) {
       const int64_t i0 = q * PPT;
+      const uint32_t gi0 = (uint32_t)(s.first + i0);  // index of particle i0 in the whole swarm
       uint8_t fl[PPT];
       ldflags<PPT>(fl, s.flag + i0);
       bool anyfl = false;
@@ -181,7 +183,7 @@ __global__ void __launch_bounds__(kSyncThreads, (PPT == 4 ? 2 : 4))
         }
         Rand4 r[PPT];
 #pragma unroll
-        for (int k = 0; k < PPT; ++k) r[k] = philox4x32_10((uint32_t)(i0 + k), (uint32_t)(j >> 1), t, kTagStep, keys);
+        for (int k = 0; k < PPT; ++k) r[k] = philox4x32_10(gi0 + (uint32_t)k, (uint32_t)(j >> 1), t, kTagStep, keys);
         {  // dim j
           const int64_t o = (int64_t)j * npad + i0;
           if (anyfl) {
@@ -229,13 +231,13 @@ __global__ void __launch_bounds__(kSyncThreads, (PPT == 4 ? 2 : 4))
 #pragma unroll
       for (int k = 0; k < PPT; ++k) {
         cc[k] = finalize<OBJ>(op, acc[k].s1, acc[k].s2);
-        if constexpr (CONS) cc[k] = __fadd_rn(cc[k], penalty(ca[k], s.ncons, __uint2float_rn((uint32_t)(i0 + k + 2))));
+        if constexpr (CONS) cc[k] = __fadd_rn(cc[k], penalty(ca[k], s.ncons, __uint2float_rn(gi0 + (uint32_t)(k + 2))));
         const bool valid = i0 + k < n;
         // if cost < best_cost: best = position (strict <, src/kernels.jl:21-24)
         fl[k] = (valid && cc[k] < pc[k]) ? 1 : 0;
         pc[k] = fl[k] ? cc[k] : pc[k];
         if (valid) {
-          const unsigned long long key = argmin_key(pc[k], (uint32_t)(i0 + k));
+          const unsigned long long key = argmin_key(pc[k], gi0 + (uint32_t)k);
           best = key < best ? key : best;
         }
       }

@@ -15,7 +15,8 @@ from .solve import (HybridPSOCache, OptimizationSolution, OptimizationStats, PSO
 from .swarm import Swarm
 from .batch import Batch
 from .serve import Server
-from . import mlp, ode
+from .shard import LocalShards, ShardedSwarm, shard_ranges
+from . import mlp, ode, shard
 
 __all__ = [
     "ParallelPSOKernel", "ParallelSyncPSOKernel", "ParallelPSOArray", "SerialPSO", "PSOAlgorithm", "HybridPSO",
@@ -27,5 +28,5 @@ __all__ = [
     "ArgumentError", "evaluate", "Objective", "REGISTRY", "sphere", "rosenbrock", "rastrigin", "ackley",
     "lotka_volterra_fit", "fitzhugh_nagumo_fit", "mlp_regression", "beale", "booth", "himmelblau",
     "quadratic", "boundary_quadratic", "shifted_sphere", "quadratic_constraint", "cuda_objective", "CUDA",
-    "Batch", "Server", "ode", "mlp",
+    "Batch", "Server", "ode", "mlp", "shard", "ShardedSwarm", "LocalShards", "shard_ranges",
 ]

@@ -181,6 +181,16 @@ _SIGNATURES = {
     "pps_hybrid_bfgs": (ctypes.c_int, [_P, ctypes.POINTER(LocalOpts), c_float_p, c_float_p,
                                        ctypes.POINTER(ctypes.c_int64), c_float_p]),
     "pps_objective_register": (ctypes.c_int, [ctypes.c_char_p, ctypes.POINTER(ctypes.c_int32)]),
+    "pps_shard_create": (ctypes.c_int, [ctypes.POINTER(Problem), ctypes.c_int64, ctypes.c_int64, ctypes.c_int64,
+                                        ctypes.c_uint64, ctypes.c_uint32, ctypes.POINTER(_P)]),
+    "pps_shard_record": (ctypes.c_int, [_P, ctypes.POINTER(_P), ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(_P)]),
+    "pps_shard_bind": (ctypes.c_int, [_P, _P, _P, ctypes.c_int32]),
+    "pps_shard_step": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                                      ctypes.c_float]),
+    "pps_shard_async": (ctypes.c_int, [_P, ctypes.c_int32, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                                       ctypes.c_float]),
+    "pps_shard_apply": (ctypes.c_int, [_P]),
+    "pps_shard_finish": (ctypes.c_int, [_P]),
     "pps_sync_run_noalloc": (ctypes.c_int, [ctypes.c_int32, c_float_p, ctypes.c_int32, ctypes.POINTER(DeviceSwarm),
                                             ctypes.c_uint64, ctypes.c_uint32, ctypes.c_int32, ctypes.c_float,
                                             ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_uint32,
