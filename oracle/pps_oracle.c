@@ -183,6 +183,36 @@ float orc_exp(float x) {
   return p * f_from_bits((uint32_t)(ki + 127) << 23);
 }
 
+/* ln x for the adaptive integrator's step-size controller: x = 2^e m, m in
+ * (sqrt(1/2), sqrt(2)], ln m = 2 atanh(s) = 2 (s + s^3/3 + ... + s^9/9) with
+ * s = (m - 1)/(m + 1), plus e ln 2 (the Cody-Waite split of orc_exp) */
+float orc_log(float x) {
+  if (!(x > 0.0f)) return (x == 0.0f) ? -INFINITY : NAN;
+  if (x == INFINITY) return x;
+  int e = 0;
+  if (x < 0x1p-126f) {
+    x = x * 0x1p+24f;
+    e = -24;
+  }
+  const uint32_t b = bits_from_f(x);
+  e += (int)(b >> 23) - 127;
+  float m = f_from_bits((b & 0x007fffffu) | 0x3f800000u);
+  if (m > 0x1.6a09e6p+0f) {
+    m = m * 0.5f;
+    e += 1;
+  }
+  const float sv = (m - 1.0f) / (m + 1.0f);
+  const float z = sv * sv;
+  float q = 0x1.c71c72p-3f;
+  q = fmaf(q, z, 0x1.249250p-2f);
+  q = fmaf(q, z, 0x1.99999ap-2f);
+  q = fmaf(q, z, 0x1.555556p-1f);
+  q = fmaf(q, z, 2.0f);
+  const float lm = sv * q;
+  const float ef = (float)e;
+  return fmaf(ef, EXP_LN2_HI, fmaf(ef, EXP_LN2_LO, lm));
+}
+
 /* orderable 32-bit image of a cost: NaN sorts above +inf */
 static inline uint32_t ord_cost(float c) {
   if (c != c) return 0xFFFFFFFFu;

@@ -206,10 +206,17 @@ typedef struct orc_ode_fit {
   int32_t nsaves;
   const float* data;   /* nsaves x 2, row major */
   float fixed[4];      /* fixed model constants (FHN: l) */
-  int32_t method;      /* ORC_ODE_RK4 (saves every save_every steps) or ORC_ODE_TSIT5 */
+  int32_t method;      /* ORC_ODE_RK4 (saves every save_every steps), ORC_ODE_TSIT5 or ORC_ODE_TSIT5_ADAPTIVE */
   float save_dt;       /* Tsit5: saves at m * save_dt from the continuous extension */
+  float rtol, atol;    /* adaptive Tsit5: tolerances of the step-size control; dt is the first step */
 } orc_ode_fit;
-enum { ORC_ODE_RK4 = 0, ORC_ODE_TSIT5 = 1 };
+enum { ORC_ODE_RK4 = 0, ORC_ODE_TSIT5 = 1, ORC_ODE_TSIT5_ADAPTIVE = 2 };
+/* adaptive Tsit5 (parameter_estim_ode!(..., Val(true)), src/ode_pso.jl:54-111):
+ * the SSE, and the steps taken (accepted + rejected; 100000 at most, after
+ * which, or when a step no longer advances t, the loss is +inf) */
+float orc_ode_loss_adaptive(const orc_ode_fit* f, const float* p, int32_t* steps);
+/* ln x of the step-size controller (the CUDA kernels' log_f, same bits) */
+float orc_log(float x);
 /* RK4 or Tsit5 integration + SSE against data (src/ode_pso.jl:47-52) */
 float orc_ode_loss(const orc_ode_fit* fit, const float* p);
 /* trajectory at the save points: out[nsaves*2] */

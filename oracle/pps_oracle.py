@@ -22,6 +22,7 @@ TAG_STEP = 0x50534F31
 SAMPLER_UNIFORM, SAMPLER_UNBOUNDED, SAMPLER_LHS = 0, 1, 2
 GBEST_FROM_PBEST, GBEST_FROM_POSITION = 0, 1
 ODE_LV, ODE_FHN = 0, 1
+ODE_RK4, ODE_TSIT5, ODE_TSIT5_ADAPTIVE = 0, 1, 2
 
 _fp = ctypes.POINTER(ctypes.c_float)
 
@@ -30,7 +31,8 @@ class OdeFit(ctypes.Structure):
     _fields_ = [("model", ctypes.c_int32), ("nparams", ctypes.c_int32), ("u0", ctypes.c_float * 2),
                 ("dt", ctypes.c_float), ("nsteps", ctypes.c_int32), ("save_every", ctypes.c_int32),
                 ("nsaves", ctypes.c_int32), ("data", _fp), ("fixed", ctypes.c_float * 4),
-                ("method", ctypes.c_int32), ("save_dt", ctypes.c_float)]
+                ("method", ctypes.c_int32), ("save_dt", ctypes.c_float), ("rtol", ctypes.c_float),
+                ("atol", ctypes.c_float)]
 
 
 USER_FN = ctypes.CFUNCTYPE(ctypes.c_float, _fp, ctypes.c_int, _fp, _fp, ctypes.c_longlong)
@@ -105,6 +107,10 @@ def load() -> ctypes.CDLL:
                                          _fp, _fp, ctypes.POINTER(ctypes.c_int32), ctypes.c_int32]
         L.orc_ode_loss.restype = ctypes.c_float
         L.orc_ode_loss.argtypes = [ctypes.POINTER(OdeFit), _fp]
+        L.orc_ode_loss_adaptive.restype = ctypes.c_float
+        L.orc_ode_loss_adaptive.argtypes = [ctypes.POINTER(OdeFit), _fp, ctypes.POINTER(ctypes.c_int32)]
+        L.orc_log.restype = ctypes.c_float
+        L.orc_log.argtypes = [ctypes.c_float]
         L.orc_ode_solve.argtypes = [ctypes.POINTER(OdeFit), _fp, _fp]
         L.orc_reduce_losses.argtypes = [ctypes.c_int32, ctypes.c_int32, ctypes.c_int64, _fp, _fp, _fp]
         L.orc_mlp_loss.restype = ctypes.c_double
@@ -205,7 +211,8 @@ class OracleProblem:
 
 class OracleOdeFit:
     def __init__(self, model: int, nparams: int, u0, dt: float, nsteps: int, save_every: int, data,
-                 fixed=(0.0, 0.0, 0.0, 0.0), method: int = 0, save_dt: float = 0.0):
+                 fixed=(0.0, 0.0, 0.0, 0.0), method: int = 0, save_dt: float = 0.0, rtol: float = 0.0,
+                 atol: float = 0.0):
         self.data = np.ascontiguousarray(np.asarray(data, np.float32).reshape(-1, 2))
         self.c = OdeFit()
         self.c.model, self.c.nparams = int(model), int(nparams)
@@ -216,10 +223,18 @@ class OracleOdeFit:
         for k, v in enumerate(fixed):
             self.c.fixed[k] = float(v)
         self.c.method, self.c.save_dt = int(method), float(save_dt)
+        self.c.rtol, self.c.atol = float(rtol), float(atol)
 
     def loss(self, p) -> float:
         p = np.ascontiguousarray(np.asarray(p, np.float32))
         return float(load().orc_ode_loss(ctypes.byref(self.c), fp(p)))
+
+    def loss_adaptive(self, p):
+        """(loss, steps taken) of the adaptive Tsit5 fit."""
+        p = np.ascontiguousarray(np.asarray(p, np.float32))
+        n = ctypes.c_int32()
+        f = load().orc_ode_loss_adaptive(ctypes.byref(self.c), fp(p), ctypes.byref(n))
+        return float(f), int(n.value)
 
     def solve(self, p) -> np.ndarray:
         p = np.ascontiguousarray(np.asarray(p, np.float32))
@@ -426,6 +441,10 @@ def ode_fit_problem(prob) -> OracleProblem:
     p = np.asarray(prob.p, np.float32)
     model = ODE_LV if prob.f.name == "lotka_volterra_fit" else ODE_FHN
     method, save_dt = (int(p[6]), float(p[7])) if p.size > 7 else (0, 0.0)
-    fit = OracleOdeFit(model, prob.dim, (p[0], p[1]), p[2], int(p[3]), int(p[4]), prob.data,
-                       fixed=(p[5], 0.0, 0.0, 0.0), method=method, save_dt=save_dt)
+    if method == ODE_TSIT5_ADAPTIVE:  # p[3], p[4] = reltol, abstol
+        fit = OracleOdeFit(model, prob.dim, (p[0], p[1]), p[2], 0, 0, prob.data, fixed=(p[5], 0.0, 0.0, 0.0),
+                           method=method, save_dt=save_dt, rtol=float(p[3]), atol=float(p[4]))
+    else:
+        fit = OracleOdeFit(model, prob.dim, (p[0], p[1]), p[2], int(p[3]), int(p[4]), prob.data,
+                           fixed=(p[5], 0.0, 0.0, 0.0), method=method, save_dt=save_dt)
     return OracleProblem(4 if model == ODE_LV else 5, prob.dim, prob.lb, prob.ub, ode=fit)

@@ -82,10 +82,16 @@ static const float R[7][3] = {{-2.763706197274826f, 2.9132554618219126f, -1.0530
                               {-27.896526289197286f, 65.09189467479366f, -34.87065786149661f},
                               {1.5f, -4.0f, 2.5f}};
 
-/* k[0] = f(u) on entry; k[0..6] the stages and (n0, n1) the new state on exit */
-static void tsit5_step(const orc_ode_fit* f, const float* p, float u0, float u1, float ka[7], float kb[7],
+/* error weights d_i = b_i - bhat_i of the embedded 4th-order solution (the
+ * minimum-norm weights satisfying the order-4 conditions, derived by
+ * tsit5_coefficients.py: the conditions leave one free parameter) */
+static const float D_ERR[7] = {0x1.44f608p-7f, 0x1.2a1940p-8f, -0x1.67af8ep-5f, 0x1.9cca80p-1f,
+                               -0x1.9f4bdcp+1f, 0x1.46ac0cp+1f, -0x1.59c28ep-4f};
+
+/* one step of size dt from (u0, u1); k[0] = f(u) on entry; k[0..6] the stages
+ * and (n0, n1) the new state on exit */
+static void tsit5_step(const orc_ode_fit* f, const float* p, float dt, float u0, float u1, float ka[7], float kb[7],
                        float* n0, float* n1) {
-  const float dt = f->dt;
   float sa, sb;
   sa = A21 * ka[0];
   sb = A21 * kb[0];
@@ -139,7 +145,7 @@ static float tsit5_run(const orc_ode_fit* f, const float* p, float* out) {
     const float tn = (float)n * dt;
     const float tn1 = (float)(n + 1) * dt;
     float n0, n1;
-    tsit5_step(f, p, u0, u1, ka, kb, &n0, &n1);
+    tsit5_step(f, p, dt, u0, u1, ka, kb, &n0, &n1);
     while (m < f->nsaves && tm <= tn1) {
       const float th = (tm - tn) / dt;
       const float y0 = tsit5_dense(u0, dt, th, ka), y1 = tsit5_dense(u1, dt, th, kb);
@@ -161,9 +167,107 @@ static float tsit5_run(const orc_ode_fit* f, const float* p, float* out) {
   return acc;
 }
 
+/* ---- adaptive Tsit5 (parameter_estim_ode!(..., Val(true)), src/ode_pso.jl:54-111,
+ * DiffEqGPU's vectorized_asolve) restated from the published methods:
+ *   E = h sum_i d_i k_i, err = sqrt(((E_1/sc_1)^2 + (E_2/sc_2)^2) / 2),
+ *   sc = abstol + reltol max(|u_n|, |u_n+1|) (Hairer, Norsett & Wanner, Solving
+ *   ODEs I, sec. II.4, eq. 4.11); accepted when err <= 1; next step h fac with
+ *   the PI controller of that section (Gustafsson): fac = 0.9 err^-0.17
+ *   err_old^0.04 in [0.2, 10] (at most 1 after a rejection), err_old =
+ *   max(err, 1e-4); a rejection retries with h max(0.2, 0.9 err^-1/5); the
+ *   last step ends at t_end = (nsaves - 1) save_dt exactly; saves inside an
+ *   accepted step from the continuous extension; 100000 steps at most, and a
+ *   step that no longer advances t, give +inf.  Same binary32 operations as
+ *   the CUDA kernel (tsit5a_loss). */
+static float err_sum(const float k[7]) {
+  float s = D_ERR[0] * k[0];
+  for (int i = 1; i < 7; ++i) s = fmaf(D_ERR[i], k[i], s);
+  return s;
+}
+
+static float tsit5a_run(const orc_ode_fit* f, const float* p, float* out, int32_t* steps) {
+  const float inf = INFINITY;
+  float u0 = f->u0[0], u1 = f->u0[1];
+  float acc = 0.0f;
+  if (out) {
+    out[0] = u0;
+    out[1] = u1;
+  } else {
+    const float e0 = f->data[0] - u0, e1 = f->data[1] - u1;
+    acc = (e0 * e0) + (e1 * e1);
+  }
+  const float tend = (float)(f->nsaves - 1) * f->save_dt;
+  float ka[7], kb[7];
+  rhs(f, p, u0, u1, &ka[0], &kb[0]);
+  float t = 0.0f, h = f->dt, errold = 1e-4f;
+  int rejected = 0, m = 1, n = 0;
+  float tm = f->save_dt;
+  for (; m < f->nsaves; ++n) {
+    if (n >= 100000) {
+      acc = inf;
+      break;
+    }
+    const float rem = tend - t;
+    const int last = h >= rem;
+    const float hh = last ? rem : h;
+    const float tn1 = last ? tend : t + hh;
+    if (!(tn1 > t)) {
+      acc = inf;
+      break;
+    }
+    float n0, n1;
+    tsit5_step(f, p, hh, u0, u1, ka, kb, &n0, &n1);
+    const float ea = hh * err_sum(ka), eb = hh * err_sum(kb);
+    const float sa = fmaf(f->rtol, fmaxf(fabsf(u0), fabsf(n0)), f->atol);
+    const float sb = fmaf(f->rtol, fmaxf(fabsf(u1), fabsf(n1)), f->atol);
+    const float ra = ea / sa, rb = eb / sb;
+    const float err = sqrtf(fmaf(ra, ra, rb * rb) * 0.5f);
+    if (err <= 1.0f) {
+      while (m < f->nsaves && tm <= tn1) {
+        const float th = (tm - t) / hh;
+        const float y0 = tsit5_dense(u0, hh, th, ka), y1 = tsit5_dense(u1, hh, th, kb);
+        if (out) {
+          out[2 * m] = y0;
+          out[2 * m + 1] = y1;
+        } else {
+          const float e0 = f->data[2 * m] - y0, e1 = f->data[2 * m + 1] - y1;
+          acc = acc + ((e0 * e0) + (e1 * e1));
+        }
+        ++m;
+        tm = (float)m * f->save_dt;
+      }
+      t = tn1;
+      u0 = n0;
+      u1 = n1;
+      ka[0] = ka[6];
+      kb[0] = kb[6];
+      float fac = 10.0f;
+      if (err > 0.0f) fac = 0.9f * orc_exp(fmaf(0.04f, orc_log(errold), -0.17f * orc_log(err)));
+      fac = fminf(rejected ? 1.0f : 10.0f, fmaxf(0.2f, fac));
+      errold = fmaxf(err, 1e-4f);
+      h = hh * fac;
+      rejected = 0;
+    } else {
+      const float fac = fmaxf(0.2f, 0.9f * orc_exp(-0.2f * orc_log(err)));
+      h = hh * fac;
+      rejected = 1;
+    }
+  }
+  if (steps) *steps = n;
+  return acc;
+}
+
+float orc_ode_loss_adaptive(const orc_ode_fit* f, const float* p, int32_t* steps) {
+  return tsit5a_run(f, p, NULL, steps);
+}
+
 void orc_ode_solve(const orc_ode_fit* f, const float* p, float* out) {
   if (f->method == ORC_ODE_TSIT5) {
     tsit5_run(f, p, out);
+    return;
+  }
+  if (f->method == ORC_ODE_TSIT5_ADAPTIVE) {
+    tsit5a_run(f, p, out, NULL);
     return;
   }
   float u0 = f->u0[0], u1 = f->u0[1];
@@ -182,6 +286,7 @@ void orc_ode_solve(const orc_ode_fit* f, const float* p, float* out) {
 
 float orc_ode_loss(const orc_ode_fit* f, const float* p) {
   if (f->method == ORC_ODE_TSIT5) return tsit5_run(f, p, NULL);
+  if (f->method == ORC_ODE_TSIT5_ADAPTIVE) return tsit5a_run(f, p, NULL, NULL);
   float u0 = f->u0[0], u1 = f->u0[1];
   float d0 = f->data[0] - u0, d1 = f->data[1] - u1;
   float acc = (d0 * d0) + (d1 * d1);

@@ -47,6 +47,38 @@ LITERALS_R = np.array([
 ])
 
 
+# the error-estimate weights as compiled: d_i = b_i - bhat_i (i = 1..7), binary32
+LITERALS_D = ["0x1.44f608p-7", "0x1.2a1940p-8", "-0x1.67af8ep-5", "0x1.9cca80p-1", "-0x1.9f4bdcp+1",
+              "0x1.46ac0cp+1", "-0x1.59c28ep-4"]
+
+
+def order4_conditions() -> tuple[np.ndarray, np.ndarray]:
+    """Rows phi with rhs 1/gamma: the 8 order conditions up to order 4, as
+    linear conditions on a weight vector."""
+    c, Ac = C, A @ C
+    trees = [(np.ones(7), 1), (c, 2), (c ** 2, 3), (Ac, 6), (c ** 3, 4), (c * Ac, 8), (A @ c ** 2, 12),
+             (A @ Ac, 24)]
+    return np.array([t for t, _ in trees]), np.array([1 / g for _, g in trees])
+
+
+def derive_embedded() -> np.ndarray:
+    """The embedded 4th-order weights bhat and the error weights d = b - bhat.
+
+    On this pair's nodes the 8 order-4 conditions have rank 6 over the 7
+    weights, so the embedded 4th-order solutions form a one-parameter family
+    b + s n (n spans the null space; b itself satisfies them); every member
+    gives an error estimate dt sum_i d_i k_i along the same direction, only
+    its size changes with s.  This build takes the member of least Euclidean
+    norm (the minimum-norm solution of the conditions), a choice of its own:
+    DiffEqGPU's embedded weights are not vendored, so the adaptive step sizes
+    are not pinned to the reference's."""
+    M, r = order4_conditions()
+    assert np.linalg.matrix_rank(M) == 6
+    bhat = np.linalg.pinv(M) @ r
+    assert np.abs(M @ bhat - r).max() < 1e-12
+    return B - bhat
+
+
 def order5_residuals() -> dict:
     b, c, Ac = B, C, A @ C
     t = {
@@ -102,3 +134,5 @@ if __name__ == "__main__":
     np.set_printoptions(precision=16)
     print("derived interpolant (r_i2, r_i3, r_i4):\n", R)
     print("max |derived - literals|", np.abs(R - LITERALS_R).max())
+    d = derive_embedded()
+    print("error weights d = b - bhat (binary32):", [float(np.float32(v)).hex() for v in d])

@@ -254,6 +254,39 @@ __device__ __forceinline__ float exp_f(float x) {
   return __fmul_rn(p, __int_as_float((ki + 127) << 23));
 }
 
+// ln(x) for the adaptive integrators' step-size controller, this project's own
+// (identical bits in the oracle's orc_log): x = 2^e m with m in (sqrt(1/2),
+// sqrt(2)], ln m = 2 atanh(s) = 2 (s + s^3/3 + ... + s^9/9), s = (m-1)/(m+1)
+// (|s| <= 0.1716, the series' remainder below 2^-28), plus e ln 2 with the
+// Cody-Waite split of exp_f.  x <= 0 or NaN gives NaN, 0 -inf, +inf +inf;
+// subnormal x is scaled into the normal range first.
+__device__ __forceinline__ float log_f(float x) {
+  if (!(x > 0.0f)) return (x == 0.0f) ? __int_as_float(0xff800000) : __int_as_float(0x7fc00000);
+  if (x == __int_as_float(0x7f800000)) return x;
+  int e = 0;
+  if (x < 0x1p-126f) {
+    x = __fmul_rn(x, 0x1p+24f);
+    e = -24;
+  }
+  const int b = __float_as_int(x);
+  e += (b >> 23) - 127;
+  float m = __int_as_float((b & 0x007fffff) | 0x3f800000);
+  if (m > 0x1.6a09e6p+0f) {
+    m = __fmul_rn(m, 0.5f);
+    e += 1;
+  }
+  const float sv = __fdiv_rn(__fsub_rn(m, 1.0f), __fadd_rn(m, 1.0f));
+  const float z = __fmul_rn(sv, sv);
+  float q = 0x1.c71c72p-3f;          // 2/9
+  q = __fmaf_rn(q, z, 0x1.249250p-2f);  // 2/7
+  q = __fmaf_rn(q, z, 0x1.99999ap-2f);  // 2/5
+  q = __fmaf_rn(q, z, 0x1.555556p-1f);  // 2/3
+  q = __fmaf_rn(q, z, 2.0f);
+  const float lm = __fmul_rn(sv, q);
+  const float ef = __int2float_rn(e);
+  return __fmaf_rn(ef, 0x1.62e430p-1f, __fmaf_rn(ef, -0x1.05c610p-29f, lm));
+}
+
 // ---------------------------------------------------------------- constraints
 // calc_penalty (src/utils.jl:320-372) for the registered constraint form
 // g_k(x) = c_k + sum_i a_ki x_i + b_ki x_i^2 (rows of `cons`: c_k, a_k[dim],

@@ -63,6 +63,7 @@ constexpr uint32_t kMlpTmemCols = 2 * kMlpN;  // two accumulator buffers
 constexpr size_t kMlpATileBytes = 128 * kMlpIn * 2;  // 4 KB per 128 samples
 constexpr size_t kMlpBBytes = (size_t)kMlpN * kMlpIn * 2;  // 8 KB
 constexpr uint64_t kMlpWaitNs = 2000000000ull;
+constexpr int kMlpFmaUnitsDefault = 4;  // hidden units (of 32) whose tanh runs on the FP32 pipe
 
 // ---------------------------------------------------------------- PTX helpers
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -162,6 +163,35 @@ __device__ __forceinline__ float tanh_fast(float x) {
   float y;
   asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
   return y;
+}
+
+// tanh on the FP32 pipe (no special-function instruction): x P(x^2) / Q(x^2)
+// on |x| <= kTanhClamp, a rational fit of this project's own
+// (tanh_coefficients.py: least maximum error, Loeb's linearisation with
+// Lawson's reweighting), the argument clamped beyond; 1 / Q from a seed taken
+// from the bits (kRcpMagic - bits(Q)) refined by one Newton and one
+// third-order step.  Maximum absolute error 1.6e-5 over all finite x (the
+// special-function tanh.approx.f32 has relative error up to about 2^-11).
+// 16 FP32/ALU instructions.
+constexpr float kTanhClamp = 0x1.900000p+2f;  // 6.25
+constexpr float kTanhA0 = 0x1.fffb1ep-1f, kTanhA1 = 0x1.d2ccf0p-4f, kTanhA2 = 0x1.7fcdecp-10f;
+constexpr float kTanhB1 = 0x1.c9ea3ep-2f, kTanhB2 = 0x1.1b6c34p-6f, kTanhB3 = 0x1.be8a44p-15f;
+constexpr int kRcpMagic = 0x7EF311C2;
+__device__ __forceinline__ float tanh_fma(float h) {
+  const float x = fminf(fmaxf(h, -kTanhClamp), kTanhClamp);
+  const float z = __fmul_rn(x, x);
+  float p = __fmaf_rn(kTanhA2, z, kTanhA1);
+  p = __fmaf_rn(p, z, kTanhA0);
+  p = __fmul_rn(p, x);
+  float q = __fmaf_rn(kTanhB3, z, kTanhB2);
+  q = __fmaf_rn(q, z, kTanhB1);
+  q = __fmaf_rn(q, z, 1.0f);
+  float y = __int_as_float(kRcpMagic - __float_as_int(q));
+  float e = __fmaf_rn(-q, y, 1.0f);
+  y = __fmaf_rn(y, e, y);
+  e = __fmaf_rn(-q, y, 1.0f);
+  y = __fmaf_rn(y, __fmaf_rn(e, e, e), y);
+  return __fmul_rn(p, y);
 }
 __device__ __forceinline__ uint16_t bf16_bits(float v) {
   return __bfloat16_as_ushort(__float2bfloat16_rn(v));
@@ -283,7 +313,11 @@ __device__ __forceinline__ void pair_put(int e, const PairLoad& L, uint8_t* sB, 
   if (d0 + 1 < kMlpDim) put_param(p, d0 + 1, L.x1, sB, sBb, sW2);
 }
 
-template <int MODE>
+// NF: hidden units (of 32) whose tanh runs on the FP32 pipe (tanh_fma), the
+// rest on the special-function pipe (tanh.approx.f32); every mode of a
+// process uses the same split, so a point's loss is the same in init, step
+// and evaluation.
+template <int MODE, int NF>
 __global__ void __launch_bounds__(kMlpThreads, 1) k_mlp_eval(SwarmDev s, MlpArgs a) {
   constexpr bool MOVE = MODE == 1;
   extern __shared__ __align__(1024) uint8_t smem[];
@@ -443,13 +477,17 @@ __global__ void __launch_bounds__(kMlpThreads, 1) k_mlp_eval(SwarmDev s, MlpArgs
         }
         const float* w2 = w2base + pp * kMlpW2Stride;
         float o = w2[32];  // b2
+        // units j with (j % 8) < NF / 4 use the FP32 pipe: spread over the sum
 #pragma unroll
         for (int j = 0; j < kMlpHidden; j += 4) {
           const float4 ww = *reinterpret_cast<const float4*>(w2 + j);
-          o = __fmaf_rn(ww.x, tanh_fast(v[j]), o);
-          o = __fmaf_rn(ww.y, tanh_fast(v[j + 1]), o);
-          o = __fmaf_rn(ww.z, tanh_fast(v[j + 2]), o);
-          o = __fmaf_rn(ww.w, tanh_fast(v[j + 3]), o);
+          const float wj[4] = {ww.x, ww.y, ww.z, ww.w};
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            const int jj = j + u;
+            const float th = ((jj & 7) < NF / 4) ? tanh_fma(v[jj]) : tanh_fast(v[jj]);
+            o = __fmaf_rn(wj[u], th, o);
+          }
         }
         const float err = __fsub_rn(o, ys);
         acc[pp] = __fmaf_rn(err, err, acc[pp]);
@@ -598,17 +636,40 @@ static int mlp_set_smem_limit() {
   std::lock_guard<std::mutex> lock(mu);
   if (done[dev]) return PPS_OK;
   const int smem = (int)mlp_smem(kMlpMaxSamples);
-  PPS_CUDA(cudaFuncSetAttribute(k_mlp_eval<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-  PPS_CUDA(cudaFuncSetAttribute(k_mlp_eval<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-  PPS_CUDA(cudaFuncSetAttribute(k_mlp_eval<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+#define PPS_MLP_SMEM(NF)                                                                               \
+  PPS_CUDA(cudaFuncSetAttribute(k_mlp_eval<0, NF>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)); \
+  PPS_CUDA(cudaFuncSetAttribute(k_mlp_eval<1, NF>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)); \
+  PPS_CUDA(cudaFuncSetAttribute(k_mlp_eval<2, NF>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem))
+  PPS_MLP_SMEM(0);
+  PPS_MLP_SMEM(4);
+  PPS_MLP_SMEM(8);
+  PPS_MLP_SMEM(12);
+#undef PPS_MLP_SMEM
   done[dev] = true;
   return PPS_OK;
+}
+
+// hidden units per 32 on the FP32 pipe: PPS_MLP_FMA_TANH = 0, 4, 8 or 12
+// overrides the default (every split computes the same network; the loss
+// differs only by the two tanh approximations' errors)
+static int mlp_fma_units() {
+  static int nf = [] {
+    const char* e = getenv("PPS_MLP_FMA_TANH");
+    const int v = e ? atoi(e) : kMlpFmaUnitsDefault;
+    return (v == 0 || v == 4 || v == 8 || v == 12) ? v : kMlpFmaUnitsDefault;
+  }();
+  return nf;
 }
 
 template <int MODE>
 static int launch_mlp(const SwarmDev& dv, const MlpArgs& a, int grid, cudaStream_t stream) {
   const size_t smem = mlp_smem(a.S);
-  k_mlp_eval<MODE><<<grid, kMlpThreads, smem, stream>>>(dv, a);
+  switch (mlp_fma_units()) {
+    case 4: k_mlp_eval<MODE, 4><<<grid, kMlpThreads, smem, stream>>>(dv, a); break;
+    case 8: k_mlp_eval<MODE, 8><<<grid, kMlpThreads, smem, stream>>>(dv, a); break;
+    case 12: k_mlp_eval<MODE, 12><<<grid, kMlpThreads, smem, stream>>>(dv, a); break;
+    default: k_mlp_eval<MODE, 0><<<grid, kMlpThreads, smem, stream>>>(dv, a); break;
+  }
   PPS_CUDA(cudaGetLastError());
   return PPS_OK;
 }

@@ -26,6 +26,7 @@ constexpr int kOdeMaxDim = 4;
 template <int MODEL, int METHOD>
 __device__ __forceinline__ float ode_eval(const float (&x)[kOdeMaxDim], const OdeCfg& c, const float* data) {
   if constexpr (METHOD == kOdeTsit5) return tsit5_loss<MODEL>(x, c, data);
+  else if constexpr (METHOD == kOdeTsit5Adaptive) return tsit5a_loss<MODEL>(x, c, data);
   else return ode_loss<MODEL>(x, c, data);
 }
 
@@ -139,6 +140,9 @@ __global__ void __launch_bounds__(kOdeThreads) k_sync_step_ode(SwarmDev s, ObjPa
     const bool lv_ = (obj) == kLvFit;                                     \
     if ((method) == kOdeTsit5) {                                          \
       if (lv_) MACRO(kOdeLV, kOdeTsit5); else MACRO(kOdeFHN, kOdeTsit5);  \
+    } else if ((method) == kOdeTsit5Adaptive) {                           \
+      if (lv_) MACRO(kOdeLV, kOdeTsit5Adaptive);                          \
+      else MACRO(kOdeFHN, kOdeTsit5Adaptive);                             \
     } else {                                                              \
       if (lv_) MACRO(kOdeLV, kOdeRk4); else MACRO(kOdeFHN, kOdeRk4);      \
     }                                                                     \
@@ -155,15 +159,26 @@ int ode_check(const pps_problem* prob) {
     return set_error(PPS_EINVAL, "ODE fits take params = [u0_1, u0_2, dt, nsteps, save_every(, l)]");
   if (prob->objective == kFhnFit && prob->dim == 3 && prob->nparams < 6)
     return set_error(PPS_EINVAL, "the FitzHugh-Nagumo fit of 3 parameters needs params[5] = l");
+  if (!prob->data || prob->ndata < 2 || (prob->ndata & 1) || prob->ndata / 2 > kOdeMaxSaves)
+    return set_error(PPS_EINVAL, "ODE fit needs data of 2 * nsaves floats, 1 <= nsaves <= %d", kOdeMaxSaves);
+  const float method = prob->nparams > 6 ? prob->params[6] : 0.0f;
+  if (method != (float)kOdeRk4 && method != (float)kOdeTsit5 && method != (float)kOdeTsit5Adaptive)
+    return set_error(PPS_EINVAL, "ODE fit: params[6] (method) is 0 (RK4), 1 (Tsit5) or 2 (adaptive Tsit5)");
+  if (method == (float)kOdeTsit5Adaptive) {
+    // params = [u0_1, u0_2, dt (first step), reltol, abstol, l, 2, save_dt]
+    const float dt0 = prob->params[2], rtol = prob->params[3], atol = prob->params[4];
+    const float save_dt = prob->nparams > 7 ? prob->params[7] : 0.0f;
+    if (!(dt0 > 0.0f) || !std::isfinite(dt0) || !(rtol > 0.0f) || !std::isfinite(rtol) || !(atol > 0.0f) ||
+        !std::isfinite(atol))
+      return set_error(PPS_EINVAL, "adaptive Tsit5 needs a first step dt > 0, reltol > 0 and abstol > 0 (finite)");
+    if (!(save_dt > 0.0f) || !std::isfinite(save_dt) || !std::isfinite((prob->ndata / 2 - 1) * save_dt))
+      return set_error(PPS_EINVAL, "ODE fit with Tsit5 needs params[7] = save_dt > 0");
+    return PPS_OK;
+  }
   const float nsteps = prob->params[3], every = prob->params[4];
   if (!(prob->params[2] > 0.0f) || !(nsteps >= 1.0f) || !(every >= 1.0f) || nsteps != (float)(int)nsteps ||
       every != (float)(int)every)
     return set_error(PPS_EINVAL, "ODE fit needs dt > 0 and integral nsteps, save_every >= 1");
-  if (!prob->data || prob->ndata < 2 || (prob->ndata & 1) || prob->ndata / 2 > kOdeMaxSaves)
-    return set_error(PPS_EINVAL, "ODE fit needs data of 2 * nsaves floats, 1 <= nsaves <= %d", kOdeMaxSaves);
-  const float method = prob->nparams > 6 ? prob->params[6] : 0.0f;
-  if (method != (float)kOdeRk4 && method != (float)kOdeTsit5)
-    return set_error(PPS_EINVAL, "ODE fit: params[6] (method) is 0 (RK4) or 1 (Tsit5)");
   if (method == (float)kOdeTsit5) {
     const float save_dt = prob->nparams > 7 ? prob->params[7] : 0.0f;
     if (!(save_dt > 0.0f) || !std::isfinite(save_dt))

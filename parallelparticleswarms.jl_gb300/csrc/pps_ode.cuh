@@ -32,17 +32,23 @@ constexpr int kOdeFHN = 1;
 constexpr int kOdeMaxSaves = 4096;
 constexpr int kOdeRk4 = 0;
 constexpr int kOdeTsit5 = 1;
+constexpr int kOdeTsit5Adaptive = 2;
+constexpr int kOdeMaxSteps = 100000;  // accepted + rejected steps per adaptive solve (then the loss is +inf)
 
 // Fit configuration, packed by the host from pps_problem.params:
 // params = [u0_1, u0_2, dt, nsteps, save_every, l (FHN), method, save_dt],
 // data = nsaves x 2 (t = 0 included).  method 0 (default): RK4, a save every
-// save_every steps; 1: Tsit5, saves at m * save_dt.
+// save_every steps; 1: Tsit5 at a fixed step, saves at m * save_dt; 2: Tsit5
+// with adaptive steps from dt, saves at m * save_dt up to (nsaves - 1)
+// save_dt, params[3] = reltol and params[4] = abstol in place of nsteps and
+// save_every.
 struct OdeCfg {
   float u0a, u0b, dt, l;
   int nsteps, save_every, nsaves;
   int method;
   float save_dt;
   int dim;  // FHN: 3 fits (a, b, tinv) with l fixed, 4 fits l as well
+  float rtol, atol;  // method 2
 };
 
 __host__ __device__ inline OdeCfg ode_cfg(const ObjParams& op, int64_t ndata) {
@@ -57,6 +63,9 @@ __host__ __device__ inline OdeCfg ode_cfg(const ObjParams& op, int64_t ndata) {
   c.method = op.np > 6 ? (int)op.p[6] : kOdeRk4;
   c.save_dt = op.np > 7 ? op.p[7] : 0.0f;
   c.dim = op.dim;
+  c.rtol = op.p[3];
+  c.atol = op.p[4];
+  if (c.method == kOdeTsit5Adaptive) c.nsteps = c.save_every = 0;
   return c;
 }
 
@@ -140,6 +149,11 @@ constexpr float r42 = -12.411077166933676f, r43 = 30.33818863028232f, r44 = -16.
 constexpr float r52 = 37.50931341651104f, r53 = -88.1789048947664f, r54 = 47.37952196281928f;
 constexpr float r62 = -27.896526289197286f, r63 = 65.09189467479366f, r64 = -34.87065786149661f;
 constexpr float r72 = 1.5f, r73 = -4.0f, r74 = 2.5f;
+// error weights d_i = b_i - bhat_i of the embedded 4th-order solution: the
+// minimum-norm weights satisfying the order-4 conditions, derived by
+// oracle/tsit5_coefficients.py (the conditions leave one free parameter)
+constexpr float d1 = 0x1.44f608p-7f, d2 = 0x1.2a1940p-8f, d3 = -0x1.67af8ep-5f, d4 = 0x1.9cca80p-1f,
+                d5 = -0x1.9f4bdcp+1f, d6 = 0x1.46ac0cp+1f, d7 = -0x1.59c28ep-4f;
 }  // namespace ts5
 
 // One step from u with k[0] = f(u) on entry; on exit k[0..6] are the seven
@@ -226,6 +240,107 @@ __device__ __forceinline__ float tsit5_loss(const float* p, const OdeCfg& c, con
     ka[0] = ka[6];
     kb[0] = kb[6];
   }
+  return acc;
+}
+
+// ---------------------------------------------------------------- adaptive Tsit5
+// The reference's parameter_estim_ode!(..., Val(true)) integrates with
+// DiffEqGPU's vectorized_asolve (src/ode_pso.jl:54-111): adaptive steps,
+// saves interpolated.  Restated from the published methods:
+//   - local error estimate E = h sum_i d_i k_i of the embedded 4th-order
+//     solution (d above), measured as err = sqrt(((E_1/sc_1)^2 + (E_2/sc_2)^2) / 2)
+//     with sc = abstol + reltol max(|u_n|, |u_n+1|) (Hairer, Norsett & Wanner,
+//     Solving ODEs I, sec. II.4, eq. 4.11);
+//   - step accepted when err <= 1; the next step h fac with the stabilised
+//     (PI) controller of the same section (Gustafsson's): fac = 0.9 err^-alpha
+//     err_old^beta, beta = 0.04, alpha = 1/5 - 0.75 beta, clamped to [0.2, 10]
+//     (at most 1 right after a rejection), err_old = max(err, 1e-4) of the last
+//     accepted step (1e-4 at the start); a rejected step retries with
+//     h max(0.2, 0.9 err^-1/5);
+//   - the last step ends exactly at t_end = (nsaves - 1) save_dt; saves inside
+//     an accepted step come from the continuous extension, as at a fixed step;
+//   - at most kOdeMaxSteps steps, and a step that no longer advances t, give
+//     a loss of +inf (a solve that did not finish).
+// err^-alpha is exp_f(-alpha log_f(err)) (both this project's own), so the
+// oracle reproduces every step size bit for bit.
+constexpr float kCtlBeta = 0.04f, kCtlAlpha = 0.17f, kCtlSafe = 0.9f;
+constexpr float kCtlFacMin = 0.2f, kCtlFacMax = 10.0f, kCtlErrMin = 1e-4f;
+
+__device__ __forceinline__ float tsit5_err_sum(const float (&k)[7]) {
+  using namespace ts5;
+  float s = __fmul_rn(d1, k[0]);
+  s = __fmaf_rn(d2, k[1], s);
+  s = __fmaf_rn(d3, k[2], s);
+  s = __fmaf_rn(d4, k[3], s);
+  s = __fmaf_rn(d5, k[4], s);
+  s = __fmaf_rn(d6, k[5], s);
+  return __fmaf_rn(d7, k[6], s);
+}
+
+// SSE of the adaptive Tsit5 solution at t_m = m save_dt against data; steps
+// (accepted and rejected) in *steps when given
+template <int MODEL>
+__device__ __forceinline__ float tsit5a_loss(const float* p, const OdeCfg& c, const float* data, int* steps = nullptr) {
+  const float inf = __int_as_float(0x7f800000);
+  float u0 = c.u0a, u1 = c.u0b;
+  float e0 = __fsub_rn(data[0], u0), e1 = __fsub_rn(data[1], u1);
+  float acc = __fadd_rn(__fmul_rn(e0, e0), __fmul_rn(e1, e1));
+  const float l = ode_l(p, c);
+  const float tend = __fmul_rn(__int2float_rn(c.nsaves - 1), c.save_dt);
+  float ka[7], kb[7];
+  ode_rhs<MODEL>(p, l, u0, u1, ka[0], kb[0]);
+  float t = 0.0f, h = c.dt, errold = kCtlErrMin;
+  bool rejected = false;
+  int m = 1, n = 0;
+  float tm = c.save_dt;
+  for (; m < c.nsaves; ++n) {
+    if (n >= kOdeMaxSteps) {
+      acc = inf;
+      break;
+    }
+    const float rem = __fsub_rn(tend, t);
+    const bool last = h >= rem;
+    const float hh = last ? rem : h;
+    const float tn1 = last ? tend : __fadd_rn(t, hh);
+    if (!(tn1 > t)) {  // the step no longer advances t
+      acc = inf;
+      break;
+    }
+    float n0, n1;
+    tsit5_step<MODEL>(p, l, hh, u0, u1, ka, kb, n0, n1);
+    const float ea = __fmul_rn(hh, tsit5_err_sum(ka)), eb = __fmul_rn(hh, tsit5_err_sum(kb));
+    const float sa = __fmaf_rn(c.rtol, fmaxf(fabsf(u0), fabsf(n0)), c.atol);
+    const float sb = __fmaf_rn(c.rtol, fmaxf(fabsf(u1), fabsf(n1)), c.atol);
+    const float ra = __fdiv_rn(ea, sa), rb = __fdiv_rn(eb, sb);
+    const float err = __fsqrt_rn(__fmul_rn(__fmaf_rn(ra, ra, __fmul_rn(rb, rb)), 0.5f));
+    if (err <= 1.0f) {
+      while (m < c.nsaves && tm <= tn1) {  // the saves inside (t, t + hh]
+        const float th = __fdiv_rn(__fsub_rn(tm, t), hh);
+        e0 = __fsub_rn(data[2 * m], tsit5_dense(u0, hh, th, ka));
+        e1 = __fsub_rn(data[2 * m + 1], tsit5_dense(u1, hh, th, kb));
+        acc = __fadd_rn(acc, __fadd_rn(__fmul_rn(e0, e0), __fmul_rn(e1, e1)));
+        ++m;
+        tm = __fmul_rn(__int2float_rn(m), c.save_dt);
+      }
+      t = tn1;
+      u0 = n0;
+      u1 = n1;
+      ka[0] = ka[6];
+      kb[0] = kb[6];
+      float fac = kCtlFacMax;
+      if (err > 0.0f)
+        fac = __fmul_rn(kCtlSafe, exp_f(__fmaf_rn(kCtlBeta, log_f(errold), __fmul_rn(-kCtlAlpha, log_f(err)))));
+      fac = fminf(rejected ? 1.0f : kCtlFacMax, fmaxf(kCtlFacMin, fac));
+      errold = fmaxf(err, kCtlErrMin);
+      h = __fmul_rn(hh, fac);
+      rejected = false;
+    } else {
+      const float fac = fmaxf(kCtlFacMin, __fmul_rn(kCtlSafe, exp_f(__fmul_rn(-0.2f, log_f(err)))));
+      h = __fmul_rn(hh, fac);
+      rejected = true;
+    }
+  }
+  if (steps) *steps = n;
   return acc;
 }
 

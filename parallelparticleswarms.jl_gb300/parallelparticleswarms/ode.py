@@ -49,10 +49,18 @@ def trajectory64(model: str, p, u0, dt: float, nsteps: int, save_every: int, l: 
     return np.array(out)
 
 
-METHODS = {"rk4": 0, "tsit5": 1}
+METHODS = {"rk4": 0, "tsit5": 1, "tsit5_adaptive": 2}
+RELTOL_DEFAULT, ABSTOL_DEFAULT = 1e-3, 1e-6  # the SciML solvers' default tolerances
 
 
-def _fit_params(u0, dt, nsteps, save_every, l, method, save_dt):
+def _fit_params(u0, dt, nsteps, save_every, l, method, save_dt, reltol=RELTOL_DEFAULT, abstol=ABSTOL_DEFAULT):
+    """The fit configuration vector p.  Adaptive Tsit5 (method 2) integrates to
+    (nsaves - 1) save_dt from a first step dt, with reltol / abstol in the
+    slots of nsteps / save_every."""
+    if method == "tsit5_adaptive":
+        if save_dt is None:
+            raise ValueError("a Tsit5 fit needs save_dt (the spacing of the observations)")
+        return [u0[0], u0[1], dt, float(reltol), float(abstol), l, 2.0, float(save_dt)]
     prm = [u0[0], u0[1], dt, nsteps, save_every, l]
     if method == "tsit5":
         if save_dt is None:
@@ -64,20 +72,21 @@ def _fit_params(u0, dt, nsteps, save_every, l, method, save_dt):
 
 
 def lv_problem(data, u0=(1.0, 1.0), dt=0.01, nsteps=1000, save_every=10, lb=0.0, ub=5.0, method="rk4",
-               save_dt=None) -> OptimizationProblem:
+               save_dt=None, reltol=RELTOL_DEFAULT, abstol=ABSTOL_DEFAULT) -> OptimizationProblem:
     """Lotka-Volterra fit: du1 = a u1 - b u1 u2, du2 = -c u2 + d u1 u2 (4 parameters)."""
     return OptimizationProblem(lotka_volterra_fit, np.zeros(4, np.float32),
-                               _fit_params(u0, dt, nsteps, save_every, 0.0, method, save_dt),
+                               _fit_params(u0, dt, nsteps, save_every, 0.0, method, save_dt, reltol, abstol),
                                lb=np.full(4, lb, np.float32), ub=np.full(4, ub, np.float32), data=data)
 
 
 def fhn_problem(data, u0=(-1.0, 1.0), dt=0.01, nsteps=2000, save_every=10, l=FHN_L, lb=0.0,
-                ub=5.0, method="rk4", save_dt=None, fit_l=False) -> OptimizationProblem:
+                ub=5.0, method="rk4", save_dt=None, fit_l=False, reltol=RELTOL_DEFAULT,
+                abstol=ABSTOL_DEFAULT) -> OptimizationProblem:
     """FitzHugh-Nagumo fit of (a, b, tinv), or of (a, b, tinv, l) with ``fit_l``:
     dv = v - v^3/3 - w + l, dw = tinv (v + a - b w)."""
     D = 4 if fit_l else 3
     return OptimizationProblem(fitzhugh_nagumo_fit, np.zeros(D, np.float32),
-                               _fit_params(u0, dt, nsteps, save_every, l, method, save_dt),
+                               _fit_params(u0, dt, nsteps, save_every, l, method, save_dt, reltol, abstol),
                                lb=np.full(D, lb, np.float32), ub=np.full(D, ub, np.float32), data=data)
 
 
@@ -135,12 +144,27 @@ def reference_benchmark_fit(model: str):
                        method="tsit5", save_dt=0.01, fit_l=True), np.array(truth)
 
 
+def adaptive(prob: OptimizationProblem, reltol: float = RELTOL_DEFAULT,
+             abstol: float = ABSTOL_DEFAULT) -> OptimizationProblem:
+    """The same Tsit5 fit with adaptive steps (its dt becomes the first step;
+    integrated to (nsaves - 1) save_dt)."""
+    p = list(np.asarray(prob.p, np.float64))
+    if len(p) < 8 or int(p[6]) not in (METHODS["tsit5"], METHODS["tsit5_adaptive"]):
+        raise ValueError("adaptive steps apply to a Tsit5 fit (method='tsit5' with save_dt)")
+    p[3], p[4], p[6] = float(reltol), float(abstol), float(METHODS["tsit5_adaptive"])
+    return OptimizationProblem(prob.f, prob.u0, p, lb=prob.lb, ub=prob.ub, data=prob.data)
+
+
 def parameter_estim_ode(prob: OptimizationProblem, n: int, *, maxiters: int = 100, w: float = 0.7298,
-                        wdamp: float = 1.0, seed: int = 0):
-    """parameter_estim_ode!(prob, cache, lb, ub, Val(false); maxiters) (src/ode_pso.jl:113-170):
-    returns (gbest position, gbest cost)."""
+                        wdamp: float = 1.0, seed: int = 0, adaptive_steps: bool = False,
+                        reltol: float = RELTOL_DEFAULT, abstol: float = ABSTOL_DEFAULT):
+    """parameter_estim_ode!(prob, cache, lb, ub, Val(adaptive); maxiters) (src/ode_pso.jl:54-170):
+    returns (gbest position, gbest cost).  ``adaptive_steps`` (Val(true),
+    :54-111) integrates a Tsit5 fit with adaptive steps at the given tolerances."""
     from .swarm import Swarm
 
+    if adaptive_steps:
+        prob = adaptive(prob, reltol, abstol)
     with Swarm(prob, n, seed=seed) as sw:
         sw.init()
         sw.sync_run(maxiters, w=w, wdamp=wdamp)

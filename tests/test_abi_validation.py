@@ -31,9 +31,9 @@ def _lv(pps, nsaves=11, **kw):
 
 
 def test_ode_method_and_save_spacing(pps, lib):
-    # an unknown integrator id in params[6]
+    # an unknown integrator id in params[6] (0 RK4, 1 Tsit5, 2 adaptive Tsit5)
     prob = _lv(pps, method="tsit5", save_dt=0.1)
-    prob.p[6] = 2.0
+    prob.p[6] = 3.0
     rc, msg, L = _create(lib, prob)
     assert rc == L.EINVAL and "method" in msg
     # Tsit5 without a positive, finite save spacing

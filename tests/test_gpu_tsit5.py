@@ -81,3 +81,47 @@ def test_tsit5_routing(pps):
         sw.sync_run(20)
         au, ac, ai = sw.gbest()
     assert i == ai and np.float32(c) == np.float32(ac) and np.array_equal(u, au)
+
+
+# ---------------------------------------------------------------- adaptive steps
+@pytest.mark.parametrize("model,n,iters,rtol", [("lv", 1000, 6, 1e-3), ("fhn", 257, 5, 1e-5), ("lv", 33, 4, 1e-6)])
+def test_adaptive_tsit5_sync_matches_oracle_every_iteration(pps, orc, model, n, iters, rtol):
+    """parameter_estim_ode!(..., Val(true)): adaptive steps per particle (the
+    embedded error estimate, the PI controller), bit-exact vs the oracle."""
+    prob, _ = pps.ode.reference_benchmark_fit(model)
+    prob = pps.ode.adaptive(prob, reltol=rtol, abstol=rtol * 1e-3)
+    op = oracle_ode_problem(orc, prob)
+    with pps.Swarm(prob, n, seed=6) as sw:
+        sw.init()
+        ref = orc.OracleSwarm(op, n, 6).init()
+        assert_state_equal(sw, ref, "init")
+        for it in range(iters):
+            sw.sync_run(1)
+            ref.sync_run(1)
+            assert_state_equal(sw, ref, f"iteration {it + 1}")
+        sw.sync_run(33)  # graph replay
+        ref.sync_run(33)
+        assert_state_equal(sw, ref, "graph")
+
+
+def test_adaptive_tsit5_objective_matches_oracle(pps, orc):
+    """Point evaluation, including parameters that make the solve hard (the
+    step-size bound and the no-progress test give +inf on both sides)."""
+    rng = np.random.default_rng(3)
+    for model in ("lv", "fhn"):
+        prob, truth = pps.ode.reference_benchmark_fit(model)
+        prob = pps.ode.adaptive(prob, reltol=1e-4, abstol=1e-7)
+        op = oracle_ode_problem(orc, prob)
+        x = rng.uniform(0, 10 if model == "lv" else 5, (700, prob.dim)).astype(np.float32)
+        x[0] = truth
+        got = pps.evaluate(prob, x)
+        want = np.array([op.objective(r) for r in x], np.float32)
+        assert np.array_equal(got, want, equal_nan=True)
+        assert got[0] < 1e-4
+
+
+def test_adaptive_tsit5_recovers_reference_benchmark_parameters(pps):
+    prob, truth = pps.ode.reference_benchmark_fit("lv")
+    u, cost = pps.ode.parameter_estim_ode(prob, 10_000, maxiters=100, seed=0, adaptive_steps=True)
+    assert cost < 0.05
+    assert np.allclose(u, truth, rtol=0.05), (u, truth)
