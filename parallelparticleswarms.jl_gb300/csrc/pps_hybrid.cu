@@ -43,16 +43,16 @@ template <int OBJ, int MAXD, bool SMEM>
 __global__ void __launch_bounds__(SMEM ? kLbfgsThreads : 128)
     k_lbfgs(const float* __restrict__ X0, int64_t ld, int64_t n, ObjParams op, const float* __restrict__ lbp,
             const float* __restrict__ ubp, LocalOpts o, float* __restrict__ xout, float* __restrict__ fout,
-            float* __restrict__ itout) {
-  lbfgs_run<OBJ, MAXD, SMEM>(X0, ld, n, op, lbp, ubp, o, xout, fout, itout);
+            float* __restrict__ itout, unsigned int* next) {
+  lbfgs_run<OBJ, MAXD, SMEM>(X0, ld, n, op, lbp, ubp, o, xout, fout, itout, next);
 }
 
 template <int OBJ, int MAXD, bool SMEM>
 __global__ void __launch_bounds__(SMEM ? kBroydenThreads : 128)
     k_broyden(const float* __restrict__ X0, int64_t ld, int64_t n, ObjParams op, const float* __restrict__ lbp,
               const float* __restrict__ ubp, LocalOpts o, float* __restrict__ xout, float* __restrict__ fout,
-              float* __restrict__ itout) {
-  broyden_run<OBJ, MAXD, SMEM>(X0, ld, n, op, lbp, ubp, o, xout, fout, itout);
+              float* __restrict__ itout, unsigned int* next) {
+  broyden_run<OBJ, MAXD, SMEM>(X0, ld, n, op, lbp, ubp, o, xout, fout, itout, next);
 }
 
 // argmin over the local results (findmin, src/hybrid.jl:145-146) and gather
@@ -62,7 +62,8 @@ struct ArgminSlot {
   unsigned int count;
   unsigned int idx;
   float cost;
-  unsigned int pad[59];
+  unsigned int next;  // the L-BFGS kernel's work counter (particles handed out after the first wave)
+  unsigned int pad[58];
 };
 
 __global__ void k_reset_slot(ArgminSlot* sl) {
@@ -143,19 +144,34 @@ static LocalBufs local_bufs(pps_swarm* s) {
 // L-BFGS: up to 16 dims the history lives in shared memory, blocks of 64
 // (m = 10: 56 KB at MAXD 10; the largest, m = 16 at MAXD 16: 136 KB, one
 // block per SM); above 16 dims in thread-local memory
+// The grid is the resident blocks (at most one thread per particle); the
+// particles after the first wave are handed out by the work counter.
+template <typename K>
+static unsigned resident_blocks(K kernel, int threads, size_t smem, int sm_count, int64_t n) {
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem) != cudaSuccess || per_sm < 1) {
+    cudaGetLastError();
+    per_sm = 1;
+  }
+  const int64_t need = (n + threads - 1) / threads;
+  const int64_t resident = (int64_t)per_sm * sm_count;
+  return (unsigned)(need < resident ? need : resident);
+}
+
 template <int OBJ, int MAXD>
 static int launch_local_lbfgs(pps_swarm* s, const float* x0, const LocalOpts& o, const LocalBufs& b) {
   const int64_t n = s->dv.n;
+  PPS_CUDA(cudaMemsetAsync(&b.slot->next, 0, sizeof(b.slot->next), s->stream));
   if constexpr (MAXD <= 16) {
     const size_t smem = sizeof(float) * lbfgs_hist_floats(o.history, MAXD) * kLbfgsThreads;
     PPS_CUDA(cudaFuncSetAttribute(k_lbfgs<OBJ, MAXD, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    const unsigned blocks = (unsigned)((n + kLbfgsThreads - 1) / kLbfgsThreads);
+    const unsigned blocks = resident_blocks(k_lbfgs<OBJ, MAXD, true>, kLbfgsThreads, smem, s->sm_count, n);
     k_lbfgs<OBJ, MAXD, true><<<blocks, kLbfgsThreads, smem, s->stream>>>(x0, s->dv.npad, n, s->op, s->dv.lb,
-                                                                          s->dv.ub, o, b.x, b.f, b.it);
+                                                                          s->dv.ub, o, b.x, b.f, b.it, &b.slot->next);
   } else {
-    const unsigned blocks = (unsigned)((n + 127) / 128);
+    const unsigned blocks = resident_blocks(k_lbfgs<OBJ, MAXD, false>, 128, 0, s->sm_count, n);
     k_lbfgs<OBJ, MAXD, false><<<blocks, 128, 0, s->stream>>>(x0, s->dv.npad, n, s->op, s->dv.lb, s->dv.ub, o, b.x,
-                                                              b.f, b.it);
+                                                              b.f, b.it, &b.slot->next);
   }
   return PPS_OK;
 }
@@ -165,17 +181,19 @@ static int launch_local_lbfgs(pps_swarm* s, const float* x0, const LocalOpts& o,
 template <int OBJ, int MAXD>
 static int launch_local_broyden(pps_swarm* s, const float* x0, const LocalOpts& o, const LocalBufs& b) {
   const int64_t n = s->dv.n;
+  PPS_CUDA(cudaMemsetAsync(&b.slot->next, 0, sizeof(b.slot->next), s->stream));
   if constexpr (MAXD >= 8) {
     const size_t smem = sizeof(float) * MAXD * MAXD * kBroydenThreads;
     if (smem > (48u << 10))
       PPS_CUDA(cudaFuncSetAttribute(k_broyden<OBJ, MAXD, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    const unsigned blocks = (unsigned)((n + kBroydenThreads - 1) / kBroydenThreads);
+    const unsigned blocks = resident_blocks(k_broyden<OBJ, MAXD, true>, kBroydenThreads, smem, s->sm_count, n);
     k_broyden<OBJ, MAXD, true><<<blocks, kBroydenThreads, smem, s->stream>>>(x0, s->dv.npad, n, s->op, s->dv.lb,
-                                                                             s->dv.ub, o, b.x, b.f, b.it);
+                                                                             s->dv.ub, o, b.x, b.f, b.it,
+                                                                             &b.slot->next);
   } else {
-    const unsigned blocks = (unsigned)((n + 127) / 128);
+    const unsigned blocks = resident_blocks(k_broyden<OBJ, MAXD, false>, 128, 0, s->sm_count, n);
     k_broyden<OBJ, MAXD, false><<<blocks, 128, 0, s->stream>>>(x0, s->dv.npad, n, s->op, s->dv.lb, s->dv.ub, o,
-                                                                b.x, b.f, b.it);
+                                                                b.x, b.f, b.it, &b.slot->next);
   }
   return PPS_OK;
 }

@@ -14,6 +14,8 @@
 // clamps each parameter (max.(x, lb), min.(x, ub)) as the other kernels do.
 #include <cmath>
 
+#include <mutex>
+
 #include "pps_internal.h"
 #include "pps_ode.cuh"
 #include "pps_publish.cuh"
@@ -23,9 +25,26 @@ namespace pps {
 constexpr int kOdeThreads = 128;
 constexpr int kOdeMaxDim = 4;
 
+// dynamic shared memory of a launch: the fixed-step Tsit5 saves' weight table
+inline size_t ode_dyn_smem(const OdeCfg& c) {
+  return c.method == kOdeTsit5 ? sizeof(float) * 8 * (size_t)c.nsaves : 0;
+}
+
+// builds the block's save table (fixed-step Tsit5 only; every thread calls it)
+template <int METHOD>
+__device__ __forceinline__ float* ode_table(const OdeCfg& c) {
+  extern __shared__ float ode_tab[];
+  if constexpr (METHOD == kOdeTsit5) {
+    tsit5_table_build(c, ode_tab);
+    __syncthreads();
+  }
+  return ode_tab;
+}
+
 template <int MODEL, int METHOD>
-__device__ __forceinline__ float ode_eval(const float (&x)[kOdeMaxDim], const OdeCfg& c, const float* data) {
-  if constexpr (METHOD == kOdeTsit5) return tsit5_loss<MODEL>(x, c, data);
+__device__ __forceinline__ float ode_eval(const float (&x)[kOdeMaxDim], const OdeCfg& c, const float* data,
+                                          const float* tab) {
+  if constexpr (METHOD == kOdeTsit5) return tsit5_loss_tab<MODEL>(x, c, data, tab);
   else if constexpr (METHOD == kOdeTsit5Adaptive) return tsit5a_loss<MODEL>(x, c, data);
   else return ode_loss<MODEL>(x, c, data);
 }
@@ -36,6 +55,7 @@ __global__ void __launch_bounds__(kOdeThreads) k_init_ode(SwarmDev s, ObjParams 
                                                           int sampler, const float* __restrict__ u0) {
   __shared__ float data[2 * kOdeMaxSaves];
   for (int k = threadIdx.x; k < 2 * cfg.nsaves; k += blockDim.x) data[k] = data_g[k];
+  const float* tab = ode_table<METHOD>(cfg);
   __syncthreads();
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
@@ -67,7 +87,7 @@ __global__ void __launch_bounds__(kOdeThreads) k_init_ode(SwarmDev s, ObjParams 
         s.P[o] = x[d];
       }
     }
-    const float c = valid ? ode_eval<MODEL, METHOD>(x, cfg, data) : __int_as_float(0x7f800000);
+    const float c = valid ? ode_eval<MODEL, METHOD>(x, cfg, data, tab) : __int_as_float(0x7f800000);
     s.cost[i] = c;
     s.pcost[i] = c;
     s.flag[i] = 0;
@@ -92,6 +112,7 @@ __global__ void __launch_bounds__(kOdeThreads) k_sync_step_ode(SwarmDev s, ObjPa
     slb[threadIdx.x] = s.lb[threadIdx.x];
     sub[threadIdx.x] = s.ub[threadIdx.x];
   }
+  const float* tab = ode_table<METHOD>(cfg);
   __syncthreads();
   const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -122,7 +143,7 @@ __global__ void __launch_bounds__(kOdeThreads) k_sync_step_ode(SwarmDev s, ObjPa
         x[d] = xd;
       }
     }
-    const float c = ode_eval<MODEL, METHOD>(x, cfg, data);
+    const float c = ode_eval<MODEL, METHOD>(x, cfg, data, tab);
     float pc = s.pcost[i];
     const bool improved = valid && c < pc;
     pc = improved ? c : pc;
@@ -194,11 +215,43 @@ int ode_check(const pps_problem* prob) {
 
 static OdeCfg cfg_of(pps_swarm* s) { return ode_cfg(s->op, s->od.ndata); }
 
+template <int MODEL, int METHOD>
+__global__ void k_eval_ode(ObjParams op, OdeCfg cfg, const float* __restrict__ data_g, const float* __restrict__ x,
+                           int64_t npts, int64_t stride, float* __restrict__ f);
+
+// The fixed-step Tsit5 kernels' dynamic shared-memory limit is raised once
+// per device to the largest save table (init precedes every captured run of
+// a swarm, so captured launches need no attribute call).
+static int ode_set_smem_limit() {
+  static std::mutex mu;
+  static bool done[64] = {};
+  int dev = 0;
+  PPS_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return set_error(PPS_ENOTSUP, "device %d out of range", dev);
+  std::lock_guard<std::mutex> lock(mu);
+  if (done[dev]) return PPS_OK;
+  const int smem = (int)(sizeof(float) * 8 * kOdeMaxSaves);
+#define PPS_ODE_SMEM(M)                                                                                         \
+  PPS_CUDA(cudaFuncSetAttribute(k_init_ode<M, kOdeTsit5>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));      \
+  PPS_CUDA(cudaFuncSetAttribute(k_sync_step_ode<M, kOdeTsit5>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)); \
+  PPS_CUDA(cudaFuncSetAttribute(k_eval_ode<M, kOdeTsit5>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem))
+  PPS_ODE_SMEM(kOdeLV);
+  PPS_ODE_SMEM(kOdeFHN);
+#undef PPS_ODE_SMEM
+  done[dev] = true;
+  return PPS_OK;
+}
+
 int launch_init_ode(pps_swarm* s, int sampler, const float* u0_dev) {
   const unsigned blocks = (unsigned)((s->dv.npad + kOdeThreads - 1) / kOdeThreads);
   const OdeCfg c = cfg_of(s);
+  const size_t dsm = ode_dyn_smem(c);
+  if (dsm) {
+    const int rc = ode_set_smem_limit();
+    if (rc) return rc;
+  }
 #define L_INIT_ODE(M, I) \
-  k_init_ode<M, I><<<blocks, kOdeThreads, 0, s->stream>>>(s->dv, s->op, c, s->od.data, s->seed, sampler, u0_dev)
+  k_init_ode<M, I><<<blocks, kOdeThreads, dsm, s->stream>>>(s->dv, s->op, c, s->od.data, s->seed, sampler, u0_dev)
   PPS_DISPATCH_ODE(s->objective, c.method, L_INIT_ODE);
 #undef L_INIT_ODE
   PPS_CUDA(cudaGetLastError());
@@ -209,9 +262,10 @@ int launch_sync_step_ode(pps_swarm* s, float c1, float c2) {
   const unsigned blocks = (unsigned)((s->dv.npad + kOdeThreads - 1) / kOdeThreads);
   const OdeCfg c = cfg_of(s);
   const int from_pos = (s->flags & PPS_FLAG_GBEST_FROM_POSITION) ? 1 : 0;
-#define L_STEP_ODE(M, I)                                                                                 \
-  k_sync_step_ode<M, I><<<blocks, kOdeThreads, 0, s->stream>>>(s->dv, s->op, c, s->od.data, s->seed, c1, c2, \
-                                                               from_pos)
+  const size_t dsm = ode_dyn_smem(c);
+#define L_STEP_ODE(M, I)                                                                                   \
+  k_sync_step_ode<M, I><<<blocks, kOdeThreads, dsm, s->stream>>>(s->dv, s->op, c, s->od.data, s->seed, c1, c2, \
+                                                                 from_pos)
   PPS_DISPATCH_ODE(s->objective, c.method, L_STEP_ODE);
 #undef L_STEP_ODE
   PPS_CUDA(cudaGetLastError());
@@ -223,6 +277,7 @@ __global__ void k_eval_ode(ObjParams op, OdeCfg cfg, const float* __restrict__ d
                            int64_t npts, int64_t stride, float* __restrict__ f) {
   __shared__ float data[2 * kOdeMaxSaves];
   for (int k = threadIdx.x; k < 2 * cfg.nsaves; k += blockDim.x) data[k] = data_g[k];
+  const float* tab = ode_table<METHOD>(cfg);
   __syncthreads();
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= npts) return;
@@ -230,14 +285,19 @@ __global__ void k_eval_ode(ObjParams op, OdeCfg cfg, const float* __restrict__ d
 #pragma unroll
   for (int d = 0; d < kOdeMaxDim; ++d)
     if (d < op.dim) p[d] = x[(int64_t)d * stride + i];
-  f[i] = ode_eval<MODEL, METHOD>(p, cfg, data);
+  f[i] = ode_eval<MODEL, METHOD>(p, cfg, data, tab);
 }
 
 int launch_eval_ode(const ObjParams& op, const ObjData& od, int objective, const float* x, int64_t npts,
                     int64_t stride, float* f, cudaStream_t stream) {
   const unsigned blocks = (unsigned)((npts + 127) / 128);
   const OdeCfg c = ode_cfg(op, od.ndata);
-#define L_EVAL_ODE(M, I) k_eval_ode<M, I><<<blocks, 128, 0, stream>>>(op, c, od.data, x, npts, stride, f)
+  const size_t dsm = ode_dyn_smem(c);
+  if (dsm) {
+    const int rc = ode_set_smem_limit();
+    if (rc) return rc;
+  }
+#define L_EVAL_ODE(M, I) k_eval_ode<M, I><<<blocks, 128, dsm, stream>>>(op, c, od.data, x, npts, stride, f)
   PPS_DISPATCH_ODE(objective, c.method, L_EVAL_ODE);
 #undef L_EVAL_ODE
   PPS_CUDA(cudaGetLastError());

@@ -210,6 +210,76 @@ __device__ __forceinline__ float tsit5_dense(float u, float dt, float th, const 
   return __fmaf_rn(dt, s, u);
 }
 
+// The fixed-step saves of a Tsit5 fit, shared by all its particles: save m
+// falls in step n(m), the first step whose end t_n+1 = (n+1) dt reaches
+// t_m = m save_dt, at theta = (t_m - t_n) / dt, so its continuous-extension
+// weights b_i(theta) are the same for every particle.  Row m (m >= 1) of the
+// table: n(m) (as int bits), then b_1..b_7(theta); saves past the last step
+// get n(m) = nsteps (never reached, as in the step loop).  Built by all threads
+// of a block before the particles' integrations (8 nsaves floats of shared
+// memory); each weight is the operation sequence tsit5_dense performs.
+__device__ __forceinline__ void tsit5_table_build(const OdeCfg& c, float* tab) {
+  using namespace ts5;
+  const float dt = c.dt;
+  for (int m = 1 + (int)threadIdx.x; m < c.nsaves; m += (int)blockDim.x) {
+    const float tm = __fmul_rn(__int2float_rn(m), c.save_dt);
+    // the smallest n with tm <= (n + 1) dt: an estimate, then corrected
+    int n = (int)__fdiv_rn(tm, dt) - 1;
+    if (n < 0) n = 0;
+    while (n > 0 && tm <= __fmul_rn(__int2float_rn(n), dt)) --n;
+    while (n < c.nsteps && tm > __fmul_rn(__int2float_rn(n + 1), dt)) ++n;
+    const float tn = __fmul_rn(__int2float_rn(n), dt);
+    const float th = __fdiv_rn(__fsub_rn(tm, tn), dt);
+    const float th2 = __fmul_rn(th, th);
+    float* row = tab + 8 * m;
+    row[0] = __int_as_float(n);
+    row[1] = __fmul_rn(th, __fmaf_rn(th, __fmaf_rn(th, __fmaf_rn(th, r14, r13), r12), 1.0f));
+    row[2] = tsit5_weight(th, th2, r22, r23, r24);
+    row[3] = tsit5_weight(th, th2, r32, r33, r34);
+    row[4] = tsit5_weight(th, th2, r42, r43, r44);
+    row[5] = tsit5_weight(th, th2, r52, r53, r54);
+    row[6] = tsit5_weight(th, th2, r62, r63, r64);
+    row[7] = tsit5_weight(th, th2, r72, r73, r74);
+  }
+}
+
+// u + dt sum_i w_i k_i with the weights of a table row (tsit5_dense's sums)
+__device__ __forceinline__ float tsit5_dense_w(float u, float dt, const float* w, const float (&k)[7]) {
+  float s = __fmul_rn(w[0], k[0]);
+#pragma unroll
+  for (int i = 1; i < 7; ++i) s = __fmaf_rn(w[i], k[i], s);
+  return __fmaf_rn(dt, s, u);
+}
+
+// tsit5_loss with the saves' weights from the table: the same operations
+template <int MODEL>
+__device__ __forceinline__ float tsit5_loss_tab(const float* p, const OdeCfg& c, const float* data, const float* tab) {
+  const float dt = c.dt;
+  float u0 = c.u0a, u1 = c.u0b;
+  float e0 = __fsub_rn(data[0], u0), e1 = __fsub_rn(data[1], u1);
+  float acc = __fadd_rn(__fmul_rn(e0, e0), __fmul_rn(e1, e1));
+  const float l = ode_l(p, c);
+  float ka[7], kb[7];
+  ode_rhs<MODEL>(p, l, u0, u1, ka[0], kb[0]);
+  int m = 1;
+  for (int n = 0; n < c.nsteps && m < c.nsaves; ++n) {
+    float n0, n1;
+    tsit5_step<MODEL>(p, l, dt, u0, u1, ka, kb, n0, n1);
+    while (m < c.nsaves && __float_as_int(tab[8 * m]) == n) {  // the saves inside (t_n, t_n+1]
+      const float* w = tab + 8 * m + 1;
+      e0 = __fsub_rn(data[2 * m], tsit5_dense_w(u0, dt, w, ka));
+      e1 = __fsub_rn(data[2 * m + 1], tsit5_dense_w(u1, dt, w, kb));
+      acc = __fadd_rn(acc, __fadd_rn(__fmul_rn(e0, e0), __fmul_rn(e1, e1)));
+      ++m;
+    }
+    u0 = n0;
+    u1 = n1;
+    ka[0] = ka[6];
+    kb[0] = kb[6];
+  }
+  return acc;
+}
+
 // SSE of the Tsit5 solution at t_m = m save_dt (m < nsaves) against data
 template <int MODEL>
 __device__ __forceinline__ float tsit5_loss(const float* p, const OdeCfg& c, const float* data) {
