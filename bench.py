@@ -420,6 +420,19 @@ def run_configs(pps) -> dict:
         except Exception as e:  # the oracle is optional on a machine without its build
             entry["cpu_oracle"] = {"unavailable": str(e)}
         out[f"ode_{model}_tsit5_reference_benchmark"] = entry
+    # the same LV benchmark with adaptive steps (parameter_estim_ode!(..., Val(true)), reltol 1e-3,
+    # abstol 1e-6, first step 0.1)
+    prob, truth = pps.ode.reference_benchmark_fit("lv")
+    aprob = pps.ode.adaptive(prob)
+    with pps.Swarm(aprob, 10_000, seed=0) as sw:
+        sw.init()
+        sw.sync_run(5)  # warm
+        sw.init()
+        ms = sw.sync_run(100)
+        u, cost, _ = sw.gbest()
+    out["ode_lv_tsit5_adaptive_reference_benchmark"] = {
+        "device_ms": ms, "particle_iters_per_s": 10_000 * 100 / (ms / 1e3), "gbest_cost": cost,
+        "max_rel_err_vs_truth": float(np.max(np.abs(u - truth) / truth)), "reltol": 1e-3, "abstol": 1e-6}
     # many small separable swarms in one batched launch against the same
     # swarms solved one at a time
     rng = np.random.default_rng(5)

@@ -622,7 +622,7 @@ static int ode_threads() {
   return v;
 }
 
-LaunchGroup batch_group_of(const BatchSwarm& d, int threads, int ppt) {
+LaunchGroup batch_group_of(const BatchSwarm& d, int threads, int ppt, int spread) {
   LaunchGroup g{};
   const int cmax = max_cluster();
   if (is_ode(d.objective)) {
@@ -634,7 +634,7 @@ LaunchGroup batch_group_of(const BatchSwarm& d, int threads, int ppt) {
   } else {
     g.kind = 0;
     g.T = threads;
-    const int64_t width = (int64_t)threads * ppt * 8;
+    const int64_t width = (int64_t)threads * ppt * spread;
     const int64_t c = (d.n + width - 1) / width;
     g.C = (int)(c < cmax ? c : cmax);
     if (g.C < 1) g.C = 1;
@@ -645,11 +645,11 @@ LaunchGroup batch_group_of(const BatchSwarm& d, int threads, int ppt) {
 static int64_t chunk_of(int64_t n, int C, int width) { return cta_chunk(n, C, width); }
 
 void batch_plan(const std::vector<BatchSwarm>& descs, int threads, int ppt, std::vector<int>* order,
-                std::vector<LaunchGroup>* groups) {
+                std::vector<LaunchGroup>* groups, int spread) {
   const int ns = (int)descs.size();
   std::map<std::tuple<int, int, int>, std::vector<int>> by;
   for (int k = 0; k < ns; ++k) {
-    const LaunchGroup g = batch_group_of(descs[k], threads, ppt);
+    const LaunchGroup g = batch_group_of(descs[k], threads, ppt, spread);
     by[std::make_tuple(-g.C, g.kind, g.T)].push_back(k);  // larger clusters first
   }
   order->clear();
@@ -746,8 +746,8 @@ struct pps_batch {
   BatchSwarm* ddescs = nullptr;
   int* dorder = nullptr;
   size_t dcap = 0;
-  int tuned_threads = 0, tuned_ppt = 0;
-  int last_threads = 0, last_ppt = 0;
+  int tuned_threads = 0, tuned_ppt = 0, tuned_spread = 8;
+  int last_threads = 0, last_ppt = 0, last_spread = 8;
   int last_groups = 0, last_max_cluster = 0;
   bool ran = false;
 };
@@ -755,7 +755,7 @@ struct pps_batch {
 namespace {
 
 std::mutex g_tune_mu;
-std::map<std::string, std::pair<int, int>> g_tune_cache;
+std::map<std::string, std::tuple<int, int, int>> g_tune_cache;  // shape -> (threads, ppt, spread)
 
 int prepare(pps_batch* b) {
   const size_t ns = b->descs.size();
@@ -797,10 +797,10 @@ int prepare(pps_batch* b) {
 }
 
 // every group on its own stream, joined back into b->stream; ev0/ev1 bracket it
-int run_groups(pps_batch* b, int threads, int ppt, int* ngroups, int* maxc) {
+int run_groups(pps_batch* b, int threads, int ppt, int spread, int* ngroups, int* maxc) {
   std::vector<int> order;
   std::vector<LaunchGroup> groups;
-  batch_plan(b->descs, threads, ppt, &order, &groups);
+  batch_plan(b->descs, threads, ppt, &order, &groups, spread);
   PPS_CUDA(cudaMemcpyAsync(b->dorder, order.data(), sizeof(int) * order.size(), cudaMemcpyHostToDevice, b->stream));
   PPS_CUDA(cudaEventRecord(b->ev0, b->stream));
   int rc = PPS_OK;
@@ -917,16 +917,13 @@ int pps_batch_run(pps_batch* b, float* device_ms) {
   if (rc) return rc;
   const int ns = (int)b->descs.size();
   // autotune the block shape for this batch shape (cached)
-  int threads = b->tuned_threads, ppt = b->tuned_ppt;
+  int threads = b->tuned_threads, ppt = b->tuned_ppt, spread = b->tuned_spread;
   if (!threads) {
     const std::string key = shape_key(b);
     {
       std::lock_guard<std::mutex> lock(g_tune_mu);
       auto it = g_tune_cache.find(key);
-      if (it != g_tune_cache.end()) {
-        threads = it->second.first;
-        ppt = it->second.second;
-      }
+      if (it != g_tune_cache.end()) std::tie(threads, ppt, spread) = it->second;
     }
     if (!threads) {
       // time each candidate on this batch with a few iterations per swarm
@@ -937,34 +934,43 @@ int pps_batch_run(pps_batch* b, float* device_ms) {
         all_ode = all_ode && is_ode(d.objective);
       }
       PPS_CUDA(cudaMemcpyAsync(b->ddescs, b->descs.data(), sizeof(BatchSwarm) * ns, cudaMemcpyHostToDevice, b->stream));
+      // block size x particles per thread x particles per thread per
+      // iteration: a batch of few swarms runs faster spread over more CTAs
+      // (more warps per SM) than over few CTAs that loop over their particles
       const int cand_t[3] = {128, 256, 512};
       const int cand_p[3] = {1, 2, 4};
+      const int cand_s[2] = {8, 2};
       float best_ms = 1e30f;
-      for (int ct : cand_t) {
-        for (int cp : cand_p) {
-          if (cp == 2 && all_ode) continue;  // ODE swarms ignore PPT
-          if ((rc = run_groups(b, ct, cp, nullptr, nullptr))) return rc;
-          PPS_CUDA(cudaEventSynchronize(b->ev1));
-          float ms = 0.0f;
-          PPS_CUDA(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
-          if (ms < best_ms) {
-            best_ms = ms;
-            threads = ct;
-            ppt = cp;
+      for (int cs : cand_s) {
+        if (cs != 8 && all_ode) continue;  // ODE fits take one particle per thread
+        for (int ct : cand_t) {
+          for (int cp : cand_p) {
+            if (cp == 2 && all_ode) continue;  // ODE swarms ignore PPT
+            if ((rc = run_groups(b, ct, cp, cs, nullptr, nullptr))) return rc;
+            PPS_CUDA(cudaEventSynchronize(b->ev1));
+            float ms = 0.0f;
+            PPS_CUDA(cudaEventElapsedTime(&ms, b->ev0, b->ev1));
+            if (ms < best_ms) {
+              best_ms = ms;
+              threads = ct;
+              ppt = cp;
+              spread = cs;
+            }
           }
         }
       }
       b->descs = saved;
       PPS_CUDA(cudaMemcpyAsync(b->ddescs, b->descs.data(), sizeof(BatchSwarm) * ns, cudaMemcpyHostToDevice, b->stream));
       std::lock_guard<std::mutex> lock(g_tune_mu);
-      g_tune_cache[key] = {threads, ppt};
+      g_tune_cache[key] = std::make_tuple(threads, ppt, spread);
     }
   }
-  if ((rc = run_groups(b, threads, ppt, &b->last_groups, &b->last_max_cluster))) return rc;
+  if ((rc = run_groups(b, threads, ppt, spread, &b->last_groups, &b->last_max_cluster))) return rc;
   PPS_CUDA(cudaEventSynchronize(b->ev1));
   if (device_ms) PPS_CUDA(cudaEventElapsedTime(device_ms, b->ev0, b->ev1));
   b->last_threads = threads;
   b->last_ppt = ppt;
+  b->last_spread = spread;
   b->ran = true;
   return PPS_OK;
 }
@@ -973,12 +979,14 @@ int pps_batch_set_shape(pps_batch* b, int32_t threads, int32_t ppt) {
   if (!b) return set_error(PPS_EINVAL, "batch is NULL");
   if (threads == 0 && ppt == 0) {
     b->tuned_threads = b->tuned_ppt = 0;
+    b->tuned_spread = 8;
     return PPS_OK;
   }
   if (!(threads == 128 || threads == 256 || threads == 512) || !(ppt == 1 || ppt == 2 || ppt == 4))
     return set_error(PPS_EINVAL, "block shape must be threads in {128, 256, 512} and ppt in {1, 2, 4}");
   b->tuned_threads = threads;
   b->tuned_ppt = ppt;
+  b->tuned_spread = 8;
   return PPS_OK;
 }
 

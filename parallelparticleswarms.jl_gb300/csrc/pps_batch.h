@@ -52,14 +52,14 @@ int batch_describe(const pps_problem* prob, int64_t n, uint64_t seed, int32_t ma
                    float c1, float c2, BatchSwarm* d, std::vector<float>* host_inputs);
 size_t batch_smem_bytes(int maxdim, int data_floats, int64_t maxchunk);
 // the (kind, T, C) a swarm is launched with: separable swarms use the
-// batch's block size and about 8 particles per thread per iteration, ODE fits
-// one particle per thread (up to 1024 threads per CTA), both split over up
-// to 16 CTAs
-LaunchGroup batch_group_of(const BatchSwarm& d, int threads, int ppt);
+// batch's block size and about `spread` particles per thread per iteration
+// (8 by default; fewer split a swarm over more CTAs), ODE fits one particle
+// per thread (up to 1024 threads per CTA), both split over up to 16 CTAs
+LaunchGroup batch_group_of(const BatchSwarm& d, int threads, int ppt, int spread = 8);
 // group swarms by (kind, T, C); order lists descriptor indices group by
 // group, longest estimated work first inside each group
 void batch_plan(const std::vector<BatchSwarm>& descs, int threads, int ppt, std::vector<int>* order,
-                std::vector<LaunchGroup>* groups);
+                std::vector<LaunchGroup>* groups, int spread = 8);
 // launch one group: descs[dorder[g.offset + k]], k < g.count, on `stream`
 int batch_launch_group(cudaStream_t stream, const BatchSwarm* ddescs, const int* dorder, const LaunchGroup& g,
                        int ppt);

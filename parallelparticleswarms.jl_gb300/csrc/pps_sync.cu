@@ -102,7 +102,7 @@ __global__ void __launch_bounds__(kSyncThreads) k_init(SwarmDev s, ObjParams op,
 // memory take fewer tiles, and all finish within about one tile of each
 // other.  A particle's arithmetic does not depend on which block takes it.
 // Resident blocks: 2 for PPT = 4 (128 registers), 4 for PPT = 2 (64
-// registers, a 24-byte spill) and PPT = 1: with 32 warps per SM, two
+// registers, no spill) and PPT = 1: with 32 warps per SM, two
 // particles per thread keep the most loads in flight.
 // CONS: the constrained path (PPT = 1 only): the cost adds calc_penalty with
 // iter = the 1-based particle index, as the reference's sync and queue-lock
