@@ -477,7 +477,8 @@ __global__ void __launch_bounds__(kMlpThreads, 1) k_mlp_eval(SwarmDev s, MlpArgs
         }
         const float* w2 = w2base + pp * kMlpW2Stride;
         float o = w2[32];  // b2
-        // units j with (j % 8) < NF / 4 use the FP32 pipe: spread over the sum
+        // units j with (j % 8) < NF / 4 use the FP32 pipe: spread over the sum (placing
+        // them last in each group of 8 measured no faster: 0.2017 vs 0.1996 ms)
 #pragma unroll
         for (int j = 0; j < kMlpHidden; j += 4) {
           const float4 ww = *reinterpret_cast<const float4*>(w2 + j);
