@@ -433,8 +433,33 @@ def run_configs(pps) -> dict:
     out["ode_lv_tsit5_adaptive_reference_benchmark"] = {
         "device_ms": ms, "particle_iters_per_s": 10_000 * 100 / (ms / 1e3), "gbest_cost": cost,
         "max_rel_err_vs_truth": float(np.max(np.abs(u - truth) / truth)), "reltol": 1e-3, "abstol": 1e-6}
-    # many small separable swarms in one batched launch against the same
-    # swarms solved one at a time
+    out["separable_batch_256"] = run_separable_batch(pps)
+    return out
+
+
+def _nvtx_range(name):
+    """An NVTX range (ncu --nvtx --nvtx-include) around a region, when torch is importable."""
+    import contextlib
+
+    try:
+        import torch
+
+        @contextlib.contextmanager
+        def rng():
+            torch.cuda.nvtx.range_push(name)
+            try:
+                yield
+            finally:
+                torch.cuda.nvtx.range_pop()
+        return rng()
+    except Exception:
+        return contextlib.nullcontext()
+
+
+def run_separable_batch(pps, plain: bool = True) -> dict:
+    """Many small separable swarms in one batched launch (the autotuner's first
+    run, then the timed run inside the NVTX range "batch_timed") against the
+    same swarms solved one at a time (a sample of 32)."""
     rng = np.random.default_rng(5)
     swarms = []
     for k in range(256):
@@ -449,10 +474,17 @@ def run_configs(pps) -> dict:
         for k, (prob, n) in enumerate(swarms):
             b.add(prob, n, maxiters=500, seed=k)
         b.run()  # autotune + warm
-        t0 = time.perf_counter()
-        bms = b.run()
-        bwall = time.perf_counter() - t0
+        with _nvtx_range("batch_timed"):
+            t0 = time.perf_counter()
+            bms = b.run()
+            bwall = time.perf_counter() - t0
         res = [b.result(k) for k in range(len(swarms))]
+        shape = b.info()
+    out = {"workload": "256 swarms (Rosenbrock / Rastrigin / Ackley, dim U{2..64}, particles U{256..2048}), "
+                       "500 iterations, one launch",
+           "batched_device_ms": bms, "batched_solves_per_s": len(swarms) / bwall, "block_shape": shape}
+    if not plain:
+        return out
     same = True
     t0 = time.perf_counter()
     sample = list(range(0, len(swarms), 8))
@@ -463,12 +495,9 @@ def run_configs(pps) -> dict:
             sw.sync_run(500)
             u, c, i = sw.gbest()
         same &= bool(np.array_equal(u, res[k][0]) and i == res[k][2])
-    plain = len(sample) / (time.perf_counter() - t0)
-    out["separable_batch_256"] = {"workload": "256 swarms (Rosenbrock / Rastrigin / Ackley, dim U{2..64}, "
-                                              "particles U{256..2048}), 500 iterations, one launch",
-                                  "batched_device_ms": bms, "batched_solves_per_s": len(swarms) / bwall,
-                                  "plain_solves_per_s": plain, "speedup_vs_plain": len(swarms) / bwall / plain,
-                                  "same_result_alone_and_batched": same}
+    rate = len(sample) / (time.perf_counter() - t0)
+    out.update({"plain_solves_per_s": rate, "speedup_vs_plain": len(swarms) / bwall / rate,
+                "same_result_alone_and_batched": same})
     return out
 
 
@@ -709,7 +738,7 @@ def main():
     ap.add_argument("--mlp-iters", type=int, default=100, help="iterations of the MLP-fit measurement")
     ap.add_argument("--user-n", type=int, default=N_PARTICLES,
                     help="particles of the user-objective (CUDA C source) measurement")
-    ap.add_argument("--only", choices=["sync", "async", "hybrid", "ode", "serve", "mlp", "configs", "user"],
+    ap.add_argument("--only", choices=["sync", "async", "hybrid", "ode", "serve", "mlp", "configs", "user", "batch"],
                     default=None,
                     help="run one workload only (for profiling); prints its result")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target length of the CPU-baseline sample")
@@ -752,12 +781,13 @@ def main():
     iters = args.iters
     seed0 = multi.swarm_seed(0, rank)
 
-    if args.only in ("hybrid", "ode", "serve", "mlp", "configs", "user"):
+    if args.only in ("hybrid", "ode", "serve", "mlp", "configs", "user", "batch"):
         fn = {"hybrid": lambda: run_hybrid(pps), "ode": lambda: run_ode_batch(pps, args.ode_fits),
               "serve": lambda: {"served": run_served(pps, args, True),
                                 "served_without_mlp": run_served(pps, args, False)},
               "mlp": lambda: run_mlp(pps, args.mlp_iters), "configs": lambda: run_configs(pps),
-              "user": lambda: run_user(pps, args.user_n)}[args.only]
+              "user": lambda: run_user(pps, args.user_n),
+              "batch": lambda: run_separable_batch(pps, plain=False)}[args.only]
         if rank == 0:
             print(json.dumps({args.only: fn()}), flush=True)
         return 0
