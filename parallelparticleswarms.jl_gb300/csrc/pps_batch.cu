@@ -820,6 +820,30 @@ int run_groups(pps_batch* b, int threads, int ppt, int spread, int* ngroups, int
   return PPS_OK;
 }
 
+// PPS_BATCH_SHAPE="threads,ppt,spread" (threads 128/256/512, ppt 1/2/4, spread 2/8); other values are ignored
+void pinned_shape(int* threads, int* ppt, int* spread) {
+  static bool parsed = false;
+  static int v[3] = {0, 0, 0};
+  static std::mutex mu;
+  std::lock_guard<std::mutex> lock(mu);
+  if (!parsed) {
+    parsed = true;
+    const char* e = getenv("PPS_BATCH_SHAPE");
+    int t = 0, p = 0, sp = 0;
+    if (e && sscanf(e, "%d,%d,%d", &t, &p, &sp) == 3 && (t == 128 || t == 256 || t == 512) &&
+        (p == 1 || p == 2 || p == 4) && (sp == 2 || sp == 8)) {
+      v[0] = t;
+      v[1] = p;
+      v[2] = sp;
+    }
+  }
+  if (v[0]) {
+    *threads = v[0];
+    *ppt = v[1];
+    *spread = v[2];
+  }
+}
+
 std::string shape_key(const pps_batch* b) {
   // objective mix and coarse size buckets
   int cnt[8] = {0};
@@ -916,8 +940,11 @@ int pps_batch_run(pps_batch* b, float* device_ms) {
   int rc = prepare(b);
   if (rc) return rc;
   const int ns = (int)b->descs.size();
-  // autotune the block shape for this batch shape (cached)
+  // autotune the block shape for this batch shape (cached), unless PPS_BATCH_SHAPE
+  // pins it for every batch ("threads,ppt,spread", e.g. "256,2,2": reproducible
+  // profiles, since the autotuner's timings are not representative under a profiler)
   int threads = b->tuned_threads, ppt = b->tuned_ppt, spread = b->tuned_spread;
+  if (!threads) pinned_shape(&threads, &ppt, &spread);
   if (!threads) {
     const std::string key = shape_key(b);
     {
