@@ -114,6 +114,10 @@ class DeviceShard:
         _lib.check(self._lib.pps_shard_bind(self._h, ctypes.c_void_p(self.local.data_ptr()),
                                             ctypes.c_void_p(self.gathered.data_ptr()), nrec))
         self.stream = torch.cuda.ExternalStream(stream.value, device=dev)
+        # the buffers were filled on torch's current stream, which the shard's
+        # (non-blocking) stream does not wait for: finish the fill before the
+        # shard's first kernel writes its record
+        torch.cuda.current_stream(dev).synchronize()
 
     # -- the shard protocol of sync_loop ------------------------------------
     def ordered(self):
