@@ -41,6 +41,7 @@ CASES = [
     ("sphere", 7, -3.0, 3.0, [], None, 777, 4, 3, False),                    # Latin hypercube
     ("shifted_sphere", 2, 0.0, 2.0, [2.0, 1.0], CONS, 600, 2, 1, False),     # constrained
     ("ackley", 10, -5.0, 5.0, [20.0, 0.2, 1.0], None, 4099, 5, 1, False),
+    ("rastrigin", 3, -5.12, 5.12, [10.0], None, 5, 5, 1, False),            # shards of one particle
 ]
 
 

@@ -125,3 +125,20 @@ def test_adaptive_tsit5_recovers_reference_benchmark_parameters(pps):
     u, cost = pps.ode.parameter_estim_ode(prob, 10_000, maxiters=100, seed=0, adaptive_steps=True)
     assert cost < 0.05
     assert np.allclose(u, truth, rtol=0.05), (u, truth)
+
+
+def test_adaptive_tsit5_served_equals_alone(pps):
+    """The server runs an adaptive fit as a swarm of its own (batches refuse it):
+    the same result as the fit solved alone."""
+    prob, _ = pps.ode.reference_benchmark_fit("fhn")
+    prob = pps.ode.adaptive(prob, reltol=1e-4, abstol=1e-7)
+    with pps.Batch() as b:
+        with pytest.raises(pps.PPSError):
+            b.add(prob, 64, maxiters=5, seed=1)
+    with pps.Server(memory_budget=64 << 20, max_launches=2) as srv:
+        u, c, i, _ = srv.wait(srv.submit(prob, 300, maxiters=12, seed=8))
+    with pps.Swarm(prob, 300, seed=8) as sw:
+        sw.init()
+        sw.sync_run(12)
+        au, ac, ai = sw.gbest()
+    assert i == ai and np.float32(c) == np.float32(ac) and np.array_equal(u, au)

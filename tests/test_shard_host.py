@@ -66,12 +66,13 @@ CASES = [
     ((0, 5, -3.0, 3.0, [], None), 777, 4, 2, 0),                  # Latin hypercube strata over the whole swarm
     ((7, 2, 0.0, 2.0, [2.0, 1.0], CONS), 500, 2, 0, 0),          # the penalty's global particle index
     ((3, 20, -5.0, 5.0, [20.0, 0.2, 1.0], None), 2049, 5, 0, 0),
+    ((2, 3, -5.12, 5.12, [10.0], None), 5, 5, 0, 0),              # shards of one particle
 ]
 
 
 @pytest.mark.parametrize("case,n,k,sampler,src", CASES,
                          ids=["rastrigin-2shards", "rosenbrock-3shards-pos", "sphere-4shards-lhs",
-                              "constrained-2shards", "ackley-5shards"])
+                              "constrained-2shards", "ackley-5shards", "one-particle-shards"])
 def test_oracle_shards_equal_the_whole_swarm(orc, case, n, k, sampler, src):
     shard = _shard_mod()
     oprob = _oprob(orc, case)
