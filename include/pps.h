@@ -410,7 +410,9 @@ typedef struct pps_device_swarm {
  *   flags                       PPS_FLAG_GBEST_FROM_POSITION or 0
  *   stream                      cudaStream_t to launch on (NULL: the legacy default stream)
  *   gcost_out, gidx_out         host pointers, may be NULL; when given, the call
- *                               waits for the stream and returns the global best
+ *                               waits for the stream and returns the global best,
+ *                               or PPS_ETIMEOUT if a bounded wait of the step
+ *                               kernel gave up (without them that is not checked)
  * The run starts from the argmin of pcost (its pbest, or its position with
  * PPS_FLAG_GBEST_FROM_POSITION) and leaves the global best in g.
  * Scratch: the per-iteration argmin state and one byte per particle live in a

@@ -104,6 +104,17 @@ static ObjParams make_params(const pps_problem* prob) {
   return op;
 }
 
+// IterState::status: bit 1, a bounded wait of the tensor-core kernel gave up;
+// bit 2, a bounded wait of the TMA-staged step kernel gave up
+int check_device_status(pps_swarm* s) {
+  if (s->objective != kMlp && !s->bounded_waits) return PPS_OK;
+  unsigned int status = 0;
+  PPS_CUDA(cudaMemcpy(&status, &s->dv.st->status, sizeof(status), cudaMemcpyDeviceToHost));
+  if (status & 2u) return set_error(PPS_ETIMEOUT, "the MLP tensor-core kernel timed out waiting for an MMA");
+  if (status & 4u) return set_error(PPS_ETIMEOUT, "the step kernel timed out waiting for a bulk copy");
+  return PPS_OK;
+}
+
 }  // namespace pps
 
 using namespace pps;
@@ -366,15 +377,6 @@ int pps_swarm_destroy(pps_swarm* s) {
   free(s->host_lb);
   if (dev >= 0 && dev != s->device) cudaSetDevice(dev);
   delete s;
-  return PPS_OK;
-}
-
-// bit 1 of IterState::status: a bounded wait of the tensor-core kernel gave up
-static int check_device_status(pps_swarm* s) {
-  if (s->objective != kMlp) return PPS_OK;
-  unsigned int status = 0;
-  PPS_CUDA(cudaMemcpy(&status, &s->dv.st->status, sizeof(status), cudaMemcpyDeviceToHost));
-  if (status & 2u) return set_error(PPS_ETIMEOUT, "the MLP tensor-core kernel timed out waiting for an MMA");
   return PPS_OK;
 }
 

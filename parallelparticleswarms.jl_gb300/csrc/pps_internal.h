@@ -58,6 +58,7 @@ struct pps_swarm {
   int shard = 0;              // 1: a particle-range shard (pps_shard_create); dv.xrec is its exchange record
   const unsigned char* shard_records = nullptr;  // shard: every shard's record after the exchange
   int shard_nrecords = 0;
+  int bounded_waits = 0;      // 1: a kernel with bounded mbarrier waits ran (a timeout sets IterState::status)
 };
 
 namespace pps {
@@ -81,6 +82,14 @@ int launch_eval(const ObjParams& op, const ObjData& od, int objective, const flo
                 int64_t stride, float* f, cudaStream_t stream);
 int async_lanes(int dim, int* slice);
 int sync_grid(pps_swarm* s);
+// the TMA-staged step (pps_sync_bulk.cu): resident blocks per SM where it
+// applies (0 where it does not), resolved outside any stream capture; the
+// launch, *taken false where the caller launches k_sync_step instead
+int sync_bulk_prepare(pps_swarm* s, int* blocks_per_sm);
+// PPS_ETIMEOUT if a bounded wait of a kernel of this swarm gave up (reads
+// IterState::status after the swarm's stream is idle), else PPS_OK
+int check_device_status(pps_swarm* s);
+int launch_sync_step_bulk(pps_swarm* s, float c1, float c2, bool* taken);
 int local_field(pps_swarm* s, int32_t field, float** dev, int* rows);
 // ODE-fit objectives (pps_ode.cu)
 int ode_check(const pps_problem* prob);

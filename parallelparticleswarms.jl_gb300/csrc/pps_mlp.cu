@@ -47,6 +47,7 @@
 #include <cuda_bf16.h>
 
 #include "pps_internal.h"
+#include "pps_mbarrier.cuh"
 #include "pps_publish.cuh"
 
 namespace pps {
@@ -66,14 +67,6 @@ constexpr uint64_t kMlpWaitNs = 2000000000ull;
 constexpr int kMlpFmaUnitsDefault = 4;  // hidden units (of 32) whose tanh runs on the FP32 pipe
 
 // ---------------------------------------------------------------- PTX helpers
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-__device__ __forceinline__ uint64_t globaltimer() {
-  uint64_t t;
-  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-  return t;
-}
 // shared-memory matrix descriptor: canonical layout without swizzle; LBO is
 // the byte distance between core matrices along K, SBO along M / N
 __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
@@ -106,36 +99,6 @@ __device__ __forceinline__ void mma_bf16_ss(uint32_t d_tmem, uint64_t adesc, uin
 }
 __device__ __forceinline__ void mma_commit(uint32_t mbar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(mbar) : "memory");
-}
-__device__ __forceinline__ void mbar_init(uint32_t mbar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(mbar), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_arrive(uint32_t mbar) {
-  asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.release.cta.shared::cta.b64 st, [%0];\n\t}\n" ::"r"(mbar)
-               : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint32_t mbar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-      "selp.u32 %0, 1, 0, p;\n\t}\n"
-      : "=r"(ok)
-      : "r"(mbar), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-// bounded wait: false when the time limit passed or another thread gave up
-// (the clock and the abort flag are looked at every 64 polls)
-__device__ __forceinline__ bool mbar_wait_bounded(uint32_t mbar, uint32_t parity, volatile int* abort_flag) {
-  if (mbar_try_wait(mbar, parity)) return true;
-  const uint64_t t0 = globaltimer();
-  for (uint32_t i = 1;; ++i) {
-    if (mbar_try_wait(mbar, parity)) return true;
-    if ((i & 63u) == 0 && (*abort_flag || globaltimer() - t0 > kMlpWaitNs)) {
-      *abort_flag = 1;
-      return false;
-    }
-  }
 }
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 __device__ __forceinline__ void tc_before_sync() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
@@ -399,7 +362,7 @@ __global__ void __launch_bounds__(kMlpThreads, 1) k_mlp_eval(SwarmDev s, MlpArgs
     mbar_init(smem_u32(&full_bar[1]), 1);
     mbar_init(smem_u32(&empty_bar[0]), kMlpWarps);
     mbar_init(smem_u32(&empty_bar[1]), kMlpWarps);
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    mbar_init_fence();
     abort_flag = 0;
     s_next[0] = grab();
   }
@@ -418,7 +381,7 @@ __global__ void __launch_bounds__(kMlpThreads, 1) k_mlp_eval(SwarmDev s, MlpArgs
   auto issue = [&](int m) {
     const uint32_t g = issued;
     const uint32_t b = g & 1u, use = g >> 1;
-    if (use >= 1 && !mbar_wait_bounded(smem_u32(&empty_bar[b]), (use - 1u) & 1u, &abort_flag)) return;
+    if (use >= 1 && !mbar_wait_bounded(smem_u32(&empty_bar[b]), (use - 1u) & 1u, &abort_flag, kMlpWaitNs)) return;
     tc_after_sync();
     const uint32_t d = tmem + b * (uint32_t)kMlpN;
     mma_bf16_ss(d, smem_desc(smem_u32(sA + (size_t)m * kMlpATileBytes), 128, 256),
@@ -456,7 +419,7 @@ __global__ void __launch_bounds__(kMlpThreads, 1) k_mlp_eval(SwarmDev s, MlpArgs
       // every lane waits; the warp goes on only if all of them saw the phase
       // (tcgen05.ld below is a warp-wide instruction)
       int okl = 1;
-      if (lane == 0) okl = mbar_wait_bounded(smem_u32(&full_bar[b]), (g >> 1) & 1u, &abort_flag) ? 1 : 0;
+      if (lane == 0) okl = mbar_wait_bounded(smem_u32(&full_bar[b]), (g >> 1) & 1u, &abort_flag, kMlpWaitNs) ? 1 : 0;
       const bool ok = __shfl_sync(0xffffffffu, okl, 0) != 0;
       __syncwarp();
       if (!ok) {

@@ -191,6 +191,7 @@ extern "C" int pps_sync_run_noalloc(int32_t objective, const float* params, int3
   h.flags = flags & PPS_FLAG_GBEST_FROM_POSITION;
 
   PPS_CUDA(cudaMemsetAsync(h.dv.flag, 0, (size_t)sw->ld, h.stream));
+  PPS_CUDA(cudaMemsetAsync(&h.dv.st->status, 0, sizeof(h.dv.st->status), h.stream));
   if ((rc = launch_set_iter(&h, iteration, w, wdamp))) return rc;
   k_noalloc_select<<<h.sm_count, 256, 0, h.stream>>>(h.dv, (h.flags & PPS_FLAG_GBEST_FROM_POSITION) ? 1 : 0);
   PPS_CUDA(cudaGetLastError());
@@ -201,6 +202,7 @@ extern "C" int pps_sync_run_noalloc(int32_t objective, const float* params, int3
     IterState st;
     PPS_CUDA(cudaMemcpyAsync(&st, h.dv.st, sizeof(st), cudaMemcpyDeviceToHost, h.stream));
     PPS_CUDA(cudaStreamSynchronize(h.stream));
+    if (st.status & 4u) return set_error(PPS_ETIMEOUT, "the step kernel timed out waiting for a bulk copy");
     if (gcost_out) *gcost_out = st.gcost;
     if (gidx_out) *gidx_out = (int64_t)st.gidx;
   }

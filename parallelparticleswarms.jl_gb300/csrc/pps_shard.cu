@@ -171,7 +171,7 @@ int pps_shard_finish(pps_swarm* s) {
   if (rc) return rc;
   if ((rc = launch_materialize(s))) return rc;
   PPS_CUDA(cudaStreamSynchronize(s->stream));
-  return PPS_OK;
+  return check_device_status(s);
 }
 
 }  // extern "C"

@@ -352,6 +352,8 @@ static int occupancy_of(int ppt, size_t smem) {
 }
 
 int sync_grid(pps_swarm* s) {
+  int bulk_blocks = 0;
+  sync_bulk_prepare(s, &bulk_blocks);  // the TMA-staged kernel's occupancy, resolved here outside any capture
   // resident blocks of the step kernel per SM (cached per objective, device, dim)
   static thread_local int cached_obj = -1, cached_blocks = 0, cached_dev = -1, cached_dim = -1;
   int per_sm = 0;
@@ -384,6 +386,11 @@ int sync_grid(pps_swarm* s) {
 
 int launch_sync_step(pps_swarm* s, float c1, float c2) {
   if (is_user(s->objective)) return launch_user_step(s, c1, c2);
+  if (s->dv.ncons == 0) {  // PPS_SYNC_KERNEL=bulk: the TMA-staged kernel where it applies
+    bool taken = false;
+    const int rc = launch_sync_step_bulk(s, c1, c2, &taken);
+    if (rc || taken) return rc;
+  }
   const int grid = sync_grid(s);
   const PhiloxKeys keys = philox_round_keys(s->seed);
   const size_t smem = 3 * sizeof(float) * (size_t)s->dv.dim;

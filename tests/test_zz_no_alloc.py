@@ -27,14 +27,15 @@ def _to_device(torch, a, ld):
 @pytest.mark.gpu
 @pytest.mark.parametrize("from_position", [False, True], ids=["gbest_from_pbest", "gbest_from_position"])
 @pytest.mark.parametrize("own_stream", [False, True], ids=["default_stream", "caller_stream"])
-def test_noalloc_matches_sync_run_on_two_calls(pps, from_position, own_stream):
+@pytest.mark.parametrize("n", [3000, 990], ids=["n3000", "n990-ld992"])
+def test_noalloc_matches_sync_run_on_two_calls(pps, from_position, own_stream, n):
     torch = pytest.importorskip("torch")
     if not torch.cuda.is_available():
         pytest.skip("torch without CUDA")
     from parallelparticleswarms import _lib
 
     lib = _lib.load()
-    D, n, K, seed = 24, 3000, 40, 17
+    D, K, seed = 24, 40, 17  # ld = 992 for n = 990: a last tile of 32 particles (half a warp's)
     ld = (n + 31) // 32 * 32
     lb = np.full(D, -5.12, np.float32)
     ub = np.full(D, 5.12, np.float32)
