@@ -172,6 +172,17 @@ def cpu_oracle_rate(n: int, iters: int, threads: int, seed: int = 0):
     return n * iters / dt, dt
 
 
+def cpu_oracle_rate_fast(n: int, iters: int, threads: int):
+    """The same sample on the oracle's timing-only fast build (-O3, fused
+    multiply-adds, unrolled), in a child process: (particle-iters/s, seconds)."""
+    env = dict(os.environ, PPS_ORACLE_BUILD="fast")
+    code = f"import bench; r, s = bench.cpu_oracle_rate({n}, {iters}, {threads}); print(r, s)"
+    out = subprocess.run([sys.executable, "-c", code], cwd=str(ROOT), env=env, capture_output=True, text=True,
+                         check=True, timeout=900)
+    r, sec = out.stdout.split()[-2:]
+    return float(r), float(sec)
+
+
 def run_reference(args, rank, world):
     """--impl reference: the oracle's CPU implementation on the same metric."""
     if rank != 0:
@@ -882,7 +893,13 @@ def main():
         rate, secs = cpu_oracle_rate(n_s, it_s, threads)
         cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"{n_s} particles x {DIM}-D Rastrigin, {it_s} sync iterations ({secs:.1f} s), "
-                         "C restatement threaded over particles"}
+                         "C restatement threaded over particles (-O2, no contraction: the checker's bits)"}
+        try:
+            frate, fsecs = cpu_oracle_rate_fast(n_s, it_s, threads)
+            cpu["fast_build"] = {"value": frate, "unit": UNIT, "seconds": fsecs,
+                                 "flags": "-O3 -ffp-contract=fast -funroll-loops (timing only: different bits)"}
+        except Exception as e:  # the figure is informative; the baseline above stands without it
+            cpu["fast_build"] = {"unavailable": f"{type(e).__name__}: {e}"[:200]}
 
     if rank == 0:
         line = {

@@ -15,7 +15,10 @@ from pathlib import Path
 import numpy as np
 
 HERE = Path(__file__).resolve().parent
-LIB_PATH = HERE / "_build" / "libpps_oracle.so"
+# PPS_ORACLE_BUILD=fast loads the timing-only build (-O3, fused multiply-adds:
+# different bits), which only the CPU baseline's fast-build figure uses
+LIB_PATH = HERE / "_build" / ("libpps_oracle_fast.so" if os.environ.get("PPS_ORACLE_BUILD") == "fast"
+                              else "libpps_oracle.so")
 
 TAG_INIT = 0x494E4954
 TAG_STEP = 0x50534F31
