@@ -351,7 +351,34 @@ static int occupancy_of(int ppt, size_t smem) {
   return per_sm;
 }
 
+// The step kernels keep g, lb and ub (12 bytes per dim) in dynamic shared
+// memory.  Without opting in, a block gets 48 kB of static and dynamic shared
+// memory together, which 4096 dims (48 kB of dynamic) exceed: above
+// kSmemOptIn bytes every step kernel of the objective opts in.  Once per
+// objective and size, from sync_grid, which runs before any stream capture.
+constexpr size_t kSmemOptIn = 40 << 10;
+
+static int sync_smem_opt_in(const pps_swarm* s) {
+  const size_t smem = 3 * sizeof(float) * (size_t)s->dv.dim;
+  if (smem <= kSmemOptIn) return PPS_OK;
+  static thread_local size_t done[kBoundaryQuadratic + 1] = {};
+  if (s->objective < 0 || s->objective > kBoundaryQuadratic || done[s->objective] >= smem) return PPS_OK;
+  const int v = (int)smem;
+#define OPT_IN(O)                                                                                           \
+  do {                                                                                                      \
+    PPS_CUDA(cudaFuncSetAttribute(k_sync_step<O, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, v));       \
+    PPS_CUDA(cudaFuncSetAttribute(k_sync_step<O, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, v));       \
+    PPS_CUDA(cudaFuncSetAttribute(k_sync_step<O, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, v));       \
+    PPS_CUDA(cudaFuncSetAttribute(k_sync_step<O, 1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, v)); \
+  } while (0)
+  PPS_DISPATCH_SEPARABLE(s->objective, OPT_IN)
+#undef OPT_IN
+  done[s->objective] = smem;
+  return PPS_OK;
+}
+
 int sync_grid(pps_swarm* s) {
+  sync_smem_opt_in(s);  // a failure here resurfaces as the launch's own error
   int bulk_blocks = 0;
   sync_bulk_prepare(s, &bulk_blocks);  // the TMA-staged kernel's occupancy, resolved here outside any capture
   // resident blocks of the step kernel per SM (cached per objective, device, dim)
@@ -386,6 +413,7 @@ int sync_grid(pps_swarm* s) {
 
 int launch_sync_step(pps_swarm* s, float c1, float c2) {
   if (is_user(s->objective)) return launch_user_step(s, c1, c2);
+  if (int rc = sync_smem_opt_in(s)) return rc;
   if (s->dv.ncons == 0) {  // PPS_SYNC_KERNEL=bulk: the TMA-staged kernel where it applies
     bool taken = false;
     const int rc = launch_sync_step_bulk(s, c1, c2, &taken);

@@ -235,6 +235,10 @@ int user_prepare(pps_swarm* s) {
     k = reinterpret_cast<const void*>(u->k_step[ppt == 1 ? 0 : (ppt == 2 ? 1 : 2)]);
   }
   const size_t smem = 3 * sizeof(float) * (size_t)s->dv.dim;
+  // g, lb, ub in dynamic shared memory: beyond 40 kB (3414 dims) the kernel
+  // opts in to more than the default 48 kB of static + dynamic
+  if (smem > ((size_t)40 << 10))
+    PPS_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int per_sm = 0;
   PPS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, kUserThreads, smem));
   if (per_sm < 1) return set_error(PPS_EINVAL, "the objective's step kernel cannot be resident (dim %d)", s->dv.dim);
@@ -278,6 +282,9 @@ int launch_user_async(pps_swarm* s, int iters, float c1, float c2) {
   UserObjective* u = loaded_or_error(s->objective, &rc);
   if (!u) return rc;
   const size_t smem = 3 * sizeof(float) * (size_t)s->dv.dim;
+  if (smem > ((size_t)40 << 10))
+    PPS_CUDA(cudaFuncSetAttribute(reinterpret_cast<const void*>(u->k_async),
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int per_sm = 0;
   PPS_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, reinterpret_cast<const void*>(u->k_async),
                                                          kUserThreads, smem));
