@@ -7,7 +7,9 @@ particle in at most 32 lanes of 32 dims (dim <= 1024) and refuses more.  At
 those limits the state must still match the oracle bit for bit, through
 single steps and the graph-replayed run, for the registered kernels, a user
 objective and the no-allocation entry point; one past them is refused
-before any device work."""
+before any device work.  Particle indices are 32-bit unsigned (argmin keys,
+Philox counters): a swarm of more than 2^31 particles must move its last
+particles as the oracle does."""
 import ctypes
 
 import numpy as np
@@ -130,3 +132,52 @@ def test_one_past_max_dim_is_refused(pps):
                                    ub=np.full(D, 1.0, np.float32))
     with pytest.raises(pps.PPSError, match="4096"):
         pps.Swarm(prob, 8, seed=0)
+
+
+def test_particle_indices_past_2p31(pps, orc):
+    """2^31 + 4113 particles of 1-D Rastrigin (45 GB of state): the first 64
+    and the last 4113 particles, whose indices pass the int32 range, match
+    oracle shards of those ranges (each given the GPU's global best before
+    every step) through init and three iterations, and the global best is the
+    lowest-index argmin of all personal bests."""
+    n = (1 << 31) + 4113
+    D, seed = 1, 21
+    lb, ub = np.full(D, -5.12, np.float32), np.full(D, 5.12, np.float32)
+    prob = pps.OptimizationProblem(pps.rastrigin, np.zeros(D, np.float32), [10.0], lb=lb, ub=ub)
+    oprob = orc.OracleProblem(2, D, lb, ub, params=[10.0])
+    ranges = [(0, 64), (1 << 31, 4113)]
+    refs = [orc.OracleSwarm(oprob, count, seed, first=first, nglobal=n) for first, count in ranges]
+    fields = (("x", 0), ("v", 1), ("pbest", 2), ("pcost", 3), ("cost", 4))
+
+    def compare(sw, where):
+        for name, field in fields:
+            full = sw.get(field)
+            for (first, count), ref in zip(ranges, refs):
+                got = full[..., first:first + count]
+                want = getattr(ref, name)
+                assert np.array_equal(got, want, equal_nan=True), f"{where}: {name} of particles {first}+ differ"
+            del full
+
+    def give_gbest(sw):
+        u, c, i = sw.gbest()
+        rec = np.zeros((16 + 4 * D + 15) // 16 * 16, np.uint8)
+        rec[0:8] = np.frombuffer(np.uint64(orc.argmin_key(np.float32(c), i)).tobytes(), np.uint8)
+        rec[8:12] = np.frombuffer(np.float32(c).tobytes(), np.uint8)
+        rec[16:16 + 4 * D] = np.frombuffer(np.asarray(u, np.float32).tobytes(), np.uint8)
+        for ref in refs:
+            ref.apply(rec)
+
+    with pps.Swarm(prob, n, seed=seed) as sw:
+        sw.init()
+        for ref in refs:
+            ref.init()
+        compare(sw, "init")
+        for it in range(3):
+            give_gbest(sw)
+            sw.sync_run(1)
+            for ref in refs:
+                ref.sync_run(1)
+            compare(sw, f"iteration {it + 1}")
+        pcost = sw.get(3)
+        u, c, i = sw.gbest()
+        assert i == int(np.argmin(pcost)) and np.float32(c) == pcost.min()
