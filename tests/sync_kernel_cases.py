@@ -24,6 +24,7 @@ CASES = [
     ("sphere", 1, 300, -3.0, 3.0, [], 25, False),                 # one dim
     ("rastrigin", 1000, 1100, -5.12, 5.12, [10.0], 5, False),     # 12 kB of bounds beside the ring
     ("himmelblau", 2, 70000, -5.0, 5.0, [], 33, False),           # 137 tiles over the resident blocks
+    ("rastrigin", 4096, 96, -5.12, 5.12, [10.0], 3, False),       # the largest dim: 48 kB of bounds
 ]
 
 

@@ -6,8 +6,8 @@ oracle.  These run the cases of sync_kernel_cases.py once more in a child
 process with PPS_SYNC_KERNEL=bulk (k_sync_step_bulk: the swarm state streamed
 through a ring of shared-memory stages by bulk copies) and require the two
 final states to be identical bit for bit: ragged last tiles, odd and single
-dims, a dim whose bounds take 12 kB of shared memory beside the ring, many
-tiles per block, the graph-replayed run, and several ring shapes."""
+dims, dims whose bounds take 12 kB and 48 kB of shared memory beside the
+ring, many tiles per block, the graph-replayed run, and several ring shapes."""
 import os
 import subprocess
 import sys
