@@ -361,8 +361,12 @@ constexpr size_t kSmemOptIn = 40 << 10;
 static int sync_smem_opt_in(const pps_swarm* s) {
   const size_t smem = 3 * sizeof(float) * (size_t)s->dv.dim;
   if (smem <= kSmemOptIn) return PPS_OK;
+  // per objective: the size opted in and the device it was set on (function
+  // attributes belong to the device's context)
   static thread_local size_t done[kBoundaryQuadratic + 1] = {};
-  if (s->objective < 0 || s->objective > kBoundaryQuadratic || done[s->objective] >= smem) return PPS_OK;
+  static thread_local int done_dev[kBoundaryQuadratic + 1] = {};
+  if (s->objective < 0 || s->objective > kBoundaryQuadratic) return PPS_OK;
+  if (done[s->objective] >= smem && done_dev[s->objective] == s->device) return PPS_OK;
   const int v = (int)smem;
 #define OPT_IN(O)                                                                                           \
   do {                                                                                                      \
@@ -374,6 +378,7 @@ static int sync_smem_opt_in(const pps_swarm* s) {
   PPS_DISPATCH_SEPARABLE(s->objective, OPT_IN)
 #undef OPT_IN
   done[s->objective] = smem;
+  done_dev[s->objective] = s->device;
   return PPS_OK;
 }
 
