@@ -344,10 +344,10 @@ __device__ void run_swarm(const BatchSwarm& sw, BatchSmem& S, float* sg, float* 
 // ---------------------------------------------------------------- ODE fits
 template <int MODEL>
 __device__ void run_swarm_ode(const BatchSwarm& sw, BatchSmem& S, float* sg, float* slb, float* sub, uint8_t* flag,
-                              float* data, int rank, int C) {
+                              float* data, int rank, int C, float one) {
   const int D = sw.dim;
   const int64_t n = sw.n, ld = sw.ld;
-  const Range R = cta_range(n, C, rank, (int)blockDim.x);
+  const Range R = cta_range(n, C, rank, 2 * (int)blockDim.x);  // whole trips of two particles per thread
   const int64_t pb = R.pb, pe = R.pe;
   const uint32_t k0 = (uint32_t)sw.seed, k1 = (uint32_t)(sw.seed >> 32);
   const OdeCfg cfg = ode_cfg(sw.op, sw.ndata);
@@ -400,9 +400,9 @@ __device__ void run_swarm_ode(const BatchSwarm& sw, BatchSmem& S, float* sg, flo
   for (int it = 0; it < sw.maxiters; ++it) {
     const uint32_t t = (uint32_t)it;
     best = ~0ull;
-    for (int64_t i = pb + threadIdx.x; i < pe; i += blockDim.x) {
+    // moves particle i of this CTA's range; its new position in x
+    auto move = [&](int64_t i, float (&x)[4]) {
       const bool pending = flag[i - pb] != 0;
-      float x[4] = {0.0f, 0.0f, 0.0f, 0.0f};
       const Rand4 r0 = philox4x32_10((uint32_t)i, 0u, t, kTagStep, k0, k1);
       const Rand4 r1 = philox4x32_10((uint32_t)i, 1u, t, kTagStep, k0, k1);
       const float ra[4] = {u01(r0.a), u01(r0.c), u01(r1.a), u01(r1.c)};
@@ -423,7 +423,9 @@ __device__ void run_swarm_ode(const BatchSwarm& sw, BatchSmem& S, float* sg, flo
           x[d] = xd;
         }
       }
-      const float c = ode_loss<MODEL>(x, cfg, data);
+    };
+    // records particle i's cost c: personal best, flag, argmin candidate
+    auto settle = [&](int64_t i, float c) {
       const float pc = sw.pcost[i];
       const bool imp = c < pc;
       const float npc = imp ? c : pc;
@@ -432,6 +434,17 @@ __device__ void run_swarm_ode(const BatchSwarm& sw, BatchSmem& S, float* sg, flo
       flag[i - pb] = imp ? 1 : 0;
       const unsigned long long key = argmin_key(npc, (uint32_t)i);
       best = key < best ? key : best;
+    };
+    // two particles per trip, i and i + blockDim.x, their losses packed
+    // (ode_loss2: bit-identical to ode_loss of each)
+    for (int64_t i = pb + threadIdx.x; i < pe; i += 2 * (int64_t)blockDim.x) {
+      const int64_t j = i + blockDim.x;
+      float xa[4] = {0.0f, 0.0f, 0.0f, 0.0f}, xb[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+      move(i, xa);
+      if (j < pe) move(j, xb);
+      const float2 c = ode_loss2<MODEL>(xa, xb, cfg, data, one);
+      settle(i, c.x);
+      if (j < pe) settle(j, c.y);
     }
     win = swarm_min(best, S, flag, pb, C, &fromx);
     const uint32_t gi = (uint32_t)win;
@@ -452,10 +465,11 @@ __device__ void run_swarm_ode(const BatchSwarm& sw, BatchSmem& S, float* sg, flo
 // One swarm per cluster of C CTAs (C = 1: a plain CTA).  Dynamic shared
 // memory: g, lb, ub (3 * maxdim floats), ODE data (data_floats floats), the
 // flags of this CTA's particles (one chunk of bytes).  Separable objectives
-// and ODE fits are separate kernels so each gets the registers it needs.
+// and ODE fits are separate kernels so each gets the registers it needs; both
+// take the same arguments (`one`, a run-time 1.0f, is read by the ODE kernel).
 template <int PPT>
 __global__ void k_batch(const BatchSwarm* __restrict__ descs, const int* __restrict__ order, int C, int maxdim,
-                        int data_floats) {
+                        int data_floats, float one) {
   extern __shared__ float dsm[];
   __shared__ BatchSmem S;
   const int swarm = blockIdx.x / C;
@@ -474,8 +488,9 @@ __global__ void k_batch(const BatchSwarm* __restrict__ descs, const int* __restr
   }
 }
 
-__global__ void __launch_bounds__(1024, 1) k_batch_ode(const BatchSwarm* __restrict__ descs, const int* __restrict__ order, int C, int maxdim,
-                            int data_floats) {
+__global__ void __launch_bounds__(1024, 1) k_batch_ode(const BatchSwarm* __restrict__ descs,
+                                                      const int* __restrict__ order, int C, int maxdim,
+                                                      int data_floats, float one) {
   extern __shared__ float dsm[];
   __shared__ BatchSmem S;
   const int swarm = blockIdx.x / C;
@@ -487,9 +502,9 @@ __global__ void __launch_bounds__(1024, 1) k_batch_ode(const BatchSwarm* __restr
   float* data = dsm + 3 * maxdim;
   uint8_t* flag = reinterpret_cast<uint8_t*>(data + data_floats);
   if (sw.objective == kLvFit)
-    run_swarm_ode<kOdeLV>(sw, S, sg, slb, sub, flag, data, rank, C);
+    run_swarm_ode<kOdeLV>(sw, S, sg, slb, sub, flag, data, rank, C, one);
   else if (sw.objective == kFhnFit)
-    run_swarm_ode<kOdeFHN>(sw, S, sg, slb, sub, flag, data, rank, C);
+    run_swarm_ode<kOdeFHN>(sw, S, sg, slb, sub, flag, data, rank, C, one);
 }
 
 }  // namespace pps
@@ -638,9 +653,14 @@ LaunchGroup batch_group_of(const BatchSwarm& d, int threads, int ppt, int spread
   const int cmax = max_cluster();
   if (is_ode(d.objective)) {
     g.kind = 1;
+    // two particles per thread and trip (the packed RK4 losses): the
+    // smallest power-of-two block from 128 that covers half the particles
     const int tmax = ode_threads();
-    g.T = d.n <= 256 ? 256 : (d.n <= 512 || tmax <= 512 ? (tmax < 512 ? 256 : 512) : 1024);
-    const int64_t c = (d.n + g.T - 1) / g.T;
+    const int64_t half = (d.n + 1) / 2;
+    int T = 128;
+    while (T < half && T < 1024 && 2 * T <= tmax) T *= 2;
+    g.T = T;
+    const int64_t c = (d.n + 2 * (int64_t)g.T - 1) / (2 * (int64_t)g.T);
     g.C = (int)(c < cmax ? c : cmax);
   } else {
     g.kind = 0;
@@ -732,7 +752,8 @@ static int launch_clustered(Kernel kernel, cudaStream_t stream, const BatchSwarm
       cudaGetLastError();  // clear the query's error and try a smaller cluster
       continue;
     }
-    e = cudaLaunchKernelEx(&cfg, kernel, ddescs, dorder + g.offset, C, g.maxdim, g.data_floats);
+    // the last argument is a run-time 1.0f for the packed ODE losses (ode_loss2)
+    e = cudaLaunchKernelEx(&cfg, kernel, ddescs, dorder + g.offset, C, g.maxdim, g.data_floats, 1.0f);
     if (e != cudaSuccess) return cuda_error(e, "cudaLaunchKernelEx(batch)");
     return PPS_OK;
   }
@@ -741,7 +762,7 @@ static int launch_clustered(Kernel kernel, cudaStream_t stream, const BatchSwarm
 
 int batch_launch_group(cudaStream_t stream, const BatchSwarm* ddescs, const int* dorder, const LaunchGroup& g,
                        int ppt) {
-  if (g.kind == 1) return launch_clustered(k_batch_ode, stream, ddescs, dorder, g, g.T);
+  if (g.kind == 1) return launch_clustered(k_batch_ode, stream, ddescs, dorder, g, 2 * g.T);
   if (ppt == 4) return launch_clustered(k_batch<4>, stream, ddescs, dorder, g, g.T * 4);
   if (ppt == 2) return launch_clustered(k_batch<2>, stream, ddescs, dorder, g, g.T * 2);
   return launch_clustered(k_batch<1>, stream, ddescs, dorder, g, g.T);

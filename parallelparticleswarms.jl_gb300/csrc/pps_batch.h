@@ -53,8 +53,9 @@ int batch_describe(const pps_problem* prob, int64_t n, uint64_t seed, int32_t ma
 size_t batch_smem_bytes(int maxdim, int data_floats, int64_t maxchunk);
 // the (kind, T, C) a swarm is launched with: separable swarms use the
 // batch's block size and about `spread` particles per thread per iteration
-// (8 by default; fewer split a swarm over more CTAs), ODE fits one particle
-// per thread (up to 1024 threads per CTA), both split over up to 16 CTAs
+// (8 by default; fewer split a swarm over more CTAs), ODE fits two particles
+// per thread (their RK4 losses packed; up to 1024 threads per CTA), both
+// split over up to 16 CTAs
 LaunchGroup batch_group_of(const BatchSwarm& d, int threads, int ppt, int spread = 8);
 // group swarms by (kind, T, C); order lists descriptor indices group by
 // group, longest estimated work first inside each group

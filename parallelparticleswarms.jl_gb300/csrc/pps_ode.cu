@@ -6,8 +6,8 @@
 // solve, _reduce_losses!, ode_update_particle_costs! (:26-41) and a host
 // minimum -- about five launches and five synchronisations.  Here the whole
 // iteration is one launch: update, RK4 integration, SSE, personal best and
-// the argmin publication fused, one thread per particle, observations in
-// shared memory.
+// the argmin publication fused, one thread per particle (two with packed
+// RK4 losses for large swarms), observations in shared memory.
 //
 // The reference clamps with max(position, lb) on whole SVectors
 // (src/ode_pso.jl:18-19), which compares lexicographically; this build
@@ -23,23 +23,39 @@
 namespace pps {
 
 constexpr int kOdeThreads = 128;
+// The step kernel's launch bounds ask for 4 resident blocks per SM: without
+// them the assembler sizes the kernel for full occupancy (32 registers),
+// which slows the integrators' dependent chains; with them it takes the 36-56
+// registers the integrators use.
+constexpr int kOdeStepMinBlocks = 4;
 constexpr int kOdeMaxDim = 4;
 
-// dynamic shared memory of a launch: the fixed-step Tsit5 saves' weight table
+// dynamic shared memory of a launch: the observations (2 floats per save),
+// then the fixed-step Tsit5 saves' weight table (8 floats per save)
 inline size_t ode_dyn_smem(const OdeCfg& c) {
-  return c.method == kOdeTsit5 ? sizeof(float) * 8 * (size_t)c.nsaves : 0;
+  return sizeof(float) * (size_t)c.nsaves * (c.method == kOdeTsit5 ? 10 : 2);
 }
 
-// builds the block's save table (fixed-step Tsit5 only; every thread calls it)
+// the block's dynamic shared memory: the observations at 0, the fixed-step
+// Tsit5 save table behind them.  Kernels index it directly so the compiler
+// keeps its loads in the shared address space.
+extern __shared__ float ode_smem[];
+
+// copies the observations to shared memory and builds the save table
+// (fixed-step Tsit5 only); every thread calls it, and it ends in a barrier
 template <int METHOD>
-__device__ __forceinline__ float* ode_table(const OdeCfg& c) {
-  extern __shared__ float ode_tab[];
-  if constexpr (METHOD == kOdeTsit5) {
-    tsit5_table_build(c, ode_tab);
-    __syncthreads();
-  }
-  return ode_tab;
+__device__ __forceinline__ void ode_smem_fill(const OdeCfg& c, const float* __restrict__ data_g) {
+  for (int k = threadIdx.x; k < 2 * c.nsaves; k += blockDim.x) ode_smem[k] = data_g[k];
+  if constexpr (METHOD == kOdeTsit5) tsit5_table_build(c, ode_smem + 2 * c.nsaves);
+  __syncthreads();
 }
+
+// Particles per thread of the step kernel: 1, or 2 for RK4 losses packed in
+// f32x2 (ode_loss2).  The packed form issues half the instructions but its
+// dependent chain is slower, so it pays only when the swarm fills the GPU
+// several times over (a throughput-bound launch); a smaller swarm, whose
+// launch is latency-bound, keeps one particle per thread.
+constexpr int64_t kOdePackedMinParticles = (int64_t)1 << 18;
 
 template <int MODEL, int METHOD>
 __device__ __forceinline__ float ode_eval(const float (&x)[kOdeMaxDim], const OdeCfg& c, const float* data,
@@ -53,10 +69,9 @@ template <int MODEL, int METHOD>
 __global__ void __launch_bounds__(kOdeThreads) k_init_ode(SwarmDev s, ObjParams op, OdeCfg cfg,
                                                           const float* __restrict__ data_g, uint64_t seed,
                                                           int sampler, const float* __restrict__ u0) {
-  __shared__ float data[2 * kOdeMaxSaves];
-  for (int k = threadIdx.x; k < 2 * cfg.nsaves; k += blockDim.x) data[k] = data_g[k];
-  const float* tab = ode_table<METHOD>(cfg);
-  __syncthreads();
+  ode_smem_fill<METHOD>(cfg, data_g);
+  const float* data = ode_smem;
+  const float* tab = ode_smem + 2 * cfg.nsaves;
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
   const int D = s.dim;
@@ -96,31 +111,35 @@ __global__ void __launch_bounds__(kOdeThreads) k_init_ode(SwarmDev s, ObjParams 
   if (publish_block_min(key, s.st)) finish_iteration(s, false, 0u, s.st->w);
 }
 
-template <int MODEL, int METHOD>
-__global__ void __launch_bounds__(kOdeThreads) k_sync_step_ode(SwarmDev s, ObjParams op, OdeCfg cfg,
+template <int MODEL, int METHOD, int PPT>
+__global__ void __launch_bounds__(kOdeThreads, kOdeStepMinBlocks) k_sync_step_ode(SwarmDev s, ObjParams op, OdeCfg cfg,
                                                                const float* __restrict__ data_g, uint64_t seed,
-                                                               float c1, float c2, int from_position) {
-  __shared__ float data[2 * kOdeMaxSaves];
+                                                               float c1, float c2, int from_position, float one) {
+  static_assert(PPT == 1 || (PPT == 2 && METHOD == kOdeRk4), "two particles per thread: RK4 only");
   __shared__ float sg[kOdeMaxDim], slb[kOdeMaxDim], sub[kOdeMaxDim];
   IterState* st = s.st;
   const uint32_t t = st->t;
   const float w = st->w;
   const int D = s.dim;
-  for (int k = threadIdx.x; k < 2 * cfg.nsaves; k += blockDim.x) data[k] = data_g[k];
   if (threadIdx.x < D) {
     sg[threadIdx.x] = s.g[threadIdx.x];
     slb[threadIdx.x] = s.lb[threadIdx.x];
     sub[threadIdx.x] = s.ub[threadIdx.x];
   }
-  const float* tab = ode_table<METHOD>(cfg);
-  __syncthreads();
+  ode_smem_fill<METHOD>(cfg, data_g);
+  const float* data = ode_smem;
+  const float* tab = ode_smem + 2 * cfg.nsaves;
   const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  unsigned long long key = ~0ull;
-  if (i < s.npad) {
-    const bool valid = i < s.n;
+  // this thread's particles: i0 (and i0 + blockDim.x) of the block's tile
+  const int64_t i0 = (int64_t)blockIdx.x * blockDim.x * PPT + threadIdx.x;
+  float x[PPT][kOdeMaxDim];
+#pragma unroll
+  for (int q = 0; q < PPT; ++q) {
+    const int64_t i = i0 + (int64_t)q * blockDim.x;
+#pragma unroll
+    for (int d = 0; d < kOdeMaxDim; ++d) x[q][d] = 0.0f;
+    if (i >= s.npad) continue;
     const bool pending = s.flag[i] != 0;
-    float x[kOdeMaxDim] = {0.0f, 0.0f, 0.0f, 0.0f};
     const Rand4 r0 = philox4x32_10((uint32_t)i, 0u, t, kTagStep, k0, k1);
     const Rand4 r1 = philox4x32_10((uint32_t)i, 1u, t, kTagStep, k0, k1);
     const float ra[4] = {u01(r0.a), u01(r0.c), u01(r1.a), u01(r1.c)};  // r1 draws of dims 0..3
@@ -140,17 +159,34 @@ __global__ void __launch_bounds__(kOdeThreads) k_sync_step_ode(SwarmDev s, ObjPa
         xd = clamp_lb_ub(__fadd_rn(xd, vd), slb[d], sub[d]);
         s.X[o] = xd;
         s.V[o] = vd;
-        x[d] = xd;
+        x[q][d] = xd;
       }
     }
-    const float c = ode_eval<MODEL, METHOD>(x, cfg, data, tab);
+  }
+  float c[PPT];
+  if constexpr (PPT == 2) {
+    const float2 cc = ode_loss2<MODEL>(x[0], x[1], cfg, data, one);
+    c[0] = cc.x;
+    c[1] = cc.y;
+  } else {
+    c[0] = ode_eval<MODEL, METHOD>(x[0], cfg, data, tab);
+  }
+  unsigned long long key = ~0ull;
+#pragma unroll
+  for (int q = 0; q < PPT; ++q) {
+    const int64_t i = i0 + (int64_t)q * blockDim.x;
+    if (i >= s.npad) continue;
+    const bool valid = i < s.n;
     float pc = s.pcost[i];
-    const bool improved = valid && c < pc;
-    pc = improved ? c : pc;
+    const bool improved = valid && c[q] < pc;
+    pc = improved ? c[q] : pc;
     s.pcost[i] = pc;
-    s.cost[i] = c;
+    s.cost[i] = c[q];
     s.flag[i] = improved ? 1 : 0;
-    if (valid) key = argmin_key(pc, (uint32_t)i);
+    if (valid) {
+      const unsigned long long k = argmin_key(pc, (uint32_t)i);
+      key = k < key ? k : key;
+    }
   }
   if (publish_block_min(key, st)) finish_iteration(s, from_position != 0, t + 1u, __fmul_rn(w, st->wdamp));
 }
@@ -220,8 +256,9 @@ __global__ void k_eval_ode(ObjParams op, OdeCfg cfg, const float* __restrict__ d
                            int64_t npts, int64_t stride, float* __restrict__ f);
 
 // The fixed-step Tsit5 kernels' dynamic shared-memory limit is raised once
-// per device to the largest save table (init precedes every captured run of
-// a swarm, so captured launches need no attribute call).
+// per device to the largest observations + save table (init precedes every
+// captured run of a swarm, so captured launches need no attribute call); the
+// other methods stay within the default 48 KB (2 floats per save).
 static int ode_set_smem_limit() {
   static std::mutex mu;
   static bool done[64] = {};
@@ -230,10 +267,10 @@ static int ode_set_smem_limit() {
   if (dev < 0 || dev >= 64) return set_error(PPS_ENOTSUP, "device %d out of range", dev);
   std::lock_guard<std::mutex> lock(mu);
   if (done[dev]) return PPS_OK;
-  const int smem = (int)(sizeof(float) * 8 * kOdeMaxSaves);
+  const int smem = (int)(sizeof(float) * 10 * kOdeMaxSaves);
 #define PPS_ODE_SMEM(M)                                                                                         \
   PPS_CUDA(cudaFuncSetAttribute(k_init_ode<M, kOdeTsit5>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));      \
-  PPS_CUDA(cudaFuncSetAttribute(k_sync_step_ode<M, kOdeTsit5>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)); \
+  PPS_CUDA(cudaFuncSetAttribute(k_sync_step_ode<M, kOdeTsit5, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem)); \
   PPS_CUDA(cudaFuncSetAttribute(k_eval_ode<M, kOdeTsit5>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem))
   PPS_ODE_SMEM(kOdeLV);
   PPS_ODE_SMEM(kOdeFHN);
@@ -246,7 +283,7 @@ int launch_init_ode(pps_swarm* s, int sampler, const float* u0_dev) {
   const unsigned blocks = (unsigned)((s->dv.npad + kOdeThreads - 1) / kOdeThreads);
   const OdeCfg c = cfg_of(s);
   const size_t dsm = ode_dyn_smem(c);
-  if (dsm) {
+  if (c.method == kOdeTsit5) {
     const int rc = ode_set_smem_limit();
     if (rc) return rc;
   }
@@ -259,13 +296,23 @@ int launch_init_ode(pps_swarm* s, int sampler, const float* u0_dev) {
 }
 
 int launch_sync_step_ode(pps_swarm* s, float c1, float c2) {
-  const unsigned blocks = (unsigned)((s->dv.npad + kOdeThreads - 1) / kOdeThreads);
   const OdeCfg c = cfg_of(s);
+  const int ppt = (c.method == kOdeRk4 && s->dv.npad >= kOdePackedMinParticles) ? 2 : 1;
+  const int64_t tile = (int64_t)kOdeThreads * ppt;
+  const unsigned blocks = (unsigned)((s->dv.npad + tile - 1) / tile);
   const int from_pos = (s->flags & PPS_FLAG_GBEST_FROM_POSITION) ? 1 : 0;
   const size_t dsm = ode_dyn_smem(c);
+  // the last argument, 1.0f, is the packed losses' run-time one
 #define L_STEP_ODE(M, I)                                                                                   \
-  k_sync_step_ode<M, I><<<blocks, kOdeThreads, dsm, s->stream>>>(s->dv, s->op, c, s->od.data, s->seed, c1, c2, \
-                                                                 from_pos)
+  do {                                                                                                     \
+    if (I == kOdeRk4 && ppt == 2)                                                                          \
+      k_sync_step_ode<M, kOdeRk4, 2><<<blocks, kOdeThreads, dsm, s->stream>>>(s->dv, s->op, c, s->od.data, \
+                                                                              s->seed, c1, c2, from_pos,  \
+                                                                              1.0f);                      \
+    else                                                                                                   \
+      k_sync_step_ode<M, I, 1><<<blocks, kOdeThreads, dsm, s->stream>>>(s->dv, s->op, c, s->od.data,       \
+                                                                        s->seed, c1, c2, from_pos, 1.0f);  \
+  } while (0)
   PPS_DISPATCH_ODE(s->objective, c.method, L_STEP_ODE);
 #undef L_STEP_ODE
   PPS_CUDA(cudaGetLastError());
@@ -275,10 +322,9 @@ int launch_sync_step_ode(pps_swarm* s, float c1, float c2) {
 template <int MODEL, int METHOD>
 __global__ void k_eval_ode(ObjParams op, OdeCfg cfg, const float* __restrict__ data_g, const float* __restrict__ x,
                            int64_t npts, int64_t stride, float* __restrict__ f) {
-  __shared__ float data[2 * kOdeMaxSaves];
-  for (int k = threadIdx.x; k < 2 * cfg.nsaves; k += blockDim.x) data[k] = data_g[k];
-  const float* tab = ode_table<METHOD>(cfg);
-  __syncthreads();
+  ode_smem_fill<METHOD>(cfg, data_g);
+  const float* data = ode_smem;
+  const float* tab = ode_smem + 2 * cfg.nsaves;
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= npts) return;
   float p[kOdeMaxDim] = {0.0f, 0.0f, 0.0f, 0.0f};
@@ -293,7 +339,7 @@ int launch_eval_ode(const ObjParams& op, const ObjData& od, int objective, const
   const unsigned blocks = (unsigned)((npts + 127) / 128);
   const OdeCfg c = ode_cfg(op, od.ndata);
   const size_t dsm = ode_dyn_smem(c);
-  if (dsm) {
+  if (c.method == kOdeTsit5) {
     const int rc = ode_set_smem_limit();
     if (rc) return rc;
   }

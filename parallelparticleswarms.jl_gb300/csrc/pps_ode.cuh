@@ -124,6 +124,76 @@ __device__ __forceinline__ float ode_loss(const float* p, const OdeCfg& c, const
   return acc;
 }
 
+// ---------------------------------------------------------------- RK4, two particles at once
+// ode_loss of two particles (lane x: xa, lane y: xb) with Blackwell's packed
+// f32x2 instructions: each lane runs exactly ode_loss's operations, one
+// instruction issue for both, bit-identical to two ode_loss calls.
+// The assembler contracts a packed multiply whose only use is a packed add
+// into one fused f32x2 multiply-add, even under -fmad=false and with .rn on
+// both, which changes the rounding (scalar multiplies and adds are left
+// alone).  So every add of a product is written here as fma(product, one,
+// other) with `one` a run-time 1.0f (a kernel argument the compiler cannot
+// see through): product * 1 is exact, so it rounds once, as the add does.
+namespace rk4x2 {
+__device__ __forceinline__ float2 dup(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 neg(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ float2 fma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 mul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+// a + b, a or b possibly a product
+__device__ __forceinline__ float2 add(float2 a, float2 b, float2 one) { return __ffma2_rn(a, one, b); }
+
+template <int MODEL>
+__device__ __forceinline__ void rhs(const float2 (&p)[4], float2 l, float2 one, float2 u0, float2 u1, float2& d0,
+                                    float2& d1) {
+  if constexpr (MODEL == kOdeLV) {
+    d0 = mul(u0, fma(neg(p[1]), u1, p[0]));
+    d1 = mul(u1, fma(p[3], u0, neg(p[2])));
+  } else {
+    const float2 v3 = mul(mul(u0, u0), u0);
+    d0 = add(add(fma(v3, dup(-0x1.555556p-2f), u0), neg(u1), one), l, one);
+    d1 = mul(p[2], fma(neg(p[1]), u1, add(u0, p[0], one)));
+  }
+}
+}  // namespace rk4x2
+
+template <int MODEL>
+__device__ __forceinline__ float2 ode_loss2(const float* pa, const float* pb, const OdeCfg& c, const float* data,
+                                            float one_) {
+  using namespace rk4x2;
+  const float2 one = dup(one_);
+  float2 p[4];
+#pragma unroll
+  for (int d = 0; d < 4; ++d) p[d] = make_float2(pa[d], pb[d]);
+  const float2 l = make_float2(ode_l(pa, c), ode_l(pb, c));
+  const float dt = c.dt;
+  const float2 h2 = dup(__fmul_rn(dt, 0.5f)), h6 = dup(__fdiv_rn(dt, 6.0f)), dt2 = dup(dt), two = dup(2.0f);
+  float2 u0 = dup(c.u0a), u1 = dup(c.u0b);
+  float2 e0 = add(dup(data[0]), neg(u0), one), e1 = add(dup(data[1]), neg(u1), one);
+  float2 acc = add(mul(e0, e0), mul(e1, e1), one);
+  for (int m = 1; m < c.nsaves; ++m) {
+#pragma unroll 2
+    for (int k = 0; k < c.save_every; ++k) {
+      float2 k1a, k1b, k2a, k2b, k3a, k3b, k4a, k4b;
+      rhs<MODEL>(p, l, one, u0, u1, k1a, k1b);
+      rhs<MODEL>(p, l, one, fma(h2, k1a, u0), fma(h2, k1b, u1), k2a, k2b);
+      rhs<MODEL>(p, l, one, fma(h2, k2a, u0), fma(h2, k2b, u1), k3a, k3b);
+      rhs<MODEL>(p, l, one, fma(dt2, k3a, u0), fma(dt2, k3b, u1), k4a, k4b);
+      float2 sa = fma(two, k2a, k1a);
+      sa = fma(two, k3a, sa);
+      sa = add(k4a, sa, one);
+      float2 sb = fma(two, k2b, k1b);
+      sb = fma(two, k3b, sb);
+      sb = add(k4b, sb, one);
+      u0 = fma(h6, sa, u0);
+      u1 = fma(h6, sb, u1);
+    }
+    e0 = add(dup(data[2 * m]), neg(u0), one);
+    e1 = add(dup(data[2 * m + 1]), neg(u1), one);
+    acc = add(acc, add(mul(e0, e0), mul(e1, e1), one), one);
+  }
+  return acc;
+}
+
 // ---------------------------------------------------------------- Tsit5
 // Tsitouras, "Runge-Kutta pairs of order 5(4) satisfying only the first
 // column simplifying assumption", Comput. Math. Appl. 62 (2011) 770-775: the

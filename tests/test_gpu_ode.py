@@ -22,6 +22,24 @@ def test_ode_sync_matches_oracle_every_iteration(pps, orc, model, n, iters):
             assert_state_equal(sw, ref, f"iteration {it + 1}")
 
 
+@pytest.mark.parametrize("model,n", [("lv", (1 << 18) + 3), ("fhn", (1 << 18) + 70)])
+def test_large_ode_swarm_packed_step_matches_oracle(pps, orc, model, n):
+    """Swarms of at least 2^18 particles step two particles per thread with
+    their RK4 losses packed in f32x2 (kOdePackedMinParticles): the state must
+    stay bit-identical to the oracle's scalar arithmetic; n is ragged so the
+    last tile's second lane is partly empty."""
+    prob, _ = pps.ode.synthetic_fit(model, 11)
+    op = oracle_ode_problem(orc, prob)
+    with pps.Swarm(prob, n, seed=21) as sw:
+        sw.init()
+        ref = orc.OracleSwarm(op, n, 21).init()
+        assert_state_equal(sw, ref, "init")
+        for it in range(2):
+            sw.sync_run(1)
+            ref.sync_run(1)
+            assert_state_equal(sw, ref, f"iteration {it + 1}")
+
+
 def test_ode_objective_matches_oracle(pps, orc):
     rng = np.random.default_rng(0)
     for model in ("lv", "fhn"):
