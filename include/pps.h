@@ -244,7 +244,8 @@ typedef struct pps_serve_config {
                              of their own with the multi-block step kernels, like a
                              plain solve, instead of in a batched launch (0: 2048,
                              negative: only MLP fits, which always do) */
-  int32_t reserved;
+  int32_t ode_single_min_n; /* the same threshold for ODE fits (0: single_min_n; negative:
+                             ODE fits of any size are batched) */
 } pps_serve_config;
 typedef struct pps_serve_stats {
   uint64_t submitted, completed, launches;

@@ -52,9 +52,10 @@ __device__ __forceinline__ void ode_smem_fill(const OdeCfg& c, const float* __re
 
 // Particles per thread of the step kernel: 1, or 2 for RK4 losses packed in
 // f32x2 (ode_loss2).  The packed form issues half the instructions but its
-// dependent chain is slower, so it pays only when the swarm fills the GPU
-// several times over (a throughput-bound launch); a smaller swarm, whose
-// launch is latency-bound, keeps one particle per thread.
+// dependent chain is slower, so it pays only when the launch is
+// throughput-bound: a swarm that fills the GPU several times over, or a
+// swarm run by the request server beside other launches.  A smaller swarm
+// solved alone, whose launch is latency-bound, keeps one particle per thread.
 constexpr int64_t kOdePackedMinParticles = (int64_t)1 << 18;
 
 template <int MODEL, int METHOD>
@@ -297,7 +298,8 @@ int launch_init_ode(pps_swarm* s, int sampler, const float* u0_dev) {
 
 int launch_sync_step_ode(pps_swarm* s, float c1, float c2) {
   const OdeCfg c = cfg_of(s);
-  const int ppt = (c.method == kOdeRk4 && s->dv.npad >= kOdePackedMinParticles) ? 2 : 1;
+  const bool served = !s->owns_memory;  // state carved from a server's arena
+  const int ppt = (c.method == kOdeRk4 && (s->dv.npad >= kOdePackedMinParticles || served)) ? 2 : 1;
   const int64_t tile = (int64_t)kOdeThreads * ppt;
   const unsigned blocks = (unsigned)((s->dv.npad + tile - 1) / tile);
   const int from_pos = (s->flags & PPS_FLAG_GBEST_FROM_POSITION) ? 1 : 0;

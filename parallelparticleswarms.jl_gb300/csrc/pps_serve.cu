@@ -4,12 +4,15 @@
 // duration.  This server admits optimization problems as they arrive and
 // solves small swarms in the batched kernel (one CTA or cluster per swarm,
 // all iterations in one launch, pps_batch.cu).  Large swarms (at least
-// `single_min_n` particles) and MLP fits, whose loss runs on the tensor cores
-// with one CTA per SM and tile (pps_mlp.cu), run instead as a swarm of their
-// own on a launch slot with the multi-block step kernels of a plain solve
-// (state carved from the same arena, iterations replayed as a CUDA graph, the
-// result written to the request's mailbox by a last kernel), concurrently
-// with the batched launches on the other slots:
+// `single_min_n` particles, or `ode_single_min_n` for ODE fits) and MLP fits,
+// whose loss runs on the tensor cores with one CTA per SM and tile
+// (pps_mlp.cu), run instead as a swarm of their own on a launch slot with the
+// multi-block step kernels of a plain solve (state carved from the same
+// arena, iterations replayed as a CUDA graph, the result written to the
+// request's mailbox by a last kernel), concurrently with the batched launches
+// on the other slots.  Every other slot's stream has the device's highest
+// priority and batched launches prefer those, so their persistent CTAs are
+// placed ahead of the per-iteration blocks of the swarms run on their own:
 //
 //   submit()  validates the problem, stamps the arrival time and queues it.
 //   worker    one host thread that, in a loop,
@@ -78,6 +81,7 @@ struct Request {
 
 struct Slot {
   cudaStream_t stream = nullptr;
+  bool high = false;             // a high-priority stream (preferred by batched launches)
   cudaEvent_t done = nullptr;
   BatchSwarm* ddescs = nullptr;
   int* dorder = nullptr;
@@ -247,14 +251,20 @@ void worker_main(pps_server* s) {
       for (Slot& sl : s->slots) busy |= sl.busy;
       if (!busy) break;
     }
-    Slot* free_slot = nullptr;
+    Slot *free_slot = nullptr, *free_high = nullptr, *free_low = nullptr;
     int inflight = 0;
     for (Slot& sl : s->slots) {
       if (sl.busy)
         ++inflight;
-      else if (!free_slot)
-        free_slot = &sl;
+      else if (sl.high && !free_high)
+        free_high = &sl;
+      else if (!sl.high && !free_low)
+        free_low = &sl;
     }
+    // a swarm of its own prefers a normal-priority slot, a batched launch a
+    // high-priority one; either takes the other kind when its own is busy
+    const bool head_single = !s->queue.empty() && s->queue.front()->single;
+    free_slot = head_single ? (free_low ? free_low : free_high) : (free_high ? free_high : free_low);
     if (free_slot && !s->queue.empty() && s->queue.front()->single) {
       Request* r = s->queue.front();
       size_t off;
@@ -360,8 +370,19 @@ int pps_serve_start(const pps_serve_config* cfg_in, pps_server** out) {
   s->arena.reset(cfg.memory_budget);
   s->slots.resize(cfg.max_launches);
   const size_t mail_floats = (size_t)cfg.max_pack * (kBatchMaxDim + 2);
+  // every other slot's stream has the device's highest priority: batched
+  // launches take those, so their persistent CTAs are placed ahead of the
+  // blocks of swarms run on their own, which relaunch every iteration
+  int prio_low = 0, prio_high = 0;
+  if ((e = cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high)) != cudaSuccess) {
+    const int rc = cuda_error(e, "cudaDeviceGetStreamPriorityRange");
+    pps_serve_stop(s);
+    return rc;
+  }
+  for (size_t k = 0; k < s->slots.size(); ++k) s->slots[k].high = (k % 2) == 0;
   for (Slot& sl : s->slots) {
-    if ((e = cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking)) != cudaSuccess ||
+    if ((e = cudaStreamCreateWithPriority(&sl.stream, cudaStreamNonBlocking, sl.high ? prio_high : prio_low)) !=
+            cudaSuccess ||
         (e = cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming)) != cudaSuccess ||
         (e = cudaMalloc(&sl.ddescs, sizeof(BatchSwarm) * cfg.max_pack)) != cudaSuccess ||
         (e = cudaMalloc(&sl.dorder, sizeof(int) * cfg.max_pack)) != cudaSuccess ||
@@ -391,8 +412,10 @@ int pps_serve_submit(pps_server* s, const pps_problem* prob, int64_t n, uint64_t
   // own with the multi-block step kernels; the rest are packed into batched
   // launches
   const bool tsit5 = prob && is_ode(prob->objective) && prob->nparams > 6 && prob->params && prob->params[6] != 0.0f;
+  const int32_t min_n = prob && is_ode(prob->objective) && s->cfg.ode_single_min_n != 0 ? s->cfg.ode_single_min_n
+                                                                                        : s->cfg.single_min_n;
   const bool single = prob && (prob->objective == kMlp || prob->ncons > 0 || is_user(prob->objective) || tsit5 ||
-                               (s->cfg.single_min_n > 0 && n >= s->cfg.single_min_n));
+                               (min_n > 0 && n >= min_n));
   if (single) {
     int rc = swarm_check(prob, n);
     if (!rc && prob->dim > kBatchMaxDim)

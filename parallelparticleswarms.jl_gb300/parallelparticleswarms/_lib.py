@@ -89,7 +89,7 @@ class ServeConfig(ctypes.Structure):
         ("ppt", ctypes.c_int32),
         ("tick_us", ctypes.c_double),
         ("single_min_n", ctypes.c_int32),
-        ("reserved", ctypes.c_int32),
+        ("ode_single_min_n", ctypes.c_int32),
     ]
 
 

@@ -16,13 +16,15 @@ class Server:
     thread that packs admitted problems into batched launches."""
 
     def __init__(self, memory_budget: int = 8 << 30, max_launches: int = 8, max_pack: int = 512, threads: int = 256,
-                 ppt: int = 1, tick_us: float = 200.0, single_min_n: int = 0):
+                 ppt: int = 1, tick_us: float = 200.0, single_min_n: int = 0, ode_single_min_n: int = 0):
         """``single_min_n``: requests with at least this many particles run as
         a swarm of their own with the multi-block step kernels (0: the
-        library's default, 2048; negative: only MLP fits, which always do)."""
+        library's default, 2048; negative: only MLP fits, which always do).
+        ``ode_single_min_n``: the same threshold for ODE fits (0: follow
+        ``single_min_n``; negative: ODE fits of any size are batched)."""
         self._lib = _lib.load()
         cfg = _lib.ServeConfig(int(memory_budget), int(max_launches), int(max_pack), int(threads), int(ppt),
-                               float(tick_us), int(single_min_n), 0)
+                               float(tick_us), int(single_min_n), int(ode_single_min_n))
         self._h = ctypes.c_void_p()
         _lib.check(self._lib.pps_serve_start(ctypes.byref(cfg), ctypes.byref(self._h)))
         self._dims: dict[int, int] = {}

@@ -95,6 +95,25 @@ def test_large_requests_run_as_swarms_of_their_own(pps):
         assert i == ai and np.float32(c) == np.float32(ac) and np.array_equal(u, au)
 
 
+def test_ode_fits_routed_by_their_own_threshold(pps):
+    """ode_single_min_n routes ODE fits apart from the other requests: with
+    single_min_n = -1 every separable request is batched whatever its size,
+    while ODE fits of at least 64 particles run as swarms of their own (their
+    RK4 step packed two particles per thread, as for every swarm the server
+    runs) and smaller ones are batched; every result equals its solve alone."""
+    reqs = _stream(pps, 20, seed=13, objectives=NO_MLP)
+    for k in range(4):
+        prob, _ = pps.ode.synthetic_fit("lv" if k % 2 == 0 else "fhn", 70 + k)
+        reqs.append((prob, (40, 64, 200, 129)[k], (3, 4, 2, 3)[k], 300 + k))
+    with pps.Server(memory_budget=1 << 30, max_launches=6, max_pack=8, tick_us=50.0, single_min_n=-1,
+                    ode_single_min_n=64) as srv:
+        tickets = [srv.submit(p, n, maxiters=it, seed=s) for (p, n, it, s) in reqs]
+        results = [srv.wait(t) for t in tickets]
+    for (prob, n, iters, s), (u, c, i, lat) in zip(reqs, results):
+        au, ac, ai = _alone(pps, prob, n, iters, s)
+        assert i == ai and np.float32(c) == np.float32(ac) and np.array_equal(u, au)
+
+
 def test_poll_and_errors(pps):
     reqs = _stream(pps, 1, seed=5, objectives=NO_MLP)
     prob, n, iters, s = reqs[0]
