@@ -142,3 +142,31 @@ def test_adaptive_tsit5_served_equals_alone(pps):
         sw.sync_run(12)
         au, ac, ai = sw.gbest()
     assert i == ai and np.float32(c) == np.float32(ac) and np.array_equal(u, au)
+
+
+@pytest.mark.parametrize("method", ["rk4", "tsit5", "tsit5_adaptive"])
+def test_ode_fit_at_the_save_limit_matches_oracle(pps, orc, method):
+    """4096 saves (kOdeMaxSaves): the observations (32 KB) and, for Tsit5 at a
+    fixed step, the save table behind them (160 KB of dynamic shared memory
+    together, above the default 48 KB) -- init, single steps and a graph
+    replay bit-identical to the oracle."""
+    nsaves = 4096
+    t = np.arange(nsaves) * 0.005
+    data = pps.ode._dense64("lv", (1.5, 1.0, 3.0, 1.0), (1.0, 1.0), t).astype(np.float32)
+    if method == "rk4":
+        prob = pps.ode.lv_problem(data, dt=0.005, nsteps=nsaves - 1, save_every=1)
+    else:
+        prob = pps.ode.lv_problem(data, dt=0.01, nsteps=(nsaves - 1) // 2 + 1, save_every=1, method=method,
+                                  save_dt=0.005)
+    op = oracle_ode_problem(orc, prob)
+    n = 70
+    with pps.Swarm(prob, n, seed=6) as sw:
+        sw.init()
+        ref = orc.OracleSwarm(op, n, 6).init()
+        assert_state_equal(sw, ref, "init")
+        sw.sync_run(1)
+        ref.sync_run(1)
+        assert_state_equal(sw, ref, "iteration 1")
+        sw.sync_run(3)  # graph replay
+        ref.sync_run(3)
+        assert_state_equal(sw, ref, "graph")
