@@ -632,6 +632,25 @@ def run_served(pps, args, with_mlp=True) -> dict:
     out["plain_sample"] = len(sample)
     out["speedup_vs_plain"] = out["closed_loop"]["solves_per_s"] / plain
     out["same_result_alone_and_served"] = same
+    if not with_mlp:
+        # the same requests with every separable request batched whatever its size
+        # (ODE fits of 2048 particles or more still run on their own), packs of <= 32:
+        # more swarms per launch, each result the same as with the default routing
+        bcfg = dict(cfg, single_min_n=-1, ode_single_min_n=2048, max_pack=32)
+        with pps.Server(**bcfg) as srv:
+            t0 = time.perf_counter()
+            ts = [srv.submit(p, n, maxiters=it, seed=s) for (p, n, it, s) in reqs]
+            bres = [srv.wait(t) for t in ts]
+            bwall = time.perf_counter() - t0
+            bst = srv.stats()
+        out["closed_loop_batched_routing"] = {
+            "server": bcfg, "wall_s": bwall, "solves_per_s": len(reqs) / bwall,
+            "speedup_vs_plain": len(reqs) / bwall / plain, "p50_ms": bst["p50_ms"], "p99_ms": bst["p99_ms"],
+            "launches": bst["launches"], "mean_pack": bst["mean_pack"],
+            "same_results_as_default_routing": all(
+                np.array_equal(a[0], b[0], equal_nan=True) and np.array_equal(np.float32(a[1]), np.float32(b[1]),
+                                                                               equal_nan=True) and a[2] == b[2]
+                for a, b in zip(res, bres))}
     # open loop: Poisson arrivals at 2000/s over the window, then drain
     out["open_loop"] = _open_loop(pps, cfg, 2000.0, window, with_mlp, seed=2)
     out["open_loop"]["note"] = "offered load above the measured closed-loop capacity: latency includes queueing"
