@@ -53,6 +53,18 @@ struct PPSLocalOpts
     max_backtracks::Int32
 end
 
+# pps_serve_config
+struct PPSServeConfig
+    memory_budget::UInt64
+    max_launches::Int32
+    max_pack::Int32
+    threads::Int32
+    ppt::Int32
+    tick_us::Float64
+    single_min_n::Int32
+    ode_single_min_n::Int32
+end
+
 const SAMPLER_AUTO, SAMPLER_UNIFORM, SAMPLER_UNBOUNDED, SAMPLER_LHS = Int32(0), Int32(1), Int32(2), Int32(3)
 const FIELD_POSITION, FIELD_VELOCITY, FIELD_PBEST, FIELD_PCOST, FIELD_COST = Int32.(0:4)
 const LAYOUT_SOA, LAYOUT_AOS = Int32(0), Int32(1)
@@ -244,6 +256,73 @@ function solve_many(probs, n; maxiters = 100, w = 0.7298f0, wdamp = 1.0f0, c1 = 
     finally
         ccall((:pps_batch_destroy, lib()), Cint, (Ptr{Cvoid},), b[])
     end
+end
+
+# ---------------------------------------------------------------- serving
+"""A request server (pps_serve_*): problems submitted as they arrive are packed into batched
+launches or run as swarms of their own, with their state in a device arena of `memory_budget`
+bytes; every result equals the problem solved alone.  Zero settings take the library's
+defaults; `single_min_n` / `ode_single_min_n` route requests by particle count."""
+mutable struct PPSServer
+    h::Ptr{Cvoid}
+    dims::Dict{UInt64, Int}
+end
+
+function PPSServer(; memory_budget = 8 << 30, max_launches = 8, max_pack = 512, threads = 256, ppt = 1,
+                   tick_us = 200.0, single_min_n = 0, ode_single_min_n = 0)
+    cfg = Ref(PPSServeConfig(UInt64(memory_budget), Int32(max_launches), Int32(max_pack), Int32(threads),
+                             Int32(ppt), Float64(tick_us), Int32(single_min_n), Int32(ode_single_min_n)))
+    out = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:pps_serve_start, lib()), Cint, (Ref{PPSServeConfig}, Ref{Ptr{Cvoid}}), cfg, out))
+    srv = PPSServer(out[], Dict{UInt64, Int}())
+    finalizer(serve_stop!, srv)
+    return srv
+end
+
+"""Queue one problem (the library copies its buffers) and return its ticket."""
+function submit!(srv::PPSServer, prob, n::Integer; maxiters = 100, seed = 0, w = 0.7298f0, wdamp = 1.0f0,
+                 c1 = 1.4962f0, c2 = 1.4962f0)
+    cp, bufs = pps_problem(prob)
+    ticket = Ref{UInt64}(0)
+    GC.@preserve bufs check(ccall((:pps_serve_submit, lib()), Cint,
+                                  (Ptr{Cvoid}, Ref{PPSProblem}, Int64, UInt64, Int32, Float32, Float32, Float32,
+                                   Float32, Ref{UInt64}),
+                                  srv.h, cp, n, seed, maxiters, w, wdamp, c1, c2, ticket))
+    srv.dims[ticket[]] = length(prob.u0)
+    return ticket[]
+end
+
+"""(u, cost, index, latency in ms) of a finished request, or `nothing` while it runs."""
+function poll(srv::PPSServer, ticket::UInt64)
+    u = Vector{Float32}(undef, srv.dims[ticket])
+    cost, idx, lat = Ref{Float32}(), Ref{Int64}(), Ref{Float64}()
+    rc = ccall((:pps_serve_poll, lib()), Cint, (Ptr{Cvoid}, UInt64, Ptr{Float32}, Ref{Float32}, Ref{Int64}, Ref{Float64}),
+               srv.h, ticket, u, cost, idx, lat)
+    rc == 5 && return nothing  # PPS_EBUSY
+    check(rc)
+    delete!(srv.dims, ticket)
+    return u, cost[], idx[], lat[]
+end
+
+"""Block until the request is done (an error after `timeout_s` seconds); returns (u, cost, index,
+latency in ms)."""
+function wait_result(srv::PPSServer, ticket::UInt64; timeout_s = 600.0)
+    u = Vector{Float32}(undef, srv.dims[ticket])
+    cost, idx, lat = Ref{Float32}(), Ref{Int64}(), Ref{Float64}()
+    check(ccall((:pps_serve_wait, lib()), Cint,
+                (Ptr{Cvoid}, UInt64, Ptr{Float32}, Ref{Float32}, Ref{Int64}, Ref{Float64}, Float64),
+                srv.h, ticket, u, cost, idx, lat, Float64(timeout_s)))
+    delete!(srv.dims, ticket)
+    return u, cost[], idx[], lat[]
+end
+
+"""Finish the queued and running requests and release the server."""
+function serve_stop!(srv::PPSServer)
+    if srv.h != C_NULL
+        ccall((:pps_serve_stop, lib()), Cint, (Ptr{Cvoid},), srv.h)
+        srv.h = C_NULL
+    end
+    return nothing
 end
 
 # ---------------------------------------------------------------- sharded swarms
