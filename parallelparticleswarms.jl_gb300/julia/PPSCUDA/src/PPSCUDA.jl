@@ -53,6 +53,52 @@ struct PPSLocalOpts
     max_backtracks::Int32
 end
 
+# pps_swarm_info
+struct PPSSwarmInfo
+    n::Int64
+    dim::Int32
+    objective::Int32
+    iteration::UInt32
+    async_lanes::Int32
+    async_slice::Int32
+    device::Int32
+    seed::UInt64
+    device_bytes::UInt64
+end
+
+# pps_serve_stats
+struct PPSServeStats
+    submitted::UInt64
+    completed::UInt64
+    launches::UInt64
+    solves_per_s::Float64
+    p50_ms::Float64
+    p99_ms::Float64
+    mean_ms::Float64
+    max_ms::Float64
+    mean_pack::Float64
+    arena_bytes::UInt64
+    arena_peak_bytes::UInt64
+    queued::Int32
+    running::Int32
+end
+
+# pps_device_swarm: a swarm in device buffers the caller owns (device pointers, e.g.
+# reinterpret(Ptr{Float32}, pointer(a)) of a CUDA.jl CuArray a)
+struct PPSDeviceSwarm
+    n::Int64
+    ld::Int64
+    dim::Int32
+    x::Ptr{Float32}
+    v::Ptr{Float32}
+    pbest::Ptr{Float32}
+    pcost::Ptr{Float32}
+    cost::Ptr{Float32}
+    lb::Ptr{Float32}
+    ub::Ptr{Float32}
+    g::Ptr{Float32}
+end
+
 # pps_serve_config
 struct PPSServeConfig
     memory_budget::UInt64
@@ -74,6 +120,18 @@ function check(rc::Integer)
     msg = unsafe_string(ccall((:pps_last_error, lib()), Cstring, ()))
     rc == 1 ? throw(ArgumentError(msg)) : error("libpps_cuda.so status $rc: $msg")
 end
+
+# ---------------------------------------------------------------- library
+"""The C ABI version the library implements (this package is written against 100)."""
+version() = ccall((:pps_version, lib()), Int32, ())
+function device_count()
+    n = Ref{Int32}(0)
+    check(ccall((:pps_device_count, lib()), Cint, (Ref{Int32},), n))
+    return Int(n[])
+end
+"""Make `device` current for this thread: swarms are created on the current device (the
+reference picks it through its backend object)."""
+set_device!(device::Integer) = check(ccall((:pps_set_device, lib()), Cint, (Int32,), device))
 
 # ---------------------------------------------------------------- objectives
 # Registered objectives: Julia functions the user marks with their engine id.
@@ -147,6 +205,21 @@ function positions(s::PPSSwarm)
     return [SVector{s.dim}(view(x, i, :)) for i in 1:(s.n)]
 end
 
+"""One state field (FIELD_POSITION, _VELOCITY, _PBEST: n x dim; FIELD_PCOST, _COST: n) from the
+device, or written to it with `set_state!` (e.g. reinit! from given velocities)."""
+function state(s::PPSSwarm, field::Int32)
+    out = field in (FIELD_PCOST, FIELD_COST) ? Vector{Float32}(undef, s.n) : Matrix{Float32}(undef, s.n, s.dim)
+    check(ccall((:pps_get_state, lib()), Cint, (Ptr{Cvoid}, Int32, Ptr{Float32}), s.h, field, out))
+    return out
+end
+function set_state!(s::PPSSwarm, field::Int32, values::AbstractArray{<:Real})
+    v = Array{Float32}(values)
+    length(v) == (field in (FIELD_PCOST, FIELD_COST) ? s.n : s.n * s.dim) ||
+        throw(DimensionMismatch("field $field of this swarm has $(field in (FIELD_PCOST, FIELD_COST) ? s.n : s.n * s.dim) values"))
+    check(ccall((:pps_set_state, lib()), Cint, (Ptr{Cvoid}, Int32, Ptr{Float32}), s.h, field, v))
+    return s
+end
+
 """The swarm as the reference's particle records, `Vector{SPSOParticle}` (3 D + 2 floats each)."""
 function particles(s::PPSSwarm)
     D = s.dim
@@ -180,6 +253,42 @@ function run!(s::PPSSwarm, opt; maxiters = 100, w = 0.7298f0, wdamp = 1.0f0, c1 
                                                     Ref{Float32}), s.h, maxiters, w, wdamp, c1, c2, ms))
     end
     return ms[]
+end
+
+"""Size, dimension, iterations run, seed and device bytes of a swarm (the cache's fields)."""
+function info(s::PPSSwarm)
+    r = Ref{PPSSwarmInfo}()
+    check(ccall((:pps_swarm_info_get, lib()), Cint, (Ptr{Cvoid}, Ref{PPSSwarmInfo}), s.h, r))
+    return r[]
+end
+
+"""The problem's objective at the rows of `X` (npoints x dim) on the device: prob.f(x, p) of a
+registered objective (src/solve.jl:54-57)."""
+function evaluate(prob, X::AbstractMatrix{<:Real})
+    cp, bufs = pps_problem(prob)
+    x = Matrix{Float32}(X)  # column-major npoints x dim = the dim-major layout of pps_eval_objective
+    f = Vector{Float32}(undef, size(x, 1))
+    GC.@preserve bufs x f check(ccall((:pps_eval_objective, lib()), Cint,
+                                      (Ref{PPSProblem}, Int64, Ptr{Float32}, Ptr{Float32}),
+                                      cp, size(x, 1), x, f))
+    return f
+end
+
+"""The synchronous run on device buffers the caller owns, for callers that cannot let the
+library allocate (CUDA.jl's pooled memory): `ds` describes them, `iteration` is the counter of
+the first step (0 after an init; add maxiters per call).  Returns (gcost, gidx) after waiting
+for `stream` (a CuStream's handle, or C_NULL for the default stream).  Calls share the
+library's static scratch (at most 2^20 particles) and must not overlap on the GPU."""
+function sync_run_noalloc!(objective::Integer, params::Vector{Float32}, ds::PPSDeviceSwarm; seed = 0,
+                           iteration = 0, maxiters = 100, w = 0.7298f0, wdamp = 1.0f0, c1 = 1.4962f0,
+                           c2 = 1.4962f0, gbest_from_position = false, stream::Ptr{Cvoid} = C_NULL)
+    gcost, gidx = Ref{Float32}(), Ref{Int64}()
+    check(ccall((:pps_sync_run_noalloc, lib()), Cint,
+                (Int32, Ptr{Float32}, Int32, Ref{PPSDeviceSwarm}, UInt64, UInt32, Int32, Float32, Float32, Float32,
+                 Float32, UInt32, Ptr{Cvoid}, Ref{Float32}, Ref{Int64}),
+                objective, params, length(params), ds, seed, iteration, maxiters, w, wdamp, c1, c2,
+                gbest_from_position ? UInt32(1) : UInt32(0), stream, gcost, gidx))
+    return gcost[], gidx[]
 end
 
 """solve(prob, alg) with alg.backend isa PPSBackend: the reference's solution fields (src/solve.jl:11-59)."""
@@ -316,6 +425,13 @@ function wait_result(srv::PPSServer, ticket::UInt64; timeout_s = 600.0)
     return u, cost[], idx[], lat[]
 end
 
+"""Requests submitted and completed, launches, solves/s and the p50 / p99 time to solution."""
+function serve_stats(srv::PPSServer)
+    r = Ref{PPSServeStats}()
+    check(ccall((:pps_serve_stats_get, lib()), Cint, (Ptr{Cvoid}, Ref{PPSServeStats}), srv.h, r))
+    return r[]
+end
+
 """Finish the queued and running requests and release the server."""
 function serve_stop!(srv::PPSServer)
     if srv.h != C_NULL
@@ -356,6 +472,11 @@ shard_bind!(s::PPSSwarm, record::Ptr, records::Ptr, nrecords::Integer) =
 shard_step!(s::PPSSwarm, first_of_run::Bool; w = 0.7298f0, wdamp = 1.0f0, c1 = 1.4962f0, c2 = 1.4962f0) =
     check(ccall((:pps_shard_step, lib()), Cint, (Ptr{Cvoid}, Int32, Float32, Float32, Float32, Float32), s.h,
                 first_of_run ? 1 : 0, w, wdamp, c1, c2))
+"""ParallelPSOKernel(global_update = false) on the shard: maxiters iterations in one launch, the
+record written after the last; exchange the records and `shard_apply!` once."""
+shard_async!(s::PPSSwarm, maxiters::Integer; w = 0.7298f0, wdamp = 1.0f0, c1 = 1.4962f0, c2 = 1.4962f0) =
+    check(ccall((:pps_shard_async, lib()), Cint, (Ptr{Cvoid}, Int32, Float32, Float32, Float32, Float32), s.h,
+                maxiters, w, wdamp, c1, c2))
 shard_apply!(s::PPSSwarm) = check(ccall((:pps_shard_apply, lib()), Cint, (Ptr{Cvoid},), s.h))
 shard_finish!(s::PPSSwarm) = check(ccall((:pps_shard_finish, lib()), Cint, (Ptr{Cvoid},), s.h))
 

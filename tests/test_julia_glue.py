@@ -10,8 +10,8 @@ ROOT = Path(__file__).resolve().parent.parent
 JL = ROOT / "parallelparticleswarms.jl_gb300" / "julia" / "PPSCUDA" / "src" / "PPSCUDA.jl"
 HEADER = ROOT / "include" / "pps.h"
 
-C_TO_JL = {"int32_t": "Int32", "int64_t": "Int64", "uint64_t": "UInt64", "float": "Float32", "double": "Float64",
-           "const float*": "Ptr{Float32}", "float*": "Ptr{Float32}"}
+C_TO_JL = {"int32_t": "Int32", "int64_t": "Int64", "uint32_t": "UInt32", "uint64_t": "UInt64", "float": "Float32",
+           "double": "Float64", "const float*": "Ptr{Float32}", "float*": "Ptr{Float32}"}
 
 
 def _c_struct(name):
@@ -23,9 +23,11 @@ def _c_struct(name):
         decl = decl.strip()
         if not decl:
             continue
-        m = re.match(r"(const float\*|float\*|int32_t|int64_t|uint64_t|float|double)\s+(\w+)$", decl)
+        m = re.match(r"(const float\*|float\*|int32_t|int64_t|uint32_t|uint64_t|float|double)\s+(\w+(?:\s*,\s*\w+)*)$",
+                     decl)
         assert m, decl
-        fields.append((m.group(2), C_TO_JL[m.group(1)]))
+        for name in m.group(2).split(","):  # one type, several declarators
+            fields.append((name.strip(), C_TO_JL[m.group(1)]))
     return fields
 
 
@@ -39,6 +41,9 @@ def test_structs_match_the_header():
     assert _jl_struct("PPSProblem") == _c_struct("pps_problem")
     assert _jl_struct("PPSLocalOpts") == _c_struct("pps_local_opts")
     assert _jl_struct("PPSServeConfig") == _c_struct("pps_serve_config")
+    assert _jl_struct("PPSServeStats") == _c_struct("pps_serve_stats")
+    assert _jl_struct("PPSSwarmInfo") == _c_struct("pps_swarm_info")
+    assert _jl_struct("PPSDeviceSwarm") == _c_struct("pps_device_swarm")
 
 
 def test_every_ccall_is_declared_and_exported(pps):
