@@ -337,34 +337,111 @@ function ode_params(u0, dt; method::Symbol = :rk4, nsteps = 0, save_every = 1, l
 end
 
 # ---------------------------------------------------------------- many solves
-"""Solve independent problems in one persistent launch (pps_batch_*); returns (u, cost) each."""
-function solve_many(probs, n; maxiters = 100, w = 0.7298f0, wdamp = 1.0f0, c1 = 1.4962f0, c2 = 1.4962f0)
-    b = Ref{Ptr{Cvoid}}(C_NULL)
-    check(ccall((:pps_batch_create, lib()), Cint, (Ref{Ptr{Cvoid}},), b))
-    keep = Any[]
-    slots = Int32[]
-    try
-        for (k, prob) in enumerate(probs)
-            cp, bufs = pps_problem(prob)
-            push!(keep, bufs)
-            slot = Ref{Int32}()
-            GC.@preserve bufs check(ccall((:pps_batch_add, lib()), Cint,
-                                          (Ptr{Cvoid}, Ref{PPSProblem}, Int64, UInt64, Int32, Float32, Float32,
-                                           Float32, Float32, Ref{Int32}),
-                                          b[], cp, n, k, maxiters, w, wdamp, c1, c2, slot))
-            push!(slots, slot[])
-        end
-        check(ccall((:pps_batch_run, lib()), Cint, (Ptr{Cvoid}, Ptr{Float32}), b[], C_NULL))
-        return map(zip(probs, slots)) do (prob, slot)
-            u = Vector{Float32}(undef, length(prob.u0))
-            cost = Ref{Float32}()
-            check(ccall((:pps_batch_result, lib()), Cint, (Ptr{Cvoid}, Int32, Ptr{Float32}, Ref{Float32}, Ptr{Int64}),
-                        b[], slot, u, cost, C_NULL))
-            (u, cost[])
-        end
-    finally
-        ccall((:pps_batch_destroy, lib()), Cint, (Ptr{Cvoid},), b[])
+"""Independent problems solved in one persistent launch (pps_batch_*): `add!` each, `run!`, then
+`result` / `state` per slot.  Each result equals the problem solved alone."""
+mutable struct PPSBatch
+    h::Ptr{Cvoid}
+    dims::Vector{Int}
+    ns::Vector{Int}
+end
+
+function PPSBatch()
+    out = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:pps_batch_create, lib()), Cint, (Ref{Ptr{Cvoid}},), out))
+    b = PPSBatch(out[], Int[], Int[])
+    finalizer(b) do x
+        x.h != C_NULL && ccall((:pps_batch_destroy, lib()), Cint, (Ptr{Cvoid},), x.h)
+        x.h = C_NULL
     end
+    return b
+end
+
+"""Queue one swarm; returns its slot."""
+function add!(b::PPSBatch, prob, n::Integer; maxiters = 100, seed = 0, w = 0.7298f0, wdamp = 1.0f0,
+              c1 = 1.4962f0, c2 = 1.4962f0)
+    cp, bufs = pps_problem(prob)
+    slot = Ref{Int32}()
+    GC.@preserve bufs check(ccall((:pps_batch_add, lib()), Cint,
+                                  (Ptr{Cvoid}, Ref{PPSProblem}, Int64, UInt64, Int32, Float32, Float32, Float32,
+                                   Float32, Ref{Int32}),
+                                  b.h, cp, n, seed, maxiters, w, wdamp, c1, c2, slot))
+    push!(b.dims, length(prob.u0))
+    push!(b.ns, Int(n))
+    return slot[]
+end
+
+"""Fix the block shape (threads in {128, 256, 512}, particles per thread in {1, 2}); (0, 0)
+returns to the autotuner."""
+set_shape!(b::PPSBatch, threads::Integer, ppt::Integer) =
+    check(ccall((:pps_batch_set_shape, lib()), Cint, (Ptr{Cvoid}, Int32, Int32), b.h, threads, ppt))
+
+"""Solve every queued swarm in one launch; returns the device time in ms."""
+function run!(b::PPSBatch)
+    ms = Ref{Float32}(0)
+    check(ccall((:pps_batch_run, lib()), Cint, (Ptr{Cvoid}, Ref{Float32}), b.h, ms))
+    return ms[]
+end
+
+"""(u, cost, index) of a slot's swarm after `run!`."""
+function result(b::PPSBatch, slot::Integer)
+    u = Vector{Float32}(undef, b.dims[slot + 1])
+    cost, idx = Ref{Float32}(), Ref{Int64}()
+    check(ccall((:pps_batch_result, lib()), Cint, (Ptr{Cvoid}, Int32, Ptr{Float32}, Ref{Float32}, Ref{Int64}),
+                b.h, slot, u, cost, idx))
+    return u, cost[], idx[]
+end
+
+"""A state field of a slot's swarm after `run!` (n x dim, or n for FIELD_PCOST / FIELD_COST)."""
+function state(b::PPSBatch, slot::Integer, field::Int32)
+    n, D = b.ns[slot + 1], b.dims[slot + 1]
+    out = field in (FIELD_PCOST, FIELD_COST) ? Vector{Float32}(undef, n) : Matrix{Float32}(undef, n, D)
+    check(ccall((:pps_batch_get_state, lib()), Cint, (Ptr{Cvoid}, Int32, Int32, Ptr{Float32}), b.h, slot, field,
+                out))
+    return out
+end
+
+"""(swarms, threads, particles per thread, device bytes) of the last run."""
+function batch_info(b::PPSBatch)
+    ns, t, ppt, bytes = Ref{Int32}(), Ref{Int32}(), Ref{Int32}(), Ref{UInt64}()
+    check(ccall((:pps_batch_info, lib()), Cint, (Ptr{Cvoid}, Ref{Int32}, Ref{Int32}, Ref{Int32}, Ref{UInt64}),
+                b.h, ns, t, ppt, bytes))
+    return Int(ns[]), Int(t[]), Int(ppt[]), Int(bytes[])
+end
+
+"""Solve independent problems in one persistent launch; returns (u, cost) each."""
+function solve_many(probs, n; maxiters = 100, w = 0.7298f0, wdamp = 1.0f0, c1 = 1.4962f0, c2 = 1.4962f0)
+    b = PPSBatch()
+    slots = [add!(b, prob, n; maxiters, seed = k, w, wdamp, c1, c2) for (k, prob) in enumerate(probs)]
+    run!(b)
+    return [result(b, slot)[1:2] for slot in slots]
+end
+
+# ---------------------------------------------------------------- device snapshots
+"""A device snapshot of a swarm's state field: the reference's `sol.original`, a new device array
+(src/solve.jl:51-56).  The swarm may run on or be destroyed while it lives; `read_copy` copies it
+to the host."""
+mutable struct PPSFieldCopy
+    h::Ptr{Cvoid}
+    n::Int
+    dim::Int
+    field::Int32
+end
+
+function snapshot(s::PPSSwarm, field::Int32 = FIELD_POSITION)
+    out = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:pps_field_copy_create, lib()), Cint, (Ptr{Cvoid}, Int32, Ref{Ptr{Cvoid}}), s.h, field, out))
+    c = PPSFieldCopy(out[], s.n, s.dim, field)
+    finalizer(c) do x
+        x.h != C_NULL && ccall((:pps_field_copy_destroy, lib()), Cint, (Ptr{Cvoid},), x.h)
+        x.h = C_NULL
+    end
+    return c
+end
+
+function read_copy(c::PPSFieldCopy)
+    out = c.field in (FIELD_PCOST, FIELD_COST) ? Vector{Float32}(undef, c.n) : Matrix{Float32}(undef, c.n, c.dim)
+    check(ccall((:pps_field_copy_read, lib()), Cint, (Ptr{Cvoid}, Ptr{Float32}), c.h, out))
+    return out
 end
 
 # ---------------------------------------------------------------- serving

@@ -1,7 +1,8 @@
 """The Julia glue package (parallelparticleswarms.jl_gb300/julia/PPSCUDA), checked
-without a Julia toolchain (none exists here): every entry point it ccalls is
-declared in include/pps.h and exported by libpps_cuda.so, and the structs it
-passes by reference have pps.h's fields in pps.h's order with matching types."""
+without a Julia toolchain (none exists here): it ccalls every entry point
+include/pps.h declares and nothing else, each one exported by libpps_cuda.so,
+and the structs it passes by reference have pps.h's fields in pps.h's order
+with matching types."""
 import re
 import subprocess
 from pathlib import Path
@@ -50,9 +51,9 @@ def test_every_ccall_is_declared_and_exported(pps):
     from parallelparticleswarms import _lib
 
     called = set(re.findall(r"ccall\(\(:(pps_\w+), lib\(\)\)", JL.read_text()))
-    assert len(called) >= 20
     declared = set(re.findall(r"PPS_API\s+[\w\s\*]+?\b(pps_\w+)\s*\(", HEADER.read_text()))
     assert called <= declared, sorted(called - declared)
+    assert declared <= called, ("entry points without a Julia binding", sorted(declared - called))
     out = subprocess.run(["nm", "-D", "--defined-only", str(_lib.LIB_PATH)], capture_output=True, text=True,
                          check=True).stdout
     assert called <= set(re.findall(r"\bT\s+(pps_\w+)", out))
